@@ -1,0 +1,76 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs oracle/_ref/ref_harness (the reference's own translation units plus a
+harness; build it with `make -C oracle ref`) on the configurations in
+tests/golden/cases/ and packs its outputs into compressed .npz files:
+
+  <case>.npz   step0_* initial state, gamma_k / axis_k (per-cell Gamma variate
+               and rotation axis the reference drew in step k), shift_k (grid
+               shift after step k), stepK_* dumped states, replay_ok.
+  mt.npz       MT19937 outputs of the reference's MTRand for a few seeds and
+               rgamma(Nc) samples (src/libcilia/mpcd.cpp:13-43).
+
+Usage: python tests/golden/make_golden.py   (needs the reference sources)
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
+
+# case name: (seed, steps, ststep, dump list)
+CASES = {
+    "fluid4": (11, 5, 0.002, "1,5"),
+    "fluid8": (7, 3, 0.002, "3"),
+    "clami10": (3, 4, 0.002, "4"),
+    "objects8": (3, 4, 0.002, "4"),
+}
+
+
+def run_case(name, seed, steps, ststep, dumps):
+    cfg = os.path.join(HERE, "cases", name + ".cfg")
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "out")
+        subprocess.run([HARNESS, "run", cfg, out, str(seed), str(steps), repr(ststep), dumps],
+                       check=True, stdout=subprocess.DEVNULL)
+        arrays = {}
+        with open(os.path.join(out, "index.txt")) as f:
+            for line in f:
+                parts = line.split()
+                shape = tuple(int(x) for x in parts[1:])
+                arrays[parts[0]] = np.fromfile(os.path.join(out, parts[0] + ".f64")).reshape(shape)
+    arrays["params"] = np.array([seed, steps, ststep], dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    return arrays
+
+
+def run_mt():
+    out = {}
+    for seed in (1, 5489, 4357):
+        txt = subprocess.run([HARNESS, "kat", str(seed), "2000"], check=True, capture_output=True, text=True).stdout
+        out[f"kat_{seed}"] = np.array([int(x) for x in txt.split()], dtype=np.uint64)
+    for nc in (2, 5, 10, 30):
+        txt = subprocess.run([HARNESS, "gamma", "42", str(nc), "500"], check=True, capture_output=True, text=True).stdout
+        out[f"gamma42_{nc}"] = np.array([float(x) for x in txt.split()])
+    np.savez_compressed(os.path.join(HERE, "mt.npz"), **out)
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference harness first: make -C oracle ref")
+    for name, (seed, steps, ststep, dumps) in CASES.items():
+        a = run_case(name, seed, steps, ststep, dumps)
+        print(name, "arrays:", len(a), "replay_ok:", a["replay_ok"][0])
+    run_mt()
+    print("mt.npz written")
+
+
+if __name__ == "__main__":
+    main()
