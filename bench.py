@@ -1,0 +1,315 @@
+"""Benchmark: MPCD particle-steps/s of the microswimmer hot path on GB300.
+
+Default workload (N = 1): `swimmer64` - 64^3 periodic cells x 10 fluid
+particles (2,621,440) plus a ciliated sphere (Clami, radius 8, 100 cilia of
+3 x 15 beads on a Fibonacci lattice; 5,143 beads), 50 MD velocity-Verlet
+substeps per MPC step, the plain float64 method.  One step = one full MPC
+step: collision, all MD substeps, grid shift, streaming and binning.
+
+value  : (fluid + beads) x steps / device time of the timed steps (CUDA events
+         on the engine's stream; the L2 is flushed between steps).
+e2e    : the same metric through the C ABI with host buffers: the fluid and
+         the swimmer are uploaded from host memory, every step reads the
+         observables back, the final state is downloaded; wall clock.
+roofline: the fluid collide+stream kernel against the measured HBM copy
+         bandwidth; algorithmic bytes per particle-step = read + write of the
+         particle state (float64: 6 x 8 B each way = 96 B; float32 split: 64 B).
+cpu_baseline: the C restatement of the reference (oracle/) with OpenMP on the
+         host cores, on a bounded sample of the same workload.
+
+--impl reference runs that CPU restatement alone (the reference's own
+sources are not available where this runs) and prints its line.
+Multi-GPU: replicas only - every rank advances its own independent box.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "multi-ciliated-microswimmers_gb300")
+for _p in (PKG, os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import simcfg  # noqa: E402
+
+METRIC = "MPCD particle-steps/s"
+UNIT = "particle-steps/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle sampling during the timed region."""
+
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def workload_cfg(name, seed):
+    cfg = simcfg.baseline_config(name, seed=seed)
+    cfg["seed"] = int(seed)
+    return cfg
+
+
+def describe(name, nf, nb, precision):
+    if name == "swimmer64":
+        geo = "64^3 cells x 10 fluid, Clami R=8 with 100 cilia (3x15 beads) on a Fibonacci lattice, 50 MD substeps"
+    elif name == "swimmer128":
+        geo = "128^3 cells x 10 fluid, Clami R=16 with 400 cilia (3x20 beads), 50 MD substeps"
+    else:
+        geo = f"{name}: periodic fluid, no swimmer"
+    return f"{name}: {geo}; {nf} fluid + {nb} beads; {precision}"
+
+
+# ------------------------------------------------------------------ GPU arm --
+
+def run_gpu(args, rank=0):
+    import cilia_gpu as cg
+
+    prec = cg.MPCD_FP64 if args.precision == "fp64" else cg.MPCD_FP32
+    cfg = workload_cfg(args.workload, seed=1000 + rank)
+    text = simcfg.dumps(cfg)
+    sim = cg.Sim(text, precision=prec, seed=1000 + rank, device=args.device)
+    eng = sim.engine
+    nf = len(eng.fluid()[1]) if args.verify_counts else int(cfg["sizex"]) ** 3 * 10
+    nb = sim.nbeads
+    ntot = nf + nb
+    eng.run(args.warmup)
+    eng.sync()
+    launches0 = eng.launch_count()
+    with ClockSampler(args.device) as clk:
+        step_ms = eng.timed_run(args.steps, flush_l2=True)
+    launches = eng.launch_count() - launches0
+    total_s = float(step_ms.sum()) / 1e3
+    value = ntot * args.steps / total_s
+    # per-kernel times on a short profiled run (events around every launch)
+    prof_steps = min(args.steps, 20)
+    eng.set_profiling(True)
+    eng.timed_run(prof_steps, flush_l2=True)
+    kt = {k: eng.kernel_time(i) for k, i in (("cell", cg.K_CELL), ("fluid", cg.K_FLUID), ("bead", cg.K_BEAD),
+                                              ("md", cg.K_MD), ("sort", cg.K_SORT))}
+    eng.set_profiling(False)
+    obs = eng.observables()
+    sim.close()
+    return dict(value=value, ms_per_step=1e3 * total_s / args.steps, nf=nf, nb=nb, kernels=kt,
+                launches=launches, clocks=clk.summary(), kT=obs["kT"], step_ms=step_ms, prof_steps=prof_steps)
+
+
+def run_e2e(args):
+    """Through the C ABI with host buffers: upload, K steps with an observables
+    read-back each, final download."""
+    import cilia_gpu as cg
+
+    prec = cg.MPCD_FP64 if args.precision == "fp64" else cg.MPCD_FP32
+    cfg = workload_cfg(args.workload, seed=77)
+    L = int(cfg["sizex"])
+    rng = np.random.default_rng(5)
+    nf = L ** 3 * 10
+    pos = rng.uniform(0, L, (nf, 3))
+    vel = rng.normal(size=(nf, 3))
+    vel -= vel.mean(axis=0)
+    sim = cg.Sim(simcfg.dumps(cfg), precision=prec, seed=77, create_fluid=False, device=args.device)
+    eng = sim.engine
+    nb = sim.nbeads
+    bpos, bvel = sim.beads()
+    t0 = time.perf_counter()
+    eng.set_fluid(pos, vel)
+    for _ in range(args.steps):
+        eng.step()
+        eng.observables()
+    p, v = eng.fluid()
+    bp, bv = sim.beads()
+    wall = time.perf_counter() - t0
+    sim.close()
+    h2d = (pos.nbytes + vel.nbytes) / args.steps
+    d2h = (p.nbytes + v.nbytes + bp.nbytes + bv.nbytes) / args.steps + 64
+    return dict(value=(nf + nb) * args.steps / wall, h2d=h2d, d2h=d2h)
+
+
+# ------------------------------------------------------------------ CPU arm --
+
+def run_cpu(args, budget_s=None, threads=None):
+    from oracle import build_from_cfg
+
+    cfg = workload_cfg(args.workload, seed=3)
+    threads = threads or os.cpu_count() or 1
+    s = build_from_cfg(cfg, seed=3)
+    s.set_threads(threads)
+    nf = s.fluid()[0].shape[0]
+    nb = s.bead_count()
+    budget = budget_s if budget_s is not None else args.cpu_budget
+    s.step()  # warm-up
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        s.step()
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= budget and n >= 2) or n >= args.steps:
+            break
+    return dict(value=(nf + nb) * n / el, steps=n, seconds=el, threads=threads, nf=nf, nb=nb)
+
+
+def clock_ok(c):
+    bad = {"hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown"}
+    return not (set(c.get("reasons", [])) & bad)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="swimmer64", choices=["swimmer64", "swimmer128", "plain32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--device", type=int, default=None)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--verify-counts", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.device is None:
+        args.device = local
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(args.device)
+        dist.init_process_group("nccl")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = run_cpu(args, budget_s=args.cpu_budget)
+        line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": r["steps"], "warmup": 1, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": describe(args.workload, r["nf"], r["nb"], "float64 CPU"),
+                                                "parallelism": f"openmp{r['threads']}"},
+                "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["threads"], "kind": "port",
+                                 "sample": f"{r['steps']} MPC steps of the full workload in {r['seconds']:.1f} s"},
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if dist is not None:
+        dist.barrier()
+    g = run_gpu(args, rank)
+    if not clock_ok(g["clocks"]):  # throttled: measure once more
+        g = run_gpu(args, rank)
+    value_rank = g["value"]
+    t_rank = g["ms_per_step"]
+    if dist is not None:
+        import torch
+
+        t = torch.tensor([t_rank], device=f"cuda:{args.device}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        value = (g["nf"] + g["nb"]) * world / (t_max / 1e3)
+        dist.barrier()
+    else:
+        t_max = t_rank
+        value = value_rank
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    bpp = 96 if args.precision == "fp64" else 64
+    fl_ms, fl_n = g["kernels"]["fluid"]
+    avg_fluid_ms = fl_ms / max(fl_n, 1)
+    achieved = g["nf"] * bpp / (avg_fluid_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+        "data": "synthetic",
+        "config": {"workload": describe(args.workload, g["nf"], g["nb"],
+                                        "float64 plain" if args.precision == "fp64" else "float32 split"),
+                   "l2": "flushed between timed steps (256 MB write, outside the timed events)",
+                   "parallelism": f"replicas{args.gpus}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "fluid_step (collide + stream + bin)",
+                     "bytes_per_particle_step": bpp, "avg_launch_ms": avg_fluid_ms},
+        "kernels_ms_per_step": {k: v[0] / max(g["prof_steps"], 1) for k, v in g["kernels"].items()},
+        "gpu_launches": g["launches"],
+        "clocks": g["clocks"],
+        "kT": g["kT"],
+    }
+    if not args.no_extra:
+        e = run_e2e(args)
+        line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                       "d2h_bytes_per_step": e["d2h"]}
+    if not args.no_cpu:
+        c = run_cpu(args)
+        line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",
+                                "sample": f"{c['steps']} MPC steps of {args.workload} ({c['nf']} fluid + "
+                                          f"{c['nb']} beads) in {c['seconds']:.1f} s, C restatement, OpenMP"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

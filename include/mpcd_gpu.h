@@ -1,0 +1,190 @@
+/* mpcd_gpu.h -- C ABI of the GB300 MPCD + microswimmer engine (libmpcd_gpu.so).
+ *
+ * One handle is one simulation box on one GPU: MPCD fluid particles, MD beads
+ * with their spring network, and the per-cell state of the SRD collision.
+ * The entry points replace the bodies of the reference's hot path:
+ *
+ *   mpcd_step           Simulation::next_tstep          (src/simulation.cpp:217-265)
+ *                       = MPCD::next_tstep (collision)  (src/libcilia/mpcd.cpp:140-247)
+ *                       + n x (md_loop*, recalc_forces) (src/libcilia/mdobject.cpp:36-72,
+ *                                                        src/simulation.cpp:202-215)
+ *                       + MPCD::shift_boxes             (src/libcilia/mpcd.cpp:249-253)
+ *                       + Fluid::move / md_loop_stop    (src/libcilia/fluid.cpp:152-167,
+ *                                                        src/libcilia/mpcd.cpp:340-394)
+ *                       + switch_logic                  (src/cilia.cpp:241-258,
+ *                                                        src/ConstantBeatCilia.cpp:8-23)
+ *   mpcd_set_fluid      Fluid::create / Fluid::load then add_impuls (src/libcilia/fluid.cpp:55-98,
+ *                       120-150, src/libcilia/mpcd.cpp:257-267)
+ *   mpcd_set_beads      MDObject::init (src/libcilia/mdobject.cpp:153-160)
+ *   mpcd_set_springs    the spring calls of Cilia::recalcforce/addcross, Sphere::recalcforce and
+ *                       Clami::global_forces (src/cilia.cpp:127-239, src/sphere.cpp:87-119,
+ *                       src/clami.cpp:188-198), flattened into one list
+ *   mpcd_set_cilia      per-cilium beat state (newlength/oldlength/midpnt/Tstroke, src/cilia.h:54-65)
+ *   mpcd_observables    MPCD::debug totals (src/libcilia/mpcd.cpp:404-467), Fluid::writedata
+ *                       (src/libcilia/fluid.cpp:169-207) and diss_energy_total
+ *   mpcd_get_shift /
+ *   mpcd_set_shift      MPCD::a, persisted in mpcd.dat (src/libcilia/mpcd.cpp:86-97, 396-403)
+ *
+ * Conventions: every function returns 0 on success or a positive MPCD_E* code;
+ * mpcd_last_error() gives the message.  No exception crosses the boundary.
+ * All pointers are HOST pointers; the library copies.  Arrays are row-major
+ * float64: positions and velocities are n x 3.  A handle must be used from one
+ * host thread at a time; it owns one CUDA stream.
+ */
+#ifndef MPCD_GPU_H
+#define MPCD_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPCD_OK 0
+#define MPCD_EINVAL 1   /* bad argument */
+#define MPCD_ECUDA 2    /* CUDA runtime error */
+#define MPCD_ESTATE 3   /* call out of order (e.g. stepping before set_fluid) */
+#define MPCD_EDEVICE 4  /* a device-side check failed (see mpcd_last_error) */
+#define MPCD_ENOMEM 5   /* device allocation failed */
+
+/* arithmetic of the fluid path */
+#define MPCD_FP64 0 /* plain: int cell + float64 in-cell offset, float64 velocities */
+#define MPCD_FP32 1 /* split: int cell + float32 in-cell offset, float32 velocities */
+
+/* boundary conditions along z (compile-time -DNOSLIP / -DSLIP in the reference) */
+#define MPCD_WALLS_NONE 0
+#define MPCD_WALLS_NOSLIP 1 /* bounce-back + virtual particles (src/libcilia/mpcd.cpp:175-198, 346-376) */
+#define MPCD_WALLS_SLIP 2
+
+typedef struct mpcd_engine mpcd_engine;
+
+typedef struct {
+  int sizes[3];          /* box edges in collision cells (cell size a = 1), each 2..1024 */
+  double tstep;          /* MPC time step h (wc.tstep) */
+  double ststep;         /* MD substep (World::ststep); substeps n = int((h + 1e-8) / ststep) */
+  int precision;         /* MPCD_FP64 or MPCD_FP32 */
+  int walls;             /* MPCD_WALLS_* */
+  double gravity;        /* body-force amplitude along x (FLUID_FLOW_G); 0 = off */
+  double omega;          /* body force ~ gravity * cos(omega * t) (src/libcilia/fluid.cpp:156-158) */
+  double bead_mass;      /* collision mass of MD beads (MDObject::partmass = 5) */
+  unsigned long long seed; /* counter-based generator seed for free-running steps */
+  int device;            /* CUDA device ordinal */
+  int sort_interval;     /* reorder particles by cell every this many steps (0 = auto) */
+} mpcd_params;
+
+/* Values that replace the generator for one step (all host arrays).  Used to
+ * reproduce a run of the reference exactly: the grid shift drawn after the
+ * collision, and for every cell the Gamma variate (rgamma, used only when the
+ * cell holds more than one particle and positive relative kinetic energy) and
+ * the unit rotation axis. */
+typedef struct {
+  const double* shift_next; /* [3], in (0,1): MPCD::a after shift_boxes */
+  const double* gamma;      /* [ncells]; < 0 where the reference drew none */
+  const double* axis;       /* [ncells][3] */
+} mpcd_inject;
+
+typedef struct {
+  double momentum[3];  /* total momentum / total mass, fluid + beads */
+  double n;            /* particles counted (fluid + beads) */
+  double mass;         /* total mass */
+  double kT;           /* sum m v^2 / (3 N) over fluid + beads (mpcd.san) */
+  double fluid_T;      /* sum v^2 / (3 N_fluid) over fluid (temp.san) */
+  double diss_energy;  /* MPCD::diss_energy_total since the last reset */
+  double globalt;      /* simulation time */
+  double energy_fluid; /* sum m v^2 / 2 over fluid, float64 */
+} mpcd_obs;
+
+/* lifecycle */
+int mpcd_create(const mpcd_params* params, mpcd_engine** out);
+int mpcd_destroy(mpcd_engine* h);
+const char* mpcd_last_error(const mpcd_engine* h);
+long mpcd_cell_count(const mpcd_engine* h);
+
+/* fluid (mass 1): n x 3 positions (any periodic image) and velocities */
+int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel);
+/* positions come back wrapped into [0, L) */
+int mpcd_get_fluid(mpcd_engine* h, long n, double* pos, double* vel);
+long mpcd_fluid_count(const mpcd_engine* h);
+
+/* grid shift and simulation time */
+int mpcd_set_shift(mpcd_engine* h, const double* a3);
+int mpcd_get_shift(mpcd_engine* h, double* a3);
+int mpcd_set_time(mpcd_engine* h, double globalt);
+int mpcd_get_time(mpcd_engine* h, double* globalt);
+
+/* MD beads, in md_objects order (rod-major).  moves[i] = 0 for beads below an
+ * object's startidx: they exert forces but are neither integrated nor binned. */
+int mpcd_set_beads(mpcd_engine* h, long nb, const double* pos, const double* vel, const int* moves);
+int mpcd_get_beads(mpcd_engine* h, long nb, double* pos, double* vel);
+
+/* Spring kinds.  Every entry is one-sided: the force acts on `target` only,
+ * F = -2 k (1 - b / |d|) d with d = x_target - x_other (MDObject::spring,
+ * src/libcilia/mdobject.cpp:8-17).  The rest length b is
+ *   MPCD_SPRING_CONST   : rest[i]
+ *   MPCD_SPRING_GUARDED : rest[i], and F = 0 when |d| == 0 (vector form, mdobject.cpp:19-29)
+ *   MPCD_SPRING_BOND    : newlength[ref[i]] of the cilium bond table
+ *   MPCD_SPRING_DIAG    : sqrt(0.5^2 + 0.5 * newlength[ref[i]]) (cilia.cpp:153, 179)
+ * A bead sums its springs in list order, as the reference does. */
+#define MPCD_SPRING_CONST 0
+#define MPCD_SPRING_GUARDED 1
+#define MPCD_SPRING_BOND 2
+#define MPCD_SPRING_DIAG 3
+int mpcd_set_springs(mpcd_engine* h, long ns, const int* target, const int* other, const int* kind,
+                     const int* ref, const double* rest, const double* k);
+
+/* Cilia with an active beat (Cilia / ConstantBeatCilia).  bond_base indexes the
+ * newlength/oldlength tables (rodlength entries per cilium). */
+#define MPCD_CILIUM_BASIC 0    /* Cilia::switch_logic (curvature-triggered) */
+#define MPCD_CILIUM_CONSTANT 1 /* ConstantBeatCilia::switch_logic (time-driven) */
+typedef struct {
+  int kind;
+  int rodlength;
+  int num_anker;
+  int bead0;     /* bead index of (filament 0, bead 0); filaments f at bead0 + f*rodlength */
+  int bond_base; /* first entry of this cilium in the newlength/oldlength tables */
+  double beatstrength, bending, max_bend, m_speed;
+  double power_stroke_duration, recovery_stroke_duration;
+  double start;   /* = num_anker */
+  double midpnt;  /* beat state */
+  double tstroke; /* Tstroke */
+} mpcd_cilium;
+/* newlength/oldlength: the bond tables (sum of rodlength entries) */
+int mpcd_set_cilia(mpcd_engine* h, int nc, const mpcd_cilium* cilia, const double* newlength,
+                   const double* oldlength);
+/* out: per cilium [midpnt, tstroke]; newlength/oldlength tables may be NULL */
+int mpcd_get_cilia(mpcd_engine* h, int nc, double* state2, double* newlength, double* oldlength);
+
+/* bins fluid and beads with the current shift (end of Simulation's constructor) */
+int mpcd_prepare(mpcd_engine* h);
+
+/* one MPC step; inj may be NULL (counter-based generator) */
+int mpcd_step(mpcd_engine* h, const mpcd_inject* inj);
+/* nsteps free-running MPC steps; observables read back only at the end */
+int mpcd_run(mpcd_engine* h, int nsteps);
+int mpcd_observables(mpcd_engine* h, mpcd_obs* out);
+int mpcd_reset_diss(mpcd_engine* h);
+/* waits for the handle's stream; reports device-side errors */
+int mpcd_sync(mpcd_engine* h);
+
+/* kernel launches issued by this handle so far (for accounting) */
+long long mpcd_launch_count(const mpcd_engine* h);
+
+/* Timing on the handle's stream.  Runs nsteps free-running steps, each
+ * bracketed by CUDA events; with flush_l2 != 0 a 256 MB scratch buffer is
+ * written between steps (outside the timed pairs) so that every step starts
+ * with a cold L2.  step_ms (may be NULL) receives each step's device time. */
+int mpcd_timed_run(mpcd_engine* h, int nsteps, int flush_l2, double* step_ms);
+
+/* Per-kernel device times: with profiling on, every launch is bracketed by
+ * events.  kernel: MPCD_K_* ; returns total milliseconds and launch count
+ * since profiling was switched on. */
+#define MPCD_K_CELL 0   /* cell_params: collision maps */
+#define MPCD_K_FLUID 1  /* fluid_step: collide + stream + bin */
+#define MPCD_K_BEAD 2   /* bead_collide */
+#define MPCD_K_MD 3     /* md: all substeps */
+#define MPCD_K_SORT 4   /* counting-sort reorder */
+int mpcd_set_profiling(mpcd_engine* h, int on);
+int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPCD_GPU_H */

@@ -1,0 +1,324 @@
+"""ctypes binding of libmpcd_gpu.so (include/mpcd_gpu.h, include/cilia_host.h).
+
+`Engine` wraps one mpcd_engine (a box of MPCD fluid plus MD beads on the GPU);
+`Sim` wraps one cilia_sim (the reference's Simulation built from a sim.cfg).
+There is no CPU fallback: if the library or a GPU is missing, construction
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libmpcd_gpu.so")
+
+MPCD_FP64, MPCD_FP32 = 0, 1
+WALLS_NONE, WALLS_NOSLIP, WALLS_SLIP = 0, 1, 2
+SPRING_CONST, SPRING_GUARDED, SPRING_BOND, SPRING_DIAG = 0, 1, 2, 3
+CILIUM_BASIC, CILIUM_CONSTANT = 0, 1
+K_CELL, K_FLUID, K_BEAD, K_MD, K_SORT = 0, 1, 2, 3, 4
+
+_D = ctypes.c_double
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+
+
+class MpcdParams(ctypes.Structure):
+    _fields_ = [("sizes", ctypes.c_int * 3), ("tstep", _D), ("ststep", _D), ("precision", ctypes.c_int),
+                ("walls", ctypes.c_int), ("gravity", _D), ("omega", _D), ("bead_mass", _D),
+                ("seed", ctypes.c_ulonglong), ("device", ctypes.c_int), ("sort_interval", ctypes.c_int)]
+
+
+class MpcdInject(ctypes.Structure):
+    _fields_ = [("shift_next", _DP), ("gamma", _DP), ("axis", _DP)]
+
+
+class MpcdObs(ctypes.Structure):
+    _fields_ = [("momentum", _D * 3), ("n", _D), ("mass", _D), ("kT", _D), ("fluid_T", _D),
+                ("diss_energy", _D), ("globalt", _D), ("energy_fluid", _D)]
+
+
+class MpcdCilium(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("rodlength", ctypes.c_int), ("num_anker", ctypes.c_int),
+                ("bead0", ctypes.c_int), ("bond_base", ctypes.c_int), ("beatstrength", _D), ("bending", _D),
+                ("max_bend", _D), ("m_speed", _D), ("power_stroke_duration", _D),
+                ("recovery_stroke_duration", _D), ("start", _D), ("midpnt", _D), ("tstroke", _D)]
+
+
+class CiliaOptions(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("device", ctypes.c_int), ("seed", ctypes.c_ulonglong),
+                ("ststep", _D), ("create_fluid", ctypes.c_int), ("read_files", ctypes.c_int),
+                ("walls", ctypes.c_int), ("gravity", _D), ("bead_mass", _D), ("sort_interval", ctypes.c_int)]
+
+
+class MpcdError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load libmpcd_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MpcdError(f"{LIB_PATH} not built: run build.py (or __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        sig = {
+            "mpcd_create": (ctypes.c_int, [ctypes.POINTER(MpcdParams), ctypes.POINTER(P)]),
+            "mpcd_destroy": (ctypes.c_int, [P]),
+            "mpcd_last_error": (ctypes.c_char_p, [P]),
+            "mpcd_cell_count": (ctypes.c_long, [P]),
+            "mpcd_set_fluid": (ctypes.c_int, [P, ctypes.c_long, _DP, _DP]),
+            "mpcd_get_fluid": (ctypes.c_int, [P, ctypes.c_long, _DP, _DP]),
+            "mpcd_fluid_count": (ctypes.c_long, [P]),
+            "mpcd_set_shift": (ctypes.c_int, [P, _DP]),
+            "mpcd_get_shift": (ctypes.c_int, [P, _DP]),
+            "mpcd_set_time": (ctypes.c_int, [P, _D]),
+            "mpcd_get_time": (ctypes.c_int, [P, _DP]),
+            "mpcd_set_beads": (ctypes.c_int, [P, ctypes.c_long, _DP, _DP, _IP]),
+            "mpcd_get_beads": (ctypes.c_int, [P, ctypes.c_long, _DP, _DP]),
+            "mpcd_set_springs": (ctypes.c_int, [P, ctypes.c_long, _IP, _IP, _IP, _IP, _DP, _DP]),
+            "mpcd_set_cilia": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdCilium), _DP, _DP]),
+            "mpcd_get_cilia": (ctypes.c_int, [P, ctypes.c_int, _DP, _DP, _DP]),
+            "mpcd_prepare": (ctypes.c_int, [P]),
+            "mpcd_step": (ctypes.c_int, [P, ctypes.POINTER(MpcdInject)]),
+            "mpcd_run": (ctypes.c_int, [P, ctypes.c_int]),
+            "mpcd_observables": (ctypes.c_int, [P, ctypes.POINTER(MpcdObs)]),
+            "mpcd_reset_diss": (ctypes.c_int, [P]),
+            "mpcd_sync": (ctypes.c_int, [P]),
+            "mpcd_launch_count": (ctypes.c_longlong, [P]),
+            "mpcd_timed_run": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, _DP]),
+            "mpcd_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
+            "mpcd_kernel_time": (ctypes.c_int, [P, ctypes.c_int, _DP, ctypes.POINTER(ctypes.c_longlong)]),
+            "cilia_sim_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
+                                                ctypes.POINTER(P)]),
+            "cilia_sim_destroy": (ctypes.c_int, [P]),
+            "cilia_sim_last_error": (ctypes.c_char_p, [P]),
+            "cilia_sim_engine": (P, [P]),
+            "cilia_sim_num_objects": (ctypes.c_int, [P]),
+            "cilia_sim_object_info": (ctypes.c_int, [P, ctypes.c_int, _IP, ctypes.c_char_p, ctypes.c_int]),
+            "cilia_sim_bead_count": (ctypes.c_long, [P]),
+            "cilia_sim_next_tstep": (ctypes.c_int, [P, ctypes.POINTER(MpcdInject)]),
+            "cilia_sim_run": (ctypes.c_int, [P]),
+            "cilia_sim_save": (ctypes.c_int, [P]),
+            "cilia_sim_write_cfg": (ctypes.c_int, [P, ctypes.c_char_p]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_DP)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Engine:
+    """One MPCD box with MD beads on the GPU (mpcd_engine)."""
+
+    def __init__(self, L, *, tstep=0.1, ststep=0.001, precision=MPCD_FP64, walls=WALLS_NONE, gravity=0.0,
+                 omega=0.0, bead_mass=5.0, seed=1, device=0, sort_interval=0, _handle=None, _owner=None):
+        self._owner = _owner
+        if _handle is not None:
+            self._h = _handle
+            self._owns = False
+        else:
+            if isinstance(L, int):
+                L = (L, L, L)
+            p = MpcdParams()
+            p.sizes[:] = [int(x) for x in L]
+            p.tstep, p.ststep, p.precision, p.walls = tstep, ststep, precision, walls
+            p.gravity, p.omega, p.bead_mass, p.seed = gravity, omega, bead_mass, seed
+            p.device, p.sort_interval = device, sort_interval
+            h = ctypes.c_void_p()
+            rc = lib().mpcd_create(ctypes.byref(p), ctypes.byref(h))
+            if rc:
+                raise MpcdError(f"mpcd_create failed with code {rc}")
+            self._h = h
+            self._owns = True
+
+    def close(self):
+        if getattr(self, "_owns", False) and self._h:
+            lib().mpcd_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _ck(self, rc, what):
+        if rc:
+            msg = lib().mpcd_last_error(self._h)
+            raise MpcdError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def ncell(self):
+        return lib().mpcd_cell_count(self._h)
+
+    def set_fluid(self, pos, vel):
+        pos, vel = _f64(pos), _f64(vel)
+        self._ck(lib().mpcd_set_fluid(self._h, pos.shape[0], _dp(pos), _dp(vel)), "set_fluid")
+
+    def fluid(self):
+        n = lib().mpcd_fluid_count(self._h)
+        pos = np.zeros((n, 3))
+        vel = np.zeros((n, 3))
+        self._ck(lib().mpcd_get_fluid(self._h, n, _dp(pos), _dp(vel)), "get_fluid")
+        return pos, vel
+
+    @property
+    def shift(self):
+        a = np.zeros(3)
+        self._ck(lib().mpcd_get_shift(self._h, _dp(a)), "get_shift")
+        return a
+
+    @shift.setter
+    def shift(self, a):
+        a = _f64(a)
+        self._ck(lib().mpcd_set_shift(self._h, _dp(a)), "set_shift")
+
+    @property
+    def time(self):
+        t = ctypes.c_double()
+        self._ck(lib().mpcd_get_time(self._h, ctypes.byref(t)), "get_time")
+        return t.value
+
+    @time.setter
+    def time(self, t):
+        self._ck(lib().mpcd_set_time(self._h, float(t)), "set_time")
+
+    def set_beads(self, pos, vel, moves=None):
+        pos, vel = _f64(pos), _f64(vel)
+        mv = None if moves is None else np.ascontiguousarray(moves, dtype=np.int32)
+        self._ck(lib().mpcd_set_beads(self._h, pos.shape[0], _dp(pos), _dp(vel),
+                                      None if mv is None else mv.ctypes.data_as(_IP)), "set_beads")
+
+    def beads(self, n):
+        pos = np.zeros((n, 3))
+        vel = np.zeros((n, 3))
+        self._ck(lib().mpcd_get_beads(self._h, n, _dp(pos), _dp(vel)), "get_beads")
+        return pos, vel
+
+    def prepare(self):
+        self._ck(lib().mpcd_prepare(self._h), "prepare")
+
+    def step(self, shift_next=None, gamma=None, axis=None):
+        if shift_next is None and gamma is None and axis is None:
+            self._ck(lib().mpcd_step(self._h, None), "step")
+            return
+        keep = [_f64(shift_next), _f64(gamma), _f64(axis)]
+        inj = MpcdInject(_dp(keep[0]), _dp(keep[1]), _dp(keep[2]))
+        self._ck(lib().mpcd_step(self._h, ctypes.byref(inj)), "step")
+
+    def run(self, nsteps):
+        self._ck(lib().mpcd_run(self._h, int(nsteps)), "run")
+
+    def sync(self):
+        self._ck(lib().mpcd_sync(self._h), "sync")
+
+    def observables(self):
+        o = MpcdObs()
+        self._ck(lib().mpcd_observables(self._h, ctypes.byref(o)), "observables")
+        return dict(momentum=np.array(o.momentum[:]), n=o.n, mass=o.mass, kT=o.kT, fluid_T=o.fluid_T,
+                    diss_energy=o.diss_energy, globalt=o.globalt, energy_fluid=o.energy_fluid)
+
+    def reset_diss(self):
+        self._ck(lib().mpcd_reset_diss(self._h), "reset_diss")
+
+    def launch_count(self):
+        return lib().mpcd_launch_count(self._h)
+
+    def timed_run(self, nsteps, flush_l2=True):
+        """Device time of each of `nsteps` free-running steps (ms)."""
+        out = np.zeros(max(int(nsteps), 1))
+        self._ck(lib().mpcd_timed_run(self._h, int(nsteps), int(flush_l2), _dp(out)), "timed_run")
+        return out[: int(nsteps)]
+
+    def set_profiling(self, on=True):
+        self._ck(lib().mpcd_set_profiling(self._h, int(on)), "set_profiling")
+
+    def kernel_time(self, kernel):
+        """(total ms, launches) of one kernel class since profiling started."""
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        self._ck(lib().mpcd_kernel_time(self._h, int(kernel), ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
+        return ms.value, n.value
+
+
+class Sim:
+    """The reference's Simulation on the GPU (cilia_sim), from cfg text or a path."""
+
+    def __init__(self, cfg, *, is_text=True, precision=MPCD_FP64, seed=1, ststep=0.0, create_fluid=True,
+                 read_files=False, walls=WALLS_NONE, gravity=0.0, bead_mass=5.0, device=0, sort_interval=0):
+        o = CiliaOptions(precision, device, seed, ststep, int(create_fluid), int(read_files), walls, gravity,
+                         bead_mass, sort_interval)
+        h = ctypes.c_void_p()
+        rc = lib().cilia_sim_create(cfg.encode() if isinstance(cfg, str) else cfg, int(is_text),
+                                    ctypes.byref(o), ctypes.byref(h))
+        if rc:
+            msg = lib().cilia_sim_last_error(None)
+            raise MpcdError(f"cilia_sim_create failed ({rc}): {msg.decode() if msg else ''}")
+        self._h = h
+        self.engine = Engine(None, _handle=lib().cilia_sim_engine(h), _owner=self)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cilia_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _ck(self, rc, what):
+        if rc:
+            msg = lib().cilia_sim_last_error(self._h)
+            raise MpcdError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def num_objects(self):
+        return lib().cilia_sim_num_objects(self._h)
+
+    def object_info(self, i):
+        info = (ctypes.c_int * 5)()
+        name = ctypes.create_string_buffer(256)
+        self._ck(lib().cilia_sim_object_info(self._h, i, info, name, 256), "object_info")
+        return dict(rods=info[0], len=info[1], startidx=info[2], offset=info[3],
+                    type=["Sphere", "Cilia", "ConstantBeatCilia", "Clami"][info[4]], name=name.value.decode())
+
+    @property
+    def nbeads(self):
+        return lib().cilia_sim_bead_count(self._h)
+
+    def beads(self):
+        return self.engine.beads(self.nbeads)
+
+    def next_tstep(self, shift_next=None, gamma=None, axis=None):
+        if shift_next is None and gamma is None and axis is None:
+            self._ck(lib().cilia_sim_next_tstep(self._h, None), "next_tstep")
+            return
+        keep = [_f64(shift_next), _f64(gamma), _f64(axis)]
+        inj = MpcdInject(_dp(keep[0]), _dp(keep[1]), _dp(keep[2]))
+        self._ck(lib().cilia_sim_next_tstep(self._h, ctypes.byref(inj)), "next_tstep")
+
+    def run(self):
+        self._ck(lib().cilia_sim_run(self._h), "run")
+
+    def save(self):
+        self._ck(lib().cilia_sim_save(self._h), "save")
+
+    def write_cfg(self, path):
+        self._ck(lib().cilia_sim_write_cfg(self._h, path.encode()), "write_cfg")

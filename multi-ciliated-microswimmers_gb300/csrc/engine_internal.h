@@ -1,0 +1,137 @@
+// Internal interfaces between the C-ABI host code (engine.cu) and the kernel
+// translation units (fluid_kernels.cu, md_kernels.cu).
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "mpcd_device.cuh"
+
+namespace mpcd {
+
+// ---------------------------------------------------------------- fluid ---
+// Plain (float64) fluid, structure of arrays.  Position = packed cell +
+// in-cell offset in [0,1) per axis.
+struct FluidF64 {
+  long n = 0;
+  uint32_t* cell = nullptr;
+  double *ox = nullptr, *oy = nullptr, *oz = nullptr;
+  double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+};
+
+// Split-precision fluid: pos = {ox, oy, oz, cell bits}, vel = {vx, vy, vz, 0}.
+struct FluidF32 {
+  long n = 0;
+  float4* pos = nullptr;
+  float4* vel = nullptr;
+};
+
+// Per-cell state.  sum: (P_x, P_y, P_z, K) mass-weighted; cnt: fluid count in
+// the low 16 bits, bead count in the high 16 bits.  par: collision map
+// v' = A v + b, stored as A (row-major 3x3) then b (12 values per cell).
+struct CellsF64 {
+  long ncell = 0;
+  double4* sum = nullptr;
+  uint32_t* cnt = nullptr;
+  double* par = nullptr;
+};
+struct CellsF32 {
+  long ncell = 0;
+  float4* sum = nullptr;
+  uint32_t* cnt = nullptr;
+  float4* par = nullptr;  // 3 float4 per cell: (A row 0, b0), (A row 1, b1), (A row 2, b2)
+};
+
+// Per-step scalars for the fluid kernels.
+struct StepArgs {
+  Box box;
+  double ta_cur[3];   // 1 - a for the shift used by this collision
+  double ta_next[3];  // 1 - a for the shift drawn after the MD loop
+  double a_cur[3];
+  double a_next[3];
+  double h;           // MPC time step
+  double gkick;       // gravity * cos(omega t) * h, added to v_x after streaming
+  int walls;          // MPCD_WALLS_*
+  double bead_mass;
+  uint64_t seed;
+  uint64_t step;      // index of this collision step (generator counter)
+  const double* inj_gamma;  // device, or nullptr
+  const double* inj_axis;   // device, or nullptr
+  unsigned* err;
+  double* diss;       // accumulated dissipated energy (float64)
+};
+
+// ------------------------------------------------------------------- MD ---
+struct CiliumDev {
+  int kind, len, num_anker, slot0, bond_base;
+  double beatstrength, bending, max_bend, m_speed, power_dur, recovery_dur, start;
+};
+
+// Beads live in "slots": the MD kernel runs one thread per slot, a tile of
+// slots per CTA, and every cilium lies inside one tile so that its beat
+// bookkeeping needs no grid-wide synchronisation.
+struct MDState {
+  int nslots = 0;        // tiles * tile_size
+  int tile = 0;          // threads per CTA
+  int ntiles = 0;
+  double* x[2] = {nullptr, nullptr};
+  double* y[2] = {nullptr, nullptr};
+  double* z[2] = {nullptr, nullptr};
+  double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+  int* moves = nullptr;  // 1 integrated + binned, 0 fixed, 2 helper, -1 empty slot
+  int* prim = nullptr;   // helper slot -> primary slot of its bead; primary -> itself
+  int* nhelp = nullptr;  // primary slot -> number of helper slots following it
+  int* tile_help = nullptr;  // per tile: 1 if it holds helper slots
+  // springs in CSR by target slot
+  int* sp_start = nullptr;
+  int* sp_other = nullptr;
+  int* sp_kind = nullptr;
+  int* sp_ref = nullptr;
+  double* sp_rest = nullptr;
+  double* sp_m2k = nullptr;  // -2k
+  // cilia
+  int ncil = 0;
+  CiliumDev* cil = nullptr;
+  double* midpnt = nullptr;
+  double* tstroke = nullptr;
+  double* newlen = nullptr;
+  double* oldlen = nullptr;
+  int* tile_cil = nullptr;  // ntiles + 1 offsets into cil (cilia sorted by tile)
+  GridBarrier bar{nullptr, nullptr};
+};
+
+struct MDStepArgs {
+  double t0, dt, tstep;
+  int n;
+  Box box;
+  double a_cur[3], a_next[3];
+  double bead_mass;
+  unsigned* err;
+};
+
+// ------------------------------------------------------------ launchers ---
+// All launchers enqueue on `s` and return the number of kernel launches.
+int launch_cell_params_f64(const CellsF64& c, const StepArgs& a, cudaStream_t s);
+int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s);
+int launch_bin_fluid_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s);
+int launch_bead_collide_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s);
+int launch_bin_beads_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s);
+int launch_md_f64(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+// reduce observables: out[0..2] sum m v, out[3] sum m v^2 (all), out[4] N, out[5] M,
+// out[6] sum v^2 over fluid, out[7] N fluid
+int launch_observables_f64(const FluidF64& f, const MDState& m, double bead_mass, double* out, cudaStream_t s);
+// counting sort of the fluid by cell; `tmp` has the same shape as `f`
+int launch_sort_f64(FluidF64& f, FluidF64& tmp, const Box& box, uint32_t* count, uint32_t* start,
+                    uint32_t* rank, uint32_t* blocksums, cudaStream_t s);
+
+int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s);
+int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s);
+int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s);
+int launch_bead_collide_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);
+int launch_bin_beads_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);
+int launch_md_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+int launch_observables_f32(const FluidF32& f, const MDState& m, double bead_mass, double* out, cudaStream_t s);
+int launch_sort_f32(FluidF32& f, FluidF32& tmp, const Box& box, uint32_t* count, uint32_t* start,
+                    uint32_t* rank, uint32_t* blocksums, cudaStream_t s);
+
+}  // namespace mpcd

@@ -1,0 +1,746 @@
+// MPCD fluid kernels: per-cell collision maps, fused collide + stream + bin,
+// bead coupling, observables and the periodic counting-sort reorder.
+//
+// One MPC step of the fluid (src/libcilia/mpcd.cpp:140-247 collision,
+// src/libcilia/fluid.cpp:152-167 + mpcd.cpp:340-394 streaming, mpcd.cpp:257-267
+// binning) is two kernels:
+//   cell_params : per cell, from the sums binned at the end of the previous step:
+//                 u = P/M, E_rel = K - M u^2, thermostat factor sc, rotation R,
+//                 and the affine collision map v' = A v + b (A = sc R, b = u - A u);
+//                 clears the sums for the next step.
+//   fluid_step  : per particle: v' = A v + b with the map of its shifted cell,
+//                 x' = x + v' h with periodic wrap, bin into the next shifted cell
+//                 (atomic sums).  One read and one write of the particle state.
+#include <cstdio>
+
+#include "engine_internal.h"
+
+namespace mpcd {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int grid_for(long n, int threads = kThreads) {
+  long g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > 152L * 64) g = 152L * 64;  // grid-stride beyond this
+  return (int)g;
+}
+
+__device__ __forceinline__ double block_sum_f64(double v) {
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+// shifted cell along one axis from the cell index and the in-cell offset:
+// floor(i + o + a) = i + (o >= 1 - a), compared on the IEEE bit patterns
+// (both operands are non-negative doubles, so integer order = numeric order)
+__device__ __forceinline__ int shifted(int i, double o, long long ta_bits, int L) {
+  int s = i + (__double_as_longlong(o) >= ta_bits ? 1 : 0);
+  return s == L ? 0 : s;
+}
+
+// reduce an offset that left [0,1) back into the cell (rare path)
+__device__ __forceinline__ void rewrap(double& o, int& i, int L) {
+  long long b = __double_as_longlong(o);
+  if (b < 0 || b >= 0x3FF0000000000000LL) {
+    double fl = floor(o);
+    o -= fl;
+    i += (int)fl;
+    if (o >= 1.0) {  // o was a tiny negative number: o - floor(o) rounded to 1
+      o = 0.0;
+      i += 1;
+    }
+    i %= L;
+    if (i < 0) i += L;
+  }
+}
+
+// the reference's cell of an unwrapped coordinate: floor(x+a) - floor((x+a)/L) L
+__device__ __forceinline__ int ref_cell_axis(double x, double a, int L) {
+  double xa = x + a;
+  int c = (int)(floor(xa) - floor(xa / L) * L);
+  if (c < 0) c += L;  // guards the rounding edge where (x+a)/L rounds up to an integer
+  if (c >= L) c -= L;
+  return c;
+}
+
+__device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, const StepArgs& a, double* A,
+                                              double* b, double& ldiss, unsigned& errbits, bool& gfail) {
+  const int nf = cnt_fluid(w), nb = cnt_beads(w);
+  const int num = nf + nb;
+  const double M = (double)nf + (double)nb * a.bead_mass;
+  const double ux = s.x / M, uy = s.y / M, uz = s.z / M;
+  const double erel = s.w - (ux * ux + uy * uy + uz * uz) * M;
+  double sc = 1.0;
+  if (erel > 0 && num > 1) {
+    double g;
+    if (a.inj_gamma) {
+      g = a.inj_gamma[cid];
+      if (g < 0) {
+        errbits |= kErrGammaMissing;
+        g = 0.0;
+      }
+    } else {
+      g = (double)gamma_mt(num, a.seed, a.step, (uint32_t)cid, &gfail);
+    }
+    sc = sqrt(g / (erel * 0.5));
+  }
+  double rx, ry, rz;
+  if (a.inj_axis) {
+    rx = a.inj_axis[3 * cid + 0];
+    ry = a.inj_axis[3 * cid + 1];
+    rz = a.inj_axis[3 * cid + 2];
+  } else {
+    random_axis(a.seed, a.step, (uint32_t)cid, rx, ry, rz);
+  }
+  const double ca = kCosAlpha, sa = kSinAlpha, oc = 1.0 - kCosAlpha;
+  // rotation about (rx, ry, rz) by alpha, entries as src/libcilia/mpcd.cpp:285-293
+  const double R00 = rx * rx + (1.0 - rx * rx) * ca;
+  const double R01 = rx * ry * oc - rz * sa;
+  const double R02 = rx * rz * oc + ry * sa;
+  const double R10 = rx * ry * oc + rz * sa;
+  const double R11 = ry * ry + (1.0 - ry * ry) * ca;
+  const double R12 = ry * rz * oc - rx * sa;
+  const double R20 = rx * rz * oc - ry * sa;
+  const double R21 = ry * rz * oc + rx * sa;
+  const double R22 = rz * rz + (1.0 - rz * rz) * ca;
+  A[0] = R00 * sc;
+  A[1] = R01 * sc;
+  A[2] = R02 * sc;
+  A[3] = R10 * sc;
+  A[4] = R11 * sc;
+  A[5] = R12 * sc;
+  A[6] = R20 * sc;
+  A[7] = R21 * sc;
+  A[8] = R22 * sc;
+  b[0] = ux - (A[0] * ux + A[1] * uy + A[2] * uz);
+  b[1] = uy - (A[3] * ux + A[4] * uy + A[5] * uz);
+  b[2] = uz - (A[6] * ux + A[7] * uy + A[8] * uz);
+  // kinetic energy removed by the thermostat: sum m v^2 - sum m v'^2 = E_rel (1 - sc^2)
+  ldiss += erel * (1.0 - sc * sc);
+}
+
+// ============================================================== float64 ===
+
+__global__ void k_cell_params_f64(CellsF64 c, StepArgs a) {
+  double ldiss = 0.0;
+  unsigned errbits = 0;
+  bool gfail = false;
+  for (long cid = (long)blockIdx.x * blockDim.x + threadIdx.x; cid < c.ncell; cid += (long)gridDim.x * blockDim.x) {
+    const uint32_t w = c.cnt[cid];
+    if (w == 0) continue;
+    const double4 s = c.sum[cid];
+    c.sum[cid] = make_double4(0.0, 0.0, 0.0, 0.0);
+    c.cnt[cid] = 0u;
+    double A[9], b[3];
+    collision_map(s, w, cid, a, A, b, ldiss, errbits, gfail);
+    double2* p = reinterpret_cast<double2*>(c.par + 12 * cid);
+    p[0] = make_double2(A[0], A[1]);
+    p[1] = make_double2(A[2], A[3]);
+    p[2] = make_double2(A[4], A[5]);
+    p[3] = make_double2(A[6], A[7]);
+    p[4] = make_double2(A[8], b[0]);
+    p[5] = make_double2(b[1], b[2]);
+  }
+  if (gfail) errbits |= kErrGammaLoop;
+  if (errbits) atomicOr(a.err, errbits);
+  double tot = block_sum_f64(ldiss);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
+}
+
+__device__ __forceinline__ void apply_map_f64(const double* par, double& vx, double& vy, double& vz) {
+  const double2* p = reinterpret_cast<const double2*>(par);
+  const double2 p0 = __ldg(p + 0), p1 = __ldg(p + 1), p2 = __ldg(p + 2);
+  const double2 p3 = __ldg(p + 3), p4 = __ldg(p + 4), p5 = __ldg(p + 5);
+  const double nx = fma(p0.x, vx, fma(p0.y, vy, fma(p1.x, vz, p4.y)));
+  const double ny = fma(p1.y, vx, fma(p2.x, vy, fma(p2.y, vz, p5.x)));
+  const double nz = fma(p3.x, vx, fma(p3.y, vy, fma(p4.x, vz, p5.y)));
+  vx = nx;
+  vy = ny;
+  vz = nz;
+}
+
+// Walls along z (NOSLIP / SLIP, src/libcilia/mpcd.cpp:346-376): the channel is
+// 0 <= z <= Lz - 1; a particle that crossed a wall during the streaming step
+// is reflected.  Returns the (possibly changed) unwrapped z.
+__device__ __forceinline__ void wall_bounce(int walls, double ztop, double& x, double& y, double& z, double& vx,
+                                            double& vy, double& vz) {
+  if (z > ztop) {
+    if (walls == 1) {
+      double t2 = (z - ztop) / vz;
+      vx = -vx;
+      vy = -vy;
+      vz = -vz;
+      x += 2.0 * t2 * vx;
+      y += 2.0 * t2 * vy;
+      z += 2.0 * t2 * vz;
+    } else {
+      vz = -vz;
+      z = -z + ztop * 2.0;
+    }
+  }
+  if (z < 0) {
+    double t2 = z / vz;
+    vx = -vx;
+    vy = -vy;
+    vz = -vz;
+    x += vx * 2.0 * t2;
+    y += vy * 2.0 * t2;
+    z += vz * 2.0 * t2;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF64 c, StepArgs a) {
+  const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
+  const long long tcx = __double_as_longlong(a.ta_cur[0]), tcy = __double_as_longlong(a.ta_cur[1]),
+                  tcz = __double_as_longlong(a.ta_cur[2]);
+  const long long tnx = __double_as_longlong(a.ta_next[0]), tny = __double_as_longlong(a.ta_next[1]),
+                  tnz = __double_as_longlong(a.ta_next[2]);
+  const double h = a.h;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t cp = f.cell[i];
+    int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
+    double ox = f.ox[i], oy = f.oy[i], oz = f.oz[i];
+    double vx = f.vx[i], vy = f.vy[i], vz = f.vz[i];
+    // collision with the map of the shifted cell
+    const long cid = shifted(ix, ox, tcx, Lx) + (long)Lx * (shifted(iy, oy, tcy, Ly) + (long)Ly * shifted(iz, oz, tcz, Lz));
+    apply_map_f64(c.par + 12 * cid, vx, vy, vz);
+    // streaming
+    if (a.walls == 0) {
+      ox = fma(vx, h, ox);
+      oy = fma(vy, h, oy);
+      oz = fma(vz, h, oz);
+    } else {
+      double x = ix + ox, y = iy + oy, z = iz + oz;
+      x += vx * h;
+      y += vy * h;
+      z += vz * h;
+      wall_bounce(a.walls, (double)(Lz - 1), x, y, z, vx, vy, vz);
+      double fx = floor(x), fy = floor(y), fz = floor(z);
+      ox = x - fx;
+      oy = y - fy;
+      oz = z - fz;
+      ix = (((int)fx % Lx) + Lx) % Lx;
+      iy = (((int)fy % Ly) + Ly) % Ly;
+      iz = (((int)fz % Lz) + Lz) % Lz;
+    }
+    rewrap(ox, ix, Lx);
+    rewrap(oy, iy, Ly);
+    rewrap(oz, iz, Lz);
+    if (a.gkick != 0.0) vx += a.gkick;
+    // bin with the next shift
+    const long cn = shifted(ix, ox, tnx, Lx) + (long)Lx * (shifted(iy, oy, tny, Ly) + (long)Ly * shifted(iz, oz, tnz, Lz));
+    const double K = vx * vx + vy * vy + vz * vz;
+    double* sp = reinterpret_cast<double*>(c.sum + cn);
+    atomicAdd(sp + 0, vx);
+    atomicAdd(sp + 1, vy);
+    atomicAdd(sp + 2, vz);
+    atomicAdd(sp + 3, K);
+    atomicAdd(c.cnt + cn, 1u);
+    f.cell[i] = pack_cell(ix, iy, iz);
+    f.ox[i] = ox;
+    f.oy[i] = oy;
+    f.oz[i] = oz;
+    f.vx[i] = vx;
+    f.vy[i] = vy;
+    f.vz[i] = vz;
+  }
+}
+
+__global__ void k_bin_fluid_f64(FluidF64 f, CellsF64 c, StepArgs a) {
+  const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
+  const long long tcx = __double_as_longlong(a.ta_cur[0]), tcy = __double_as_longlong(a.ta_cur[1]),
+                  tcz = __double_as_longlong(a.ta_cur[2]);
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t cp = f.cell[i];
+    const long cid = shifted(cell_x(cp), f.ox[i], tcx, Lx) +
+                     (long)Lx * (shifted(cell_y(cp), f.oy[i], tcy, Ly) + (long)Ly * shifted(cell_z(cp), f.oz[i], tcz, Lz));
+    const double vx = f.vx[i], vy = f.vy[i], vz = f.vz[i];
+    double* sp = reinterpret_cast<double*>(c.sum + cid);
+    atomicAdd(sp + 0, vx);
+    atomicAdd(sp + 1, vy);
+    atomicAdd(sp + 2, vz);
+    atomicAdd(sp + 3, vx * vx + vy * vy + vz * vz);
+    atomicAdd(c.cnt + cid, 1u);
+  }
+}
+
+__device__ __forceinline__ long bead_cell(const Box& box, const double* a, double x, double y, double z) {
+  return ref_cell_axis(x, a[0], box.L[0]) +
+         (long)box.L[0] * (ref_cell_axis(y, a[1], box.L[1]) + (long)box.L[1] * ref_cell_axis(z, a[2], box.L[2]));
+}
+
+__global__ void k_bead_collide_f64(MDState m, CellsF64 c, StepArgs a) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    double vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
+    apply_map_f64(c.par + 12 * cid, vx, vy, vz);
+    m.vx[s] = vx;
+    m.vy[s] = vy;
+    m.vz[s] = vz;
+  }
+}
+
+__global__ void k_bin_beads_f64(MDState m, CellsF64 c, StepArgs a) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    const double mb = a.bead_mass, vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
+    double* sp = reinterpret_cast<double*>(c.sum + cid);
+    atomicAdd(sp + 0, vx * mb);
+    atomicAdd(sp + 1, vy * mb);
+    atomicAdd(sp + 2, vz * mb);
+    atomicAdd(sp + 3, mb * (vx * vx + vy * vy + vz * vz));
+    atomicAdd(c.cnt + cid, 1u << 16);
+  }
+}
+
+__global__ void k_observables_f64(FluidF64 f, MDState m, double bead_mass, double* out) {
+  double px = 0, py = 0, pz = 0, e = 0, n = 0, ms = 0, ef = 0, nf = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const double vx = f.vx[i], vy = f.vy[i], vz = f.vz[i];
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    px += vx;
+    py += vy;
+    pz += vz;
+    e += v2;
+    ef += v2;
+    n += 1.0;
+    ms += 1.0;
+    nf += 1.0;
+  }
+  for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += (long)gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const double vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
+    px += bead_mass * vx;
+    py += bead_mass * vy;
+    pz += bead_mass * vz;
+    e += bead_mass * (vx * vx + vy * vy + vz * vz);
+    n += 1.0;
+    ms += bead_mass;
+  }
+  double vals[8] = {px, py, pz, e, n, ms, ef, nf};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    double t = block_sum_f64(vals[k]);
+    if (threadIdx.x == 0) atomicAdd(out + k, t);
+  }
+}
+
+// ================================================================== sort ===
+
+__global__ void k_sort_count(const uint32_t* cell, long n, Box box, uint32_t* count, uint32_t* rank) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t cp = cell[i];
+    const long c = box.lin(cell_x(cp), cell_y(cp), cell_z(cp));
+    rank[i] = atomicAdd(count + c, 1u);
+  }
+}
+
+__global__ void k_sort_count_f32(const float4* pos, long n, Box box, uint32_t* count, uint32_t* rank) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t cp = __float_as_uint(pos[i].w);
+    const long c = box.lin(cell_x(cp), cell_y(cp), cell_z(cp));
+    rank[i] = atomicAdd(count + c, 1u);
+  }
+}
+
+// exclusive scan of `count` (n entries) into `start`, three passes
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_blocks(const uint32_t* in, long n, uint32_t* blocksums) {
+  __shared__ uint32_t red[32];
+  long i = (long)blockIdx.x * kScanBlock + threadIdx.x;
+  uint32_t v = i < n ? in[i] : 0u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t r = red[threadIdx.x];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (threadIdx.x == 0) blocksums[blockIdx.x] = r;
+  }
+}
+
+__global__ void k_scan_blocksums(uint32_t* blocksums, int nb) {
+  // single block: sequential over chunks of 1024 with an in-block scan
+  __shared__ uint32_t wsum[32];
+  uint32_t carry = 0;
+  for (int base = 0; base < nb; base += kScanBlock) {
+    int i = base + threadIdx.x;
+    uint32_t v = i < nb ? blocksums[i] : 0u;
+    uint32_t x = v;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      uint32_t w = wsum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    uint32_t incl = x + (wid > 0 ? wsum[wid - 1] : 0u);
+    if (i < nb) blocksums[i] = carry + incl - v;  // exclusive
+    uint32_t total = wsum[31];
+    __syncthreads();
+    carry += total;
+  }
+}
+
+__global__ void k_scan_apply(const uint32_t* in, long n, const uint32_t* blockoff, uint32_t* out) {
+  __shared__ uint32_t wsum[32];
+  long i = (long)blockIdx.x * kScanBlock + threadIdx.x;
+  uint32_t v = i < n ? in[i] : 0u;
+  uint32_t x = v;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  uint32_t incl = x + (wid > 0 ? wsum[wid - 1] : 0u);
+  if (i < n) out[i] = blockoff[blockIdx.x] + incl - v;
+}
+
+__global__ void k_sort_scatter_f64(FluidF64 src, FluidF64 dst, Box box, const uint32_t* start, const uint32_t* rank) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < src.n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t cp = src.cell[i];
+    const long c = box.lin(cell_x(cp), cell_y(cp), cell_z(cp));
+    const long d = (long)start[c] + rank[i];
+    dst.cell[d] = cp;
+    dst.ox[d] = src.ox[i];
+    dst.oy[d] = src.oy[i];
+    dst.oz[d] = src.oz[i];
+    dst.vx[d] = src.vx[i];
+    dst.vy[d] = src.vy[i];
+    dst.vz[d] = src.vz[i];
+  }
+}
+
+__global__ void k_sort_scatter_f32(FluidF32 src, FluidF32 dst, Box box, const uint32_t* start, const uint32_t* rank) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < src.n; i += (long)gridDim.x * blockDim.x) {
+    const float4 p = src.pos[i];
+    const uint32_t cp = __float_as_uint(p.w);
+    const long c = box.lin(cell_x(cp), cell_y(cp), cell_z(cp));
+    const long d = (long)start[c] + rank[i];
+    dst.pos[d] = p;
+    dst.vel[d] = src.vel[i];
+  }
+}
+
+int scan_counts(const uint32_t* count, long ncell, uint32_t* start, uint32_t* blocksums, cudaStream_t s) {
+  const int nb = (int)((ncell + kScanBlock - 1) / kScanBlock);
+  k_scan_blocks<<<nb, kScanBlock, 0, s>>>(count, ncell, blocksums);
+  k_scan_blocksums<<<1, kScanBlock, 0, s>>>(blocksums, nb);
+  k_scan_apply<<<nb, kScanBlock, 0, s>>>(count, ncell, blocksums, start);
+  return 3;
+}
+
+// ============================================================== float32 ===
+// Split precision: position = packed cell + float32 offset, velocity float32,
+// per-cell sums and collision maps float32.  The thermostat factor and the
+// rotation are computed per cell in float64 and rounded once.
+
+__device__ __forceinline__ int shifted_f(int i, float o, float ta, int L) {
+  int s = i + (o >= ta ? 1 : 0);
+  return s == L ? 0 : s;
+}
+
+__device__ __forceinline__ void rewrap_f(float& o, int& i, int L) {
+  if (o < 0.0f || o >= 1.0f) {
+    float fl = floorf(o);
+    o -= fl;
+    i += (int)fl;
+    if (o >= 1.0f) {
+      o = 0.0f;
+      i += 1;
+    }
+    i %= L;
+    if (i < 0) i += L;
+  }
+}
+
+__device__ __forceinline__ void red_add_v4(float4* addr, float4 v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
+__global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
+  double ldiss = 0.0;
+  unsigned errbits = 0;
+  bool gfail = false;
+  for (long cid = (long)blockIdx.x * blockDim.x + threadIdx.x; cid < c.ncell; cid += (long)gridDim.x * blockDim.x) {
+    const uint32_t w = c.cnt[cid];
+    if (w == 0) continue;
+    const float4 sf = c.sum[cid];
+    c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    c.cnt[cid] = 0u;
+    double A[9], b[3];
+    collision_map(make_double4(sf.x, sf.y, sf.z, sf.w), w, cid, a, A, b, ldiss, errbits, gfail);
+    float4* p = c.par + 3 * cid;
+    p[0] = make_float4((float)A[0], (float)A[1], (float)A[2], (float)b[0]);
+    p[1] = make_float4((float)A[3], (float)A[4], (float)A[5], (float)b[1]);
+    p[2] = make_float4((float)A[6], (float)A[7], (float)A[8], (float)b[2]);
+  }
+  if (gfail) errbits |= kErrGammaLoop;
+  if (errbits) atomicOr(a.err, errbits);
+  double tot = block_sum_f64(ldiss);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
+}
+
+__device__ __forceinline__ void apply_map_f32(const float4* par, float& vx, float& vy, float& vz) {
+  const float4 r0 = __ldg(par + 0), r1 = __ldg(par + 1), r2 = __ldg(par + 2);
+  const float nx = fmaf(r0.x, vx, fmaf(r0.y, vy, fmaf(r0.z, vz, r0.w)));
+  const float ny = fmaf(r1.x, vx, fmaf(r1.y, vy, fmaf(r1.z, vz, r1.w)));
+  const float nz = fmaf(r2.x, vx, fmaf(r2.y, vy, fmaf(r2.z, vz, r2.w)));
+  vx = nx;
+  vy = ny;
+  vz = nz;
+}
+
+__global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF32 c, StepArgs a) {
+  const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
+  const float tcx = (float)a.ta_cur[0], tcy = (float)a.ta_cur[1], tcz = (float)a.ta_cur[2];
+  const float tnx = (float)a.ta_next[0], tny = (float)a.ta_next[1], tnz = (float)a.ta_next[2];
+  const float h = (float)a.h, gk = (float)a.gkick;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const float4 p = f.pos[i];
+    const float4 v = f.vel[i];
+    const uint32_t cp = __float_as_uint(p.w);
+    int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
+    float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
+    const long cid = shifted_f(ix, ox, tcx, Lx) + (long)Lx * (shifted_f(iy, oy, tcy, Ly) + (long)Ly * shifted_f(iz, oz, tcz, Lz));
+    apply_map_f32(c.par + 3 * cid, vx, vy, vz);
+    if (a.walls == 0) {
+      ox = fmaf(vx, h, ox);
+      oy = fmaf(vy, h, oy);
+      oz = fmaf(vz, h, oz);
+    } else {
+      double x = ix + (double)ox, y = iy + (double)oy, z = iz + (double)oz;
+      double dvx = vx, dvy = vy, dvz = vz;
+      x += dvx * a.h;
+      y += dvy * a.h;
+      z += dvz * a.h;
+      wall_bounce(a.walls, (double)(Lz - 1), x, y, z, dvx, dvy, dvz);
+      double fx = floor(x), fy = floor(y), fz = floor(z);
+      ox = (float)(x - fx);
+      oy = (float)(y - fy);
+      oz = (float)(z - fz);
+      ix = (((int)fx % Lx) + Lx) % Lx;
+      iy = (((int)fy % Ly) + Ly) % Ly;
+      iz = (((int)fz % Lz) + Lz) % Lz;
+      vx = (float)dvx;
+      vy = (float)dvy;
+      vz = (float)dvz;
+    }
+    rewrap_f(ox, ix, Lx);
+    rewrap_f(oy, iy, Ly);
+    rewrap_f(oz, iz, Lz);
+    vx += gk;
+    const long cn = shifted_f(ix, ox, tnx, Lx) + (long)Lx * (shifted_f(iy, oy, tny, Ly) + (long)Ly * shifted_f(iz, oz, tnz, Lz));
+    red_add_v4(c.sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
+    atomicAdd(c.cnt + cn, 1u);
+    f.pos[i] = make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz)));
+    f.vel[i] = make_float4(vx, vy, vz, 0.f);
+  }
+}
+
+__global__ void k_bin_fluid_f32(FluidF32 f, CellsF32 c, StepArgs a) {
+  const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
+  const float tcx = (float)a.ta_cur[0], tcy = (float)a.ta_cur[1], tcz = (float)a.ta_cur[2];
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const float4 p = f.pos[i];
+    const float4 v = f.vel[i];
+    const uint32_t cp = __float_as_uint(p.w);
+    const long cid = shifted_f(cell_x(cp), p.x, tcx, Lx) +
+                     (long)Lx * (shifted_f(cell_y(cp), p.y, tcy, Ly) + (long)Ly * shifted_f(cell_z(cp), p.z, tcz, Lz));
+    red_add_v4(c.sum + cid, make_float4(v.x, v.y, v.z, v.x * v.x + v.y * v.y + v.z * v.z));
+    atomicAdd(c.cnt + cid, 1u);
+  }
+}
+
+__global__ void k_bead_collide_f32(MDState m, CellsF32 c, StepArgs a) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    float vx = (float)m.vx[s], vy = (float)m.vy[s], vz = (float)m.vz[s];
+    apply_map_f32(c.par + 3 * cid, vx, vy, vz);
+    m.vx[s] = vx;
+    m.vy[s] = vy;
+    m.vz[s] = vz;
+  }
+}
+
+__global__ void k_bin_beads_f32(MDState m, CellsF32 c, StepArgs a) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    const float mb = (float)a.bead_mass;
+    const float vx = (float)m.vx[s], vy = (float)m.vy[s], vz = (float)m.vz[s];
+    red_add_v4(c.sum + cid, make_float4(vx * mb, vy * mb, vz * mb, mb * (vx * vx + vy * vy + vz * vz)));
+    atomicAdd(c.cnt + cid, 1u << 16);
+  }
+}
+
+__global__ void k_observables_f32(FluidF32 f, MDState m, double bead_mass, double* out) {
+  double px = 0, py = 0, pz = 0, e = 0, n = 0, ms = 0, ef = 0, nf = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const float4 v = f.vel[i];
+    const double vx = v.x, vy = v.y, vz = v.z;
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    px += vx;
+    py += vy;
+    pz += vz;
+    e += v2;
+    ef += v2;
+    n += 1.0;
+    ms += 1.0;
+    nf += 1.0;
+  }
+  for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += (long)gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const double vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
+    px += bead_mass * vx;
+    py += bead_mass * vy;
+    pz += bead_mass * vz;
+    e += bead_mass * (vx * vx + vy * vy + vz * vz);
+    n += 1.0;
+    ms += bead_mass;
+  }
+  double vals[8] = {px, py, pz, e, n, ms, ef, nf};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    double t = block_sum_f64(vals[k]);
+    if (threadIdx.x == 0) atomicAdd(out + k, t);
+  }
+}
+
+}  // namespace
+
+// ============================================================ launchers ===
+
+int launch_cell_params_f64(const CellsF64& c, const StepArgs& a, cudaStream_t s) {
+  k_cell_params_f64<<<grid_for(c.ncell), kThreads, 0, s>>>(c, a);
+  return 1;
+}
+int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s) {
+  if (f.n == 0) return 0;
+  k_fluid_step_f64<<<grid_for(f.n), kThreads, 0, s>>>(f, c, a);
+  return 1;
+}
+int launch_bin_fluid_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s) {
+  if (f.n == 0) return 0;
+  k_bin_fluid_f64<<<grid_for(f.n), kThreads, 0, s>>>(f, c, a);
+  return 1;
+}
+int launch_bead_collide_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bead_collide_f64<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, a);
+  return 1;
+}
+int launch_bin_beads_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bin_beads_f64<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, a);
+  return 1;
+}
+int launch_observables_f64(const FluidF64& f, const MDState& m, double bead_mass, double* out, cudaStream_t s) {
+  long n = f.n > m.nslots ? f.n : m.nslots;
+  k_observables_f64<<<grid_for(n) < 1024 ? grid_for(n) : 1024, kThreads, 0, s>>>(f, m, bead_mass, out);
+  return 1;
+}
+int launch_sort_f64(FluidF64& f, FluidF64& tmp, const Box& box, uint32_t* count, uint32_t* start, uint32_t* rank,
+                    uint32_t* blocksums, cudaStream_t s) {
+  const long ncell = (long)box.L[0] * box.L[1] * box.L[2];
+  cudaMemsetAsync(count, 0, ncell * sizeof(uint32_t), s);
+  k_sort_count<<<grid_for(f.n), kThreads, 0, s>>>(f.cell, f.n, box, count, rank);
+  int k = 1 + scan_counts(count, ncell, start, blocksums, s);
+  tmp.n = f.n;
+  k_sort_scatter_f64<<<grid_for(f.n), kThreads, 0, s>>>(f, tmp, box, start, rank);
+  FluidF64 t = f;
+  f = tmp;
+  tmp = t;
+  return k + 1;
+}
+
+int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s) {
+  k_cell_params_f32<<<grid_for(c.ncell), kThreads, 0, s>>>(c, a);
+  return 1;
+}
+int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s) {
+  if (f.n == 0) return 0;
+  k_fluid_step_f32<<<grid_for(f.n), kThreads, 0, s>>>(f, c, a);
+  return 1;
+}
+int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s) {
+  if (f.n == 0) return 0;
+  k_bin_fluid_f32<<<grid_for(f.n), kThreads, 0, s>>>(f, c, a);
+  return 1;
+}
+int launch_bead_collide_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bead_collide_f32<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, a);
+  return 1;
+}
+int launch_bin_beads_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bin_beads_f32<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, a);
+  return 1;
+}
+int launch_observables_f32(const FluidF32& f, const MDState& m, double bead_mass, double* out, cudaStream_t s) {
+  long n = f.n > m.nslots ? f.n : m.nslots;
+  k_observables_f32<<<grid_for(n) < 1024 ? grid_for(n) : 1024, kThreads, 0, s>>>(f, m, bead_mass, out);
+  return 1;
+}
+int launch_sort_f32(FluidF32& f, FluidF32& tmp, const Box& box, uint32_t* count, uint32_t* start, uint32_t* rank,
+                    uint32_t* blocksums, cudaStream_t s) {
+  const long ncell = (long)box.L[0] * box.L[1] * box.L[2];
+  cudaMemsetAsync(count, 0, ncell * sizeof(uint32_t), s);
+  k_sort_count_f32<<<grid_for(f.n), kThreads, 0, s>>>(f.pos, f.n, box, count, rank);
+  int k = 1 + scan_counts(count, ncell, start, blocksums, s);
+  tmp.n = f.n;
+  k_sort_scatter_f32<<<grid_for(f.n), kThreads, 0, s>>>(f, tmp, box, start, rank);
+  FluidF32 t = f;
+  f = tmp;
+  tmp = t;
+  return k + 1;
+}
+
+}  // namespace mpcd

@@ -1,0 +1,172 @@
+// Device-side building blocks shared by the MPCD kernels.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#ifndef MPCD_HD
+#define MPCD_HD __host__ __device__ __forceinline__
+#endif
+
+namespace mpcd {
+
+// -------------------------------------------------------------- errors ---
+// Bits of the device error word (read back by mpcd_sync / the getters).
+enum : unsigned {
+  kErrGammaMissing = 1u,   // injected Gamma < 0 for a cell that needs one
+  kErrGammaLoop = 2u,      // Marsaglia-Tsang loop exceeded its iteration cap
+  kErrBarrier = 4u,        // grid barrier wait exceeded its iteration cap
+  kErrCellRange = 8u,      // a particle's cell index was out of range
+  kErrCellOverflow = 16u,  // more than 65535 particles of one kind in a cell
+};
+
+// ----------------------------------------------------------- constants ---
+// SRD rotation by 130 degrees: the reference's cos/sin constants
+// (src/libcilia/mpcd.h:72-76), used as given.
+constexpr double kCosAlpha = -0.6427876;
+constexpr double kSinAlpha = 0.76604444;
+constexpr double kPi = 3.14159265358979323846;
+
+// ------------------------------------------------------------- Philox ---
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies on a 128-bit
+// counter with a 64-bit key bumped by the Weyl constants each round.
+struct u32x4 {
+  uint32_t x, y, z, w;
+};
+
+MPCD_HD void mulhilo(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  hi = (uint32_t)(p >> 32);
+  lo = (uint32_t)p;
+}
+
+MPCD_HD u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo(M0, c.x, hi0, lo0);
+    mulhilo(M1, c.z, hi1, lo1);
+    c = u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// Stream identifiers: which quantity a counter block feeds.
+enum : uint32_t { kStreamShift = 1, kStreamCell = 2, kStreamWall = 3, kStreamInit = 4 };
+
+// counter = (index, step_lo, step_hi ^ (stream << 24), round)
+MPCD_HD u32x4 draw4(uint64_t seed, uint64_t step, uint32_t stream, uint32_t index, uint32_t round) {
+  u32x4 c{index, (uint32_t)step, (uint32_t)(step >> 32) ^ (stream << 24), round};
+  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// uniform in (0,1), 32-bit resolution, like MTRand::randDblExc
+MPCD_HD double u01_dbl(uint32_t u) { return ((double)u + 0.5) * (1.0 / 4294967296.0); }
+// uniform in (0,1), float (24-bit)
+MPCD_HD float u01_flt(uint32_t u) { return ((float)(u >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+
+// Gamma(k = 3(N-1)/2, 1) by Marsaglia & Tsang (2000), the method of
+// src/libcilia/mpcd.cpp:13-43, driven by Philox draws in float.  The loop is
+// capped; on exhaustion it returns the mean and sets *failed.
+__device__ __forceinline__ float gamma_mt(int nc, uint64_t seed, uint64_t step, uint32_t cell, bool* failed) {
+  const float d = 1.5f * (float)nc - 1.8333333333f;
+  const float c = (1.0f / 3.0f) * rsqrtf(d);
+  for (uint32_t round = 0; round < 64; ++round) {
+    u32x4 r = draw4(seed, step, kStreamCell, cell, 16u + round);
+    float u1 = u01_flt(r.x), u2 = u01_flt(r.y);
+    float x = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+    float v = 1.0f + c * x;
+    if (v <= 0.0f) continue;
+    v = v * v * v;
+    float u = u01_flt(r.z);
+    float x2 = x * x;
+    if (u < 1.0f - 0.0331f * x2 * x2) return d * v;
+    if (logf(u) < 0.5f * x2 + d * (1.0f - v + logf(v))) return d * v;
+  }
+  *failed = true;
+  return d;
+}
+
+// Uniform random axis from two uniforms (src/libcilia/mpcd.cpp:277-283), in double.
+__device__ __forceinline__ void random_axis(uint64_t seed, uint64_t step, uint32_t cell, double& rx, double& ry,
+                                            double& rz) {
+  u32x4 r = draw4(seed, step, kStreamCell, cell, 0u);
+  double phi = 2.0 * kPi * u01_dbl(r.x);
+  double ct = 2.0 * u01_dbl(r.y) - 1.0;
+  double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+  double sp, cp;
+  sincos(phi, &sp, &cp);
+  rx = st * cp;
+  ry = st * sp;
+  rz = ct;
+}
+
+// ---------------------------------------------------------------- cells ---
+// A particle's cell is packed as ix | iy << 10 | iz << 20 (edges up to 1024).
+MPCD_HD uint32_t pack_cell(int ix, int iy, int iz) { return (uint32_t)ix | ((uint32_t)iy << 10) | ((uint32_t)iz << 20); }
+MPCD_HD int cell_x(uint32_t c) { return (int)(c & 1023u); }
+MPCD_HD int cell_y(uint32_t c) { return (int)((c >> 10) & 1023u); }
+MPCD_HD int cell_z(uint32_t c) { return (int)((c >> 20) & 1023u); }
+
+struct Box {
+  int L[3];
+  MPCD_HD int lin(int ix, int iy, int iz) const { return ix + L[0] * (iy + L[1] * iz); }
+};
+
+// Count word of a cell: fluid particles in the low 16 bits, beads in the high.
+MPCD_HD int cnt_fluid(uint32_t w) { return (int)(w & 0xffffu); }
+MPCD_HD int cnt_beads(uint32_t w) { return (int)(w >> 16); }
+
+// ----------------------------------------------------------- barriers ---
+// Grid-wide barrier for cooperative launches: one arrival counter and a
+// generation word.  Every wait is bounded; on timeout it sets kErrBarrier in
+// *err and returns false, and the caller leaves the kernel.
+struct GridBarrier {
+  unsigned* count;
+  unsigned* gen;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks, unsigned* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    unsigned g = ld_acquire(b.gen);
+    __threadfence();
+    unsigned arrived = atomicAdd(b.count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(b.count, 0u);
+      __threadfence();
+      st_release(b.gen, g + 1);
+    } else {
+      unsigned long long spins = 0;
+      while (ld_acquire(b.gen) == g) {
+        if (++spins > (1ull << 24)) {  // ~ seconds at the polling interval below
+          atomicOr(err, kErrBarrier);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (ok && (ld_acquire(err) & kErrBarrier)) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+}  // namespace mpcd

@@ -266,7 +266,7 @@ def baseline_config(which: str, **kw) -> dict:
     swimmer128: 128^3 fluid, radius 16, 400 cilia of rodlength 20.
     """
     if which == "plain32":
-        return plain_fluid(32, name="plain32", **kw)
+        return plain_fluid(32, name="plain32")
     if which in ("swimmer64", "swimmer128"):
         L, R, nc, rl = (64, 8.0, 100, 15) if which == "swimmer64" else (128, 16.0, 400, 20)
         cfg = plain_fluid(L, name=which)
