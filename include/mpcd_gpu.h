@@ -68,6 +68,8 @@ typedef struct {
   unsigned long long seed; /* counter-based generator seed for free-running steps */
   int device;            /* CUDA device ordinal */
   int sort_interval;     /* reorder particles by cell every this many steps (0 = auto) */
+  int md_split;          /* MD spring arithmetic: -1 auto (split when precision is FP32),
+                            0 float64, 1 split (float on hi/lo position pairs; state stays float64) */
 } mpcd_params;
 
 /* Values that replace the generator for one step (all host arrays).  Used to

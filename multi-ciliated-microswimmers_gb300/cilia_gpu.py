@@ -29,7 +29,8 @@ _IP = ctypes.POINTER(ctypes.c_int)
 class MpcdParams(ctypes.Structure):
     _fields_ = [("sizes", ctypes.c_int * 3), ("tstep", _D), ("ststep", _D), ("precision", ctypes.c_int),
                 ("walls", ctypes.c_int), ("gravity", _D), ("omega", _D), ("bead_mass", _D),
-                ("seed", ctypes.c_ulonglong), ("device", ctypes.c_int), ("sort_interval", ctypes.c_int)]
+                ("seed", ctypes.c_ulonglong), ("device", ctypes.c_int), ("sort_interval", ctypes.c_int),
+                ("md_split", ctypes.c_int)]
 
 
 class MpcdInject(ctypes.Structure):
@@ -129,7 +130,8 @@ class Engine:
     """One MPCD box with MD beads on the GPU (mpcd_engine)."""
 
     def __init__(self, L, *, tstep=0.1, ststep=0.001, precision=MPCD_FP64, walls=WALLS_NONE, gravity=0.0,
-                 omega=0.0, bead_mass=5.0, seed=1, device=0, sort_interval=0, _handle=None, _owner=None):
+                 omega=0.0, bead_mass=5.0, seed=1, device=0, sort_interval=0, md_split=-1, _handle=None,
+                 _owner=None):
         self._owner = _owner
         if _handle is not None:
             self._h = _handle
@@ -141,7 +143,7 @@ class Engine:
             p.sizes[:] = [int(x) for x in L]
             p.tstep, p.ststep, p.precision, p.walls = tstep, ststep, precision, walls
             p.gravity, p.omega, p.bead_mass, p.seed = gravity, omega, bead_mass, seed
-            p.device, p.sort_interval = device, sort_interval
+            p.device, p.sort_interval, p.md_split = device, sort_interval, md_split
             h = ctypes.c_void_p()
             rc = lib().mpcd_create(ctypes.byref(p), ctypes.byref(h))
             if rc:

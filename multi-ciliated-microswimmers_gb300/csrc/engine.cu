@@ -20,9 +20,6 @@
 #include "../../include/mpcd_gpu.h"
 #include "engine_internal.h"
 
-namespace mpcd {
-int md_max_coresident_blocks(int tile, int f32cells);
-}
 
 using namespace mpcd;
 
@@ -120,6 +117,7 @@ void shift_from_counter(uint64_t seed, uint64_t step, double* a) {
 }
 
 void free_fluid(FluidF64& f) {
+  cudaFree(f.id);
   cudaFree(f.cell);
   cudaFree(f.ox);
   cudaFree(f.oy);
@@ -145,6 +143,10 @@ void free_md(MDState& m) {
   cudaFree(m.tile_help);
   cudaFree(m.sp_start);
   cudaFree(m.sp_other);
+  cudaFree(m.sp_local);
+  cudaFree(m.halo);
+  cudaFree(m.halo_start);
+  cudaFree(m.diag);
   cudaFree(m.sp_kind);
   cudaFree(m.sp_ref);
   cudaFree(m.sp_rest);
@@ -166,6 +168,7 @@ int alloc_fluid(mpcd_engine* h, long n) {
     free_fluid(h->f64tmp);
     for (FluidF64* f : {&h->f64, &h->f64tmp}) {
       f->n = n;
+      CK(dalloc(&f->id, n));
       CK(dalloc(&f->cell, n));
       CK(dalloc(&f->ox, n));
       CK(dalloc(&f->oy, n));
@@ -175,12 +178,14 @@ int alloc_fluid(mpcd_engine* h, long n) {
       CK(dalloc(&f->vz, n));
     }
   } else {
-    cudaFree(h->f32.pos);
-    cudaFree(h->f32.vel);
-    cudaFree(h->f32tmp.pos);
-    cudaFree(h->f32tmp.vel);
+    for (FluidF32* f : {&h->f32, &h->f32tmp}) {
+      cudaFree(f->id);
+      cudaFree(f->pos);
+      cudaFree(f->vel);
+    }
     for (FluidF32* f : {&h->f32, &h->f32tmp}) {
       f->n = n;
+      CK(dalloc(&f->id, n));
       CK(dalloc(&f->pos, n));
       CK(dalloc(&f->vel, n));
     }
@@ -299,8 +304,7 @@ int build_md(mpcd_engine* h) {
   m.tile = tile;
   m.ntiles = (int)fill.size();
   m.nslots = m.ntiles * tile;
-  const int cap = md_max_coresident_blocks(tile, h->p.precision == MPCD_FP32 ? 1 : 0);
-  if (m.ntiles > cap) return fail(h, MPCD_EINVAL, "MD tiles exceed the co-resident CTA limit of the device");
+  m.split = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 0) : (h->p.md_split ? 1 : 0);
   const int ns = m.nslots;
   std::vector<double> X(ns, 0.0), Y(ns, 0.0), Z(ns, 0.0), VX(ns, 0.0), VY(ns, 0.0), VZ(ns, 0.0);
   std::vector<int> mv(ns, -1), prim(ns, 0), nhelp(ns, 0), thelp(m.ntiles, 0);
@@ -348,6 +352,30 @@ int build_md(mpcd_engine* h) {
     srest[d] = h->sp_rest[i];
     sm2k[d] = -2.0 * h->sp_kk[i];
   }
+  // halos: per tile the distinct slots of other tiles its springs reach, and
+  // every spring's other bead as an index into the tile's staged positions
+  std::vector<int> sl(nsp), halo, hstart(m.ntiles + 1, 0);
+  int hmax = 0;
+  for (int t = 0; t < m.ntiles; ++t) {
+    const int b0 = t * tile, b1 = b0 + tile;
+    std::vector<int> ext;
+    for (int s2 = start[b0]; s2 < start[b1]; ++s2)
+      if (so[s2] < b0 || so[s2] >= b1) ext.push_back(so[s2]);
+    std::sort(ext.begin(), ext.end());
+    ext.erase(std::unique(ext.begin(), ext.end()), ext.end());
+    for (int s2 = start[b0]; s2 < start[b1]; ++s2) {
+      if (so[s2] >= b0 && so[s2] < b1)
+        sl[s2] = so[s2] - b0;
+      else
+        sl[s2] = tile + (int)(std::lower_bound(ext.begin(), ext.end(), so[s2]) - ext.begin());
+    }
+    hstart[t + 1] = hstart[t] + (int)ext.size();
+    halo.insert(halo.end(), ext.begin(), ext.end());
+    hmax = std::max(hmax, (int)ext.size());
+  }
+  m.hmax = hmax;
+  const int cap = md_max_coresident_blocks(m, h->p.precision == MPCD_FP32 ? 1 : 0);
+  if (m.ntiles > cap) return fail(h, MPCD_EINVAL, "MD tiles exceed the co-resident CTA limit of the device");
   // cilia
   std::vector<CiliumDev> cd(h->cil.size());
   std::vector<double> mid(h->cil.size()), ts(h->cil.size());
@@ -389,6 +417,10 @@ int build_md(mpcd_engine* h) {
   CK(dalloc(&m.tile_help, m.ntiles));
   CK(dalloc(&m.sp_start, ns + 1));
   CK(dalloc(&m.sp_other, nsp));
+  CK(dalloc(&m.sp_local, nsp));
+  CK(dalloc(&m.halo, halo.size()));
+  CK(dalloc(&m.halo_start, m.ntiles + 1));
+  CK(dalloc(&m.diag, nbond));
   CK(dalloc(&m.sp_kind, nsp));
   CK(dalloc(&m.sp_ref, nsp));
   CK(dalloc(&m.sp_rest, nsp));
@@ -416,6 +448,7 @@ int build_md(mpcd_engine* h) {
   CK(up(m.sp_start, start.data(), (ns + 1) * 4));
   if (nsp) {
     CK(up(m.sp_other, so.data(), nsp * 4));
+    CK(up(m.sp_local, sl.data(), nsp * 4));
     CK(up(m.sp_kind, sk.data(), nsp * 4));
     CK(up(m.sp_ref, sr.data(), nsp * 4));
     CK(up(m.sp_rest, srest.data(), nsp * 8));
@@ -427,9 +460,14 @@ int build_md(mpcd_engine* h) {
     CK(up(m.tstroke, ts.data(), cd.size() * 8));
   }
   if (nbond) {
+    std::vector<double> dg(nbond);
+    for (size_t k = 0; k < nbond; ++k) dg[k] = std::sqrt(0.5 * 0.5 + 0.5 * h->newlen[k]);
     CK(up(m.newlen, h->newlen.data(), nbond * 8));
     CK(up(m.oldlen, h->oldlen.data(), nbond * 8));
+    CK(up(m.diag, dg.data(), nbond * 8));
   }
+  if (!halo.empty()) CK(up(m.halo, halo.data(), halo.size() * 4));
+  CK(up(m.halo_start, hstart.data(), (m.ntiles + 1) * 4));
   CK(up(m.tile_cil, tcil.data(), (m.ntiles + 1) * 4));
   m.bar.count = h->d_bar;
   m.bar.gen = h->d_bar + 1;
@@ -603,10 +641,11 @@ int mpcd_destroy(mpcd_engine* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_fluid(h->f64);
   free_fluid(h->f64tmp);
-  cudaFree(h->f32.pos);
-  cudaFree(h->f32.vel);
-  cudaFree(h->f32tmp.pos);
-  cudaFree(h->f32tmp.vel);
+  for (FluidF32* f : {&h->f32, &h->f32tmp}) {
+    cudaFree(f->id);
+    cudaFree(f->pos);
+    cudaFree(f->vel);
+  }
   cudaFree(h->c64.sum);
   cudaFree(h->c64.cnt);
   cudaFree(h->c64.par);
@@ -662,6 +701,9 @@ int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel)
       }
       cell[i] = pack_cell(c[0], c[1], c[2]);
     }
+    std::vector<uint32_t> ids(n);
+    for (long i = 0; i < n; ++i) ids[i] = (uint32_t)i;
+    CK(cudaMemcpy(h->f64.id, ids.data(), n * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->f64.cell, cell.data(), n * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->f64.ox, o[0].data(), n * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->f64.oy, o[1].data(), n * 8, cudaMemcpyHostToDevice));
@@ -686,6 +728,9 @@ int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel)
       P[i] = make_float4(f[0], f[1], f[2], bits_to_float(pack_cell(c[0], c[1], c[2])));
       V[i] = make_float4((float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f);
     }
+    std::vector<uint32_t> ids(n);
+    for (long i = 0; i < n; ++i) ids[i] = (uint32_t)i;
+    CK(cudaMemcpy(h->f32.id, ids.data(), n * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->f32.pos, P.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->f32.vel, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
   }
@@ -712,28 +757,36 @@ int mpcd_get_fluid(mpcd_engine* h, long n, double* pos, double* vel) {
     CK(cudaMemcpy(v[0].data(), h->f64.vx, n * 8, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(v[1].data(), h->f64.vy, n * 8, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(v[2].data(), h->f64.vz, n * 8, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> ids(n);
+    CK(cudaMemcpy(ids.data(), h->f64.id, n * 4, cudaMemcpyDeviceToHost));
     for (long i = 0; i < n; ++i) {
+      const long d = ids[i];
+      if (d < 0 || d >= n) return fail(h, MPCD_EDEVICE, "particle id out of range");
       const int c[3] = {cell_x(cell[i]), cell_y(cell[i]), cell_z(cell[i])};
       for (int q = 0; q < 3; ++q) {
-        if (pos) pos[3 * i + q] = c[q] + o[q][i];
-        if (vel) vel[3 * i + q] = v[q][i];
+        if (pos) pos[3 * d + q] = c[q] + o[q][i];
+        if (vel) vel[3 * d + q] = v[q][i];
       }
     }
   } else {
     std::vector<float4> P(n), V(n);
     CK(cudaMemcpy(P.data(), h->f32.pos, n * sizeof(float4), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(V.data(), h->f32.vel, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> ids(n);
+    CK(cudaMemcpy(ids.data(), h->f32.id, n * 4, cudaMemcpyDeviceToHost));
     for (long i = 0; i < n; ++i) {
+      const long d = ids[i];
+      if (d < 0 || d >= n) return fail(h, MPCD_EDEVICE, "particle id out of range");
       uint32_t cp = float_to_bits(P[i].w);
       if (pos) {
-        pos[3 * i] = cell_x(cp) + (double)P[i].x;
-        pos[3 * i + 1] = cell_y(cp) + (double)P[i].y;
-        pos[3 * i + 2] = cell_z(cp) + (double)P[i].z;
+        pos[3 * d] = cell_x(cp) + (double)P[i].x;
+        pos[3 * d + 1] = cell_y(cp) + (double)P[i].y;
+        pos[3 * d + 2] = cell_z(cp) + (double)P[i].z;
       }
       if (vel) {
-        vel[3 * i] = V[i].x;
-        vel[3 * i + 1] = V[i].y;
-        vel[3 * i + 2] = V[i].z;
+        vel[3 * d] = V[i].x;
+        vel[3 * d + 1] = V[i].y;
+        vel[3 * d + 2] = V[i].z;
       }
     }
   }

@@ -14,6 +14,7 @@ namespace mpcd {
 // in-cell offset in [0,1) per axis.
 struct FluidF64 {
   long n = 0;
+  uint32_t* id = nullptr;  // caller's index of each particle (permuted by the sort)
   uint32_t* cell = nullptr;
   double *ox = nullptr, *oy = nullptr, *oz = nullptr;
   double *vx = nullptr, *vy = nullptr, *vz = nullptr;
@@ -22,6 +23,7 @@ struct FluidF64 {
 // Split-precision fluid: pos = {ox, oy, oz, cell bits}, vel = {vx, vy, vz, 0}.
 struct FluidF32 {
   long n = 0;
+  uint32_t* id = nullptr;  // caller's index of each particle (permuted by the sort)
   float4* pos = nullptr;
   float4* vel = nullptr;
 };
@@ -62,6 +64,8 @@ struct StepArgs {
 };
 
 // ------------------------------------------------------------------- MD ---
+int md_max_coresident_blocks(const struct MDState& m, int f32cells);
+
 struct CiliumDev {
   int kind, len, num_anker, slot0, bond_base;
   double beatstrength, bending, max_bend, m_speed, power_dur, recovery_dur, start;
@@ -85,6 +89,12 @@ struct MDState {
   // springs in CSR by target slot
   int* sp_start = nullptr;
   int* sp_other = nullptr;
+  int* sp_local = nullptr;   // other bead as an index into the tile's staged positions
+  int* halo = nullptr;       // per tile: global slots of other tiles' beads its springs reach
+  int* halo_start = nullptr; // ntiles + 1
+  int hmax = 0;              // largest halo of any tile
+  double* diag = nullptr;    // per bond: diagonal rest length sqrt(0.5^2 + 0.5 newlength)
+  int split = 0;             // 1: float spring arithmetic on hi/lo position pairs
   int* sp_kind = nullptr;
   int* sp_ref = nullptr;
   double* sp_rest = nullptr;

@@ -130,8 +130,12 @@ __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, c
   b[0] = ux - (A[0] * ux + A[1] * uy + A[2] * uz);
   b[1] = uy - (A[3] * ux + A[4] * uy + A[5] * uz);
   b[2] = uz - (A[6] * ux + A[7] * uy + A[8] * uz);
-  // kinetic energy removed by the thermostat: sum m v^2 - sum m v'^2 = E_rel (1 - sc^2)
-  ldiss += erel * (1.0 - sc * sc);
+  // dissipated energy (src/libcilia/mpcd.cpp:166-168, 232-234, 243-246): every
+  // cell adds sum m v^2 before the collision here, and every particle
+  // subtracts its m v'^2 after it (fluid_step, bead_collide), so the total
+  // matches the reference's bookkeeping including the rounding of its
+  // rotation constants
+  ldiss += s.w;
 }
 
 // ============================================================== float64 ===
@@ -211,6 +215,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
   const long long tnx = __double_as_longlong(a.ta_next[0]), tny = __double_as_longlong(a.ta_next[1]),
                   tnz = __double_as_longlong(a.ta_next[2]);
   const double h = a.h;
+  double ke_after = 0.0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
     const uint32_t cp = f.cell[i];
     int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
@@ -219,6 +224,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
     // collision with the map of the shifted cell
     const long cid = shifted(ix, ox, tcx, Lx) + (long)Lx * (shifted(iy, oy, tcy, Ly) + (long)Ly * shifted(iz, oz, tcz, Lz));
     apply_map_f64(c.par + 12 * cid, vx, vy, vz);
+    ke_after += vx * vx + vy * vy + vz * vz;
     // streaming
     if (a.walls == 0) {
       ox = fma(vx, h, ox);
@@ -259,6 +265,8 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
     f.vy[i] = vy;
     f.vz[i] = vz;
   }
+  const double tot = block_sum_f64(ke_after);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, -tot);
 }
 
 __global__ void k_bin_fluid_f64(FluidF64 f, CellsF64 c, StepArgs a) {
@@ -285,15 +293,19 @@ __device__ __forceinline__ long bead_cell(const Box& box, const double* a, doubl
 }
 
 __global__ void k_bead_collide_f64(MDState m, CellsF64 c, StepArgs a) {
+  double ke_after = 0.0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
     if (m.moves[s] != 1) continue;
     const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
     double vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
     apply_map_f64(c.par + 12 * cid, vx, vy, vz);
+    ke_after += a.bead_mass * (vx * vx + vy * vy + vz * vz);
     m.vx[s] = vx;
     m.vy[s] = vy;
     m.vz[s] = vz;
   }
+  const double tot = block_sum_f64(ke_after);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, -tot);
 }
 
 __global__ void k_bin_beads_f64(MDState m, CellsF64 c, StepArgs a) {
@@ -445,6 +457,7 @@ __global__ void k_sort_scatter_f64(FluidF64 src, FluidF64 dst, Box box, const ui
     const uint32_t cp = src.cell[i];
     const long c = box.lin(cell_x(cp), cell_y(cp), cell_z(cp));
     const long d = (long)start[c] + rank[i];
+    dst.id[d] = src.id[i];
     dst.cell[d] = cp;
     dst.ox[d] = src.ox[i];
     dst.oy[d] = src.oy[i];
@@ -461,6 +474,7 @@ __global__ void k_sort_scatter_f32(FluidF32 src, FluidF32 dst, Box box, const ui
     const uint32_t cp = __float_as_uint(p.w);
     const long c = box.lin(cell_x(cp), cell_y(cp), cell_z(cp));
     const long d = (long)start[c] + rank[i];
+    dst.id[d] = src.id[i];
     dst.pos[d] = p;
     dst.vel[d] = src.vel[i];
   }
@@ -541,6 +555,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF3
   const float tcx = (float)a.ta_cur[0], tcy = (float)a.ta_cur[1], tcz = (float)a.ta_cur[2];
   const float tnx = (float)a.ta_next[0], tny = (float)a.ta_next[1], tnz = (float)a.ta_next[2];
   const float h = (float)a.h, gk = (float)a.gkick;
+  float ke_after = 0.0f;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
     const float4 p = f.pos[i];
     const float4 v = f.vel[i];
@@ -549,6 +564,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF3
     float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
     const long cid = shifted_f(ix, ox, tcx, Lx) + (long)Lx * (shifted_f(iy, oy, tcy, Ly) + (long)Ly * shifted_f(iz, oz, tcz, Lz));
     apply_map_f32(c.par + 3 * cid, vx, vy, vz);
+    ke_after += vx * vx + vy * vy + vz * vz;
     if (a.walls == 0) {
       ox = fmaf(vx, h, ox);
       oy = fmaf(vy, h, oy);
@@ -581,6 +597,8 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF3
     f.pos[i] = make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz)));
     f.vel[i] = make_float4(vx, vy, vz, 0.f);
   }
+  const double tot = block_sum_f64((double)ke_after);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, -tot);
 }
 
 __global__ void k_bin_fluid_f32(FluidF32 f, CellsF32 c, StepArgs a) {
@@ -598,15 +616,19 @@ __global__ void k_bin_fluid_f32(FluidF32 f, CellsF32 c, StepArgs a) {
 }
 
 __global__ void k_bead_collide_f32(MDState m, CellsF32 c, StepArgs a) {
+  double ke_after = 0.0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
     if (m.moves[s] != 1) continue;
     const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
     float vx = (float)m.vx[s], vy = (float)m.vy[s], vz = (float)m.vz[s];
     apply_map_f32(c.par + 3 * cid, vx, vy, vz);
+    ke_after += a.bead_mass * ((double)vx * vx + (double)vy * vy + (double)vz * vz);
     m.vx[s] = vx;
     m.vy[s] = vy;
     m.vz[s] = vz;
   }
+  const double tot = block_sum_f64(ke_after);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, -tot);
 }
 
 __global__ void k_bin_beads_f32(MDState m, CellsF32 c, StepArgs a) {

@@ -651,6 +651,7 @@ Simulation::Simulation(const libconfig::Setting& root, const SimOptions& o) : op
   p.seed = seed;
   p.device = opt.device;
   p.sort_interval = opt.sort_interval;
+  p.md_split = opt.md_split;
   check(mpcd_create(&p, &eng), eng, "mpcd_create");
   mpcd_set_time(eng, wc.globalt);
   // MPCD::MPCD: grid shift from mpcd.dat or three draws (src/libcilia/mpcd.cpp:86-97)

@@ -188,6 +188,7 @@ struct SimOptions {
   double gravity = 0.0;
   double bead_mass = 5.0;
   int sort_interval = 0;
+  int md_split = -1;       // -1 auto, 0 float64 springs, 1 split springs
 };
 
 class Simulation {
