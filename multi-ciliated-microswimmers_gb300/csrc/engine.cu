@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -141,6 +142,7 @@ void free_md(MDState& m) {
   cudaFree(m.prim);
   cudaFree(m.nhelp);
   cudaFree(m.tile_help);
+  cudaFree(m.tile_react);
   cudaFree(m.sp_start);
   cudaFree(m.sp_other);
   cudaFree(m.sp_local);
@@ -229,6 +231,13 @@ StepArgs step_args(mpcd_engine* h, const double* a_cur, const double* a_next, do
   s.step = (uint64_t)h->steps + 1;
   s.err = h->d_err;
   s.diss = h->d_diss;
+  for (int q = 0; q < 3; ++q) {
+    s.fta_cur[q] = (float)s.ta_cur[q];
+    s.fta_next[q] = (float)s.ta_next[q];
+  }
+  s.fh = (float)s.h;
+  s.fgkick = (float)s.gkick;
+  s.fbead_mass = (float)s.bead_mass;
   return s;
 }
 
@@ -242,8 +251,12 @@ int check_launch(mpcd_engine* h, const char* what) {
 // owns 1 + h consecutive slots (h helper slots when its spring list is longer
 // than kChunk, each helper summing one chunk).  Every cilium occupies
 // contiguous slots of one tile; the other beads fill the remaining space.
-int build_md(mpcd_engine* h) {
-  const int kChunk = 32;
+int build_md(mpcd_engine* h, bool allow_cluster = true, bool no_react = false) {
+  // springs per helper slot: the longest serial spring chain of any thread.
+  // Odd, so that the helper slots' spring lists start in different
+  // shared-memory banks.
+  int kChunk = 31;
+  if (const char* env = std::getenv("MPCD_MD_CHUNK")) kChunk = std::max(2, std::min(256, std::atoi(env)));
   free_md(h->md);
   MDState& m = h->md;
   if (h->nb == 0) {
@@ -261,50 +274,244 @@ int build_md(mpcd_engine* h) {
   std::vector<int> width(nb);
   for (long b = 0; b < nb; ++b) width[b] = 1 + (nspr[b] > kChunk ? (nspr[b] + kChunk - 1) / kChunk - 1 : 0);
   std::vector<int> owner(nb, -1);  // cilium owning the bead
+  for (size_t c = 0; c < h->cil.size(); ++c)
+    for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) {
+      const long b = (long)h->cil[c].bead0 + k;
+      if (b < 0 || b >= nb) return fail(h, MPCD_EINVAL, "cilium bead range outside the bead array");
+      if (owner[b] >= 0) return fail(h, MPCD_EINVAL, "beads shared by two cilia");
+      owner[b] = (int)c;
+    }
+  // Hubs (a sphere's centre: one spring to every surface bead).  When every
+  // spring of a hub has an exact reverse partner inside the same run of
+  // non-cilium beads, the cluster layout drops the hub's own list and sums the
+  // partners' forces, negated, over the tile (react[j] marks the partners).
+  std::vector<int> run_id(nb, -1);
+  for (long b = 0, r = 0; b < nb; ++b)
+    if (owner[b] < 0) run_id[b] = (b > 0 && owner[b - 1] < 0) ? run_id[b - 1] : (int)r++;
+  std::vector<int> bstart(nb + 1, 0), blist(nsp);
+  for (long i = 0; i < nsp; ++i) bstart[h->sp_t[i] + 1]++;
+  for (long b = 0; b < nb; ++b) bstart[b + 1] += bstart[b];
+  {
+    std::vector<int> fillp(bstart.begin(), bstart.end() - 1);
+    for (long i = 0; i < nsp; ++i) blist[fillp[h->sp_t[i]]++] = (int)i;
+  }
+  std::vector<char> hub(nb, 0), react(nsp, 0), dropped(nsp, 0);
+  if (!no_react) {
+    for (long b = 0; b < nb; ++b) {
+      if (owner[b] >= 0 || nspr[b] <= kChunk) continue;
+      std::vector<int> partners;
+      bool ok = true;
+      for (int q = bstart[b]; q < bstart[b + 1] && ok; ++q) {
+        const int i = blist[q];
+        const int o = h->sp_o[i];
+        if (h->sp_k[i] != MPCD_SPRING_CONST || run_id[o] != run_id[b] || o == b) {
+          ok = false;
+          break;
+        }
+        int found = -1;
+        for (int r = bstart[o]; r < bstart[o + 1]; ++r) {
+          const int j = blist[r];
+          if (h->sp_o[j] == b && h->sp_k[j] == MPCD_SPRING_CONST && h->sp_rest[j] == h->sp_rest[i] &&
+              h->sp_kk[j] == h->sp_kk[i] && !react[j]) {
+            found = j;
+            break;
+          }
+        }
+        if (found < 0) ok = false;
+        else partners.push_back(found);
+      }
+      if (!ok) continue;
+      hub[b] = 1;
+      for (int j : partners) react[j] = 1;
+      for (int q = bstart[b]; q < bstart[b + 1]; ++q) dropped[blist[q]] = 1;
+    }
+  }
+  // every bead of a cilium owns the same number of slots (the kernels address
+  // a cilium's beads as slot0 + stride * (filament * rodlength + bead))
+  auto pad_cilia = [&]() {
+    for (size_t c = 0; c < h->cil.size(); ++c) {
+      int wmax = 1;
+      for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) wmax = std::max(wmax, width[h->cil[c].bead0 + k]);
+      for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) width[h->cil[c].bead0 + k] = wmax;
+    }
+  };
+  pad_cilia();
+  std::vector<int> width_grid = width;
+  int cl_chunk = kChunk;  // springs per slot of the chosen layout
   int maxw = 0;
   for (size_t c = 0; c < h->cil.size(); ++c) {
     const mpcd_cilium& cl = h->cil[c];
     int w = 0;
-    for (int k = 0; k < 3 * cl.rodlength; ++k) {
-      long b = (long)cl.bead0 + k;
-      if (b < 0 || b >= nb) return fail(h, MPCD_EINVAL, "cilium bead range outside the bead array");
-      if (owner[b] >= 0) return fail(h, MPCD_EINVAL, "beads shared by two cilia");
-      owner[b] = (int)c;
-      w += width[b];
-    }
+    for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[(long)cl.bead0 + k];
     maxw = std::max(maxw, w);
   }
   for (long b = 0; b < nb; ++b)
     if (owner[b] < 0) maxw = std::max(maxw, width[b]);
-  const int tile = std::max(32, ((maxw + 15) / 16) * 16);
-  if (tile > 1024) return fail(h, MPCD_EINVAL, "an MD group needs more than 1024 slots");
-  std::vector<int> fill;
-  std::vector<int> slot_of(nb, -1);
-  std::vector<int> cil_tile(h->cil.size());
-  for (size_t c = 0; c < h->cil.size(); ++c) {
-    const mpcd_cilium& cl = h->cil[c];
-    int w = 0;
-    for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[cl.bead0 + k];
-    if (fill.empty() || fill.back() + w > tile) fill.push_back(0);
-    const int t = (int)fill.size() - 1;
-    cil_tile[c] = t;
-    for (int k = 0; k < 3 * cl.rodlength; ++k) {
-      slot_of[cl.bead0 + k] = t * tile + fill[t];
-      fill[t] += width[cl.bead0 + k];
+  // Pack: cilia first (each contiguous in one tile), then the other beads in
+  // the remaining space.  Returns the number of tiles.
+  std::vector<int> fill, slot_of(nb, -1), cil_tile(h->cil.size());
+  auto pack = [&](int tile) {
+    fill.clear();
+    std::fill(slot_of.begin(), slot_of.end(), -1);
+    for (size_t c = 0; c < h->cil.size(); ++c) {
+      const mpcd_cilium& cl = h->cil[c];
+      int w = 0;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[cl.bead0 + k];
+      if (fill.empty() || fill.back() + w > tile) fill.push_back(0);
+      const int t = (int)fill.size() - 1;
+      cil_tile[c] = t;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) {
+        slot_of[cl.bead0 + k] = t * tile + fill[t];
+        fill[t] += width[cl.bead0 + k];
+      }
+    }
+    size_t tcur = 0;
+    for (long b = 0; b < nb; ++b) {
+      if (owner[b] >= 0) continue;
+      while (tcur < fill.size() && fill[tcur] + width[b] > tile) ++tcur;
+      if (tcur == fill.size()) fill.push_back(0);
+      slot_of[b] = (int)tcur * tile + fill[tcur];
+      fill[tcur] += width[b];
+    }
+    return (int)fill.size();
+  };
+  m.split = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 0) : (h->p.md_split ? 1 : 0);
+  // Cluster packing (split arithmetic): runs of consecutive non-cilium beads
+  // wider than 64 slots (a sphere, whose centre bead reaches every surface
+  // bead) each stay whole in one tile; cilia follow in order (next fit, so a
+  // tile's cilia have contiguous bond tables); the remaining beads fill gaps.
+  bool keep_hubs_whole = false;  // one-lane layout: hub runs stay in one tile (reactions)
+  auto pack_cluster = [&](int tile) {
+    fill.clear();
+    std::fill(slot_of.begin(), slot_of.end(), -1);
+    std::vector<std::pair<long, long>> runs;  // [begin, end) of non-cilium beads
+    for (long b = 0; b < nb;) {
+      if (owner[b] >= 0) {
+        ++b;
+        continue;
+      }
+      long e = b;
+      while (e < nb && owner[e] < 0) ++e;
+      runs.push_back({b, e});
+      b = e;
+    }
+    std::vector<char> placed(nb, 0);
+    for (auto& r : runs) {
+      long w = 0;
+      bool has_hub = false;
+      for (long b = r.first; b < r.second; ++b) {
+        w += width[b];
+        has_hub = has_hub || hub[b];
+      }
+      if (has_hub && keep_hubs_whole && w > tile) return 1 << 20;  // a hub's run must stay whole
+      if (w <= 64 || w > tile) continue;
+      fill.push_back(0);
+      const int t = (int)fill.size() - 1;
+      for (long b = r.first; b < r.second; ++b) {
+        slot_of[b] = t * tile + fill[t];
+        fill[t] += width[b];
+        placed[b] = 1;
+      }
+    }
+    const int first_cil_tile = (int)fill.size();
+    for (size_t c = 0; c < h->cil.size(); ++c) {
+      const mpcd_cilium& cl = h->cil[c];
+      int w = 0;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[cl.bead0 + k];
+      if ((int)fill.size() == first_cil_tile || fill.back() + w > tile) fill.push_back(0);
+      const int t = (int)fill.size() - 1;
+      cil_tile[c] = t;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) {
+        slot_of[cl.bead0 + k] = t * tile + fill[t];
+        fill[t] += width[cl.bead0 + k];
+      }
+    }
+    for (long b = 0; b < nb; ++b) {
+      if (owner[b] >= 0 || placed[b]) continue;
+      size_t t = 0;
+      while (t < fill.size() && fill[t] + width[b] > tile) ++t;
+      if (t == fill.size()) fill.push_back(0);
+      slot_of[b] = (int)t * tile + fill[t];
+      fill[t] += width[b];
+    }
+    return (int)fill.size();
+  };
+  int tile = 0;
+  m.cluster = 0;
+  if (m.split && allow_cluster) {
+    int lanes_hi = 2, lanes_lo = 1;
+    if (const char* env = std::getenv("MPCD_MD_LANES")) lanes_hi = lanes_lo = std::max(1, std::min(2, std::atoi(env)));
+    for (int lanes = lanes_hi; lanes >= lanes_lo && !m.cluster; --lanes) {
+      // one lane per slot: short chunks (two slots per cilium bead) keep the
+      // serial spring chains short; hubs take their force from reactions
+      const int chunk = lanes == 2 ? kChunk : std::min(kChunk, 11);
+      keep_hubs_whole = lanes == 1;
+      for (long b = 0; b < nb; ++b)
+        width[b] = (hub[b] && keep_hubs_whole) ? 1
+                                               : 1 + (nspr[b] > chunk ? (nspr[b] + chunk - 1) / chunk - 1 : 0);
+      cl_chunk = chunk;
+      pad_cilia();
+      int maxw_cl = 0;
+      for (size_t c = 0; c < h->cil.size(); ++c) {
+        int w = 0;
+        for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) w += width[h->cil[c].bead0 + k];
+        maxw_cl = std::max(maxw_cl, w);
+      }
+      for (long b = 0; b < nb; ++b)
+        if (owner[b] < 0) maxw_cl = std::max(maxw_cl, width[b]);
+      maxw = maxw_cl;
+      const int tmax = 1024 / lanes;
+      for (int t = std::max(32, ((maxw + 31) / 32) * 32); t <= tmax; t += 32)
+        if (pack_cluster(t) <= 16) {
+          tile = t;
+          m.cluster = 1;
+          m.cl_lanes = lanes;
+          break;
+        }
     }
   }
-  size_t tcur = 0;
-  for (long b = 0; b < nb; ++b) {
-    if (owner[b] >= 0) continue;
-    while (tcur < fill.size() && fill[tcur] + width[b] > tile) ++tcur;
-    if (tcur == fill.size()) fill.push_back(0);
-    slot_of[b] = (int)tcur * tile + fill[tcur];
-    fill[tcur] += width[b];
+  if (m.cluster && !keep_hubs_whole) {  // two-lane layout: hubs keep their own lists and helpers
+    std::fill(hub.begin(), hub.end(), 0);
+    std::fill(react.begin(), react.end(), 0);
+    std::fill(dropped.begin(), dropped.end(), 0);
+  }
+  if (!m.cluster) {
+    width = width_grid;
+    cl_chunk = kChunk;
+    std::fill(hub.begin(), hub.end(), 0);
+    std::fill(react.begin(), react.end(), 0);
+    std::fill(dropped.begin(), dropped.end(), 0);
+    maxw = 0;
+    for (size_t c = 0; c < h->cil.size(); ++c) {
+      int w = 0;
+      for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) w += width[h->cil[c].bead0 + k];
+      maxw = std::max(maxw, w);
+    }
+    for (long b = 0; b < nb; ++b)
+      if (owner[b] < 0) maxw = std::max(maxw, width[b]);
+    tile = std::max(32, ((maxw + 15) / 16) * 16);
+    if (tile > 1024) return fail(h, MPCD_EINVAL, "an MD group needs more than 1024 slots");
+    pack(tile);
+  }
+  // a hub and all its partners must share one tile, one hub per tile
+  std::vector<int> tile_react;
+  {
+    const int nt = (int)fill.size();
+    tile_react.assign(nt, -1);
+    bool bad = false;
+    for (long b = 0; b < nb && !bad; ++b) {
+      if (!hub[b]) continue;
+      const int t = slot_of[b] / tile;
+      if (tile_react[t] >= 0) bad = true;
+      tile_react[t] = slot_of[b] - t * tile;
+    }
+    for (long i = 0; i < nsp && !bad; ++i)
+      if (react[i] && slot_of[h->sp_t[i]] / tile != slot_of[h->sp_o[i]] / tile) bad = true;
+    if (bad) return build_md(h, allow_cluster, true);
   }
   m.tile = tile;
   m.ntiles = (int)fill.size();
   m.nslots = m.ntiles * tile;
-  m.split = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 0) : (h->p.md_split ? 1 : 0);
   const int ns = m.nslots;
   std::vector<double> X(ns, 0.0), Y(ns, 0.0), Z(ns, 0.0), VX(ns, 0.0), VY(ns, 0.0), VZ(ns, 0.0);
   std::vector<int> mv(ns, -1), prim(ns, 0), nhelp(ns, 0), thelp(m.ntiles, 0);
@@ -334,27 +541,33 @@ int build_md(mpcd_engine* h) {
   std::vector<int> seen(nb, 0);
   std::vector<int> sslot(nsp);
   for (long i = 0; i < nsp; ++i) {
+    if (dropped[i]) {
+      sslot[i] = -1;
+      continue;
+    }
     const int b = h->sp_t[i];
-    const int chunk = width[b] > 1 ? seen[b] / kChunk : 0;
+    const int chunk = width[b] > 1 ? seen[b] / cl_chunk : 0;
     seen[b]++;
     sslot[i] = slot_of[b] + chunk;
     start[sslot[i] + 1]++;
   }
   for (int s = 0; s < ns; ++s) start[s + 1] += start[s];
   std::vector<int> pos(start.begin(), start.end() - 1);
-  std::vector<int> so(nsp), sk(nsp), sr(nsp);
-  std::vector<double> srest(nsp), sm2k(nsp);
+  const long nspk = start[ns];  // springs kept
+  std::vector<int> so(nspk), sk(nspk), sr(nspk);
+  std::vector<double> srest(nspk), sm2k(nspk);
   for (long i = 0; i < nsp; ++i) {
+    if (sslot[i] < 0) continue;
     const int d = pos[sslot[i]]++;
     so[d] = slot_of[h->sp_o[i]];
-    sk[d] = h->sp_k[i];
+    sk[d] = h->sp_k[i] | (react[i] ? kSpringReact : 0);
     sr[d] = h->sp_r[i];
     srest[d] = h->sp_rest[i];
     sm2k[d] = -2.0 * h->sp_kk[i];
   }
   // halos: per tile the distinct slots of other tiles its springs reach, and
   // every spring's other bead as an index into the tile's staged positions
-  std::vector<int> sl(nsp), halo, hstart(m.ntiles + 1, 0);
+  std::vector<int> sl(nspk), halo, hstart(m.ntiles + 1, 0);
   int hmax = 0;
   for (int t = 0; t < m.ntiles; ++t) {
     const int b0 = t * tile, b1 = b0 + tile;
@@ -374,17 +587,29 @@ int build_md(mpcd_engine* h) {
     hmax = std::max(hmax, (int)ext.size());
   }
   m.hmax = hmax;
-  const int cap = md_max_coresident_blocks(m, h->p.precision == MPCD_FP32 ? 1 : 0);
-  if (m.ntiles > cap) return fail(h, MPCD_EINVAL, "MD tiles exceed the co-resident CTA limit of the device");
+  if (m.cluster) {
+    // per-tile maxima for the cluster kernel's shared-memory layout
+    m.cl_nsp_max = 0;
+    m.cl_nbond_max = 0;
+    std::vector<int> tb(m.ntiles, 0);
+    for (size_t c = 0; c < h->cil.size(); ++c) tb[cil_tile[c]] += h->cil[c].rodlength;
+    for (int t = 0; t < m.ntiles; ++t) {
+      m.cl_nsp_max = std::max(m.cl_nsp_max, start[(t + 1) * tile] - start[t * tile]);
+      m.cl_nbond_max = std::max(m.cl_nbond_max, tb[t]);
+    }
+    if (!md_cluster_feasible(m)) return build_md(h, false);  // grid layout instead
+  } else {
+    const int cap = md_max_coresident_blocks(m, h->p.precision == MPCD_FP32 ? 1 : 0);
+    if (m.ntiles > cap) return fail(h, MPCD_EINVAL, "MD tiles exceed the co-resident CTA limit of the device");
+  }
   // cilia
   std::vector<CiliumDev> cd(h->cil.size());
   std::vector<double> mid(h->cil.size()), ts(h->cil.size());
   std::vector<int> tcil(m.ntiles + 1, 0);
   for (size_t c = 0; c < h->cil.size(); ++c) {
     const mpcd_cilium& cl = h->cil[c];
-    for (int k = 0; k < 3 * cl.rodlength; ++k)
-      if (width[cl.bead0 + k] != 1) return fail(h, MPCD_EINVAL, "cilium bead with more than 32 springs");
     CiliumDev& d = cd[c];
+    d.stride = width[cl.bead0];
     d.kind = cl.kind;
     d.len = cl.rodlength;
     d.num_anker = cl.num_anker;
@@ -416,15 +641,16 @@ int build_md(mpcd_engine* h) {
   CK(dalloc(&m.nhelp, ns));
   CK(dalloc(&m.tile_help, m.ntiles));
   CK(dalloc(&m.sp_start, ns + 1));
-  CK(dalloc(&m.sp_other, nsp));
-  CK(dalloc(&m.sp_local, nsp));
+  CK(dalloc(&m.sp_other, nspk));
+  CK(dalloc(&m.sp_local, nspk));
   CK(dalloc(&m.halo, halo.size()));
   CK(dalloc(&m.halo_start, m.ntiles + 1));
   CK(dalloc(&m.diag, nbond));
-  CK(dalloc(&m.sp_kind, nsp));
-  CK(dalloc(&m.sp_ref, nsp));
-  CK(dalloc(&m.sp_rest, nsp));
-  CK(dalloc(&m.sp_m2k, nsp));
+  CK(dalloc(&m.sp_kind, nspk));
+  CK(dalloc(&m.sp_ref, nspk));
+  CK(dalloc(&m.sp_rest, nspk));
+  CK(dalloc(&m.sp_m2k, nspk));
+  CK(dalloc(&m.tile_react, m.ntiles));
   m.ncil = (int)h->cil.size();
   CK(dalloc(&m.cil, cd.size()));
   CK(dalloc(&m.midpnt, cd.size()));
@@ -446,14 +672,15 @@ int build_md(mpcd_engine* h) {
   CK(up(m.nhelp, nhelp.data(), ns * 4));
   CK(up(m.tile_help, thelp.data(), m.ntiles * 4));
   CK(up(m.sp_start, start.data(), (ns + 1) * 4));
-  if (nsp) {
-    CK(up(m.sp_other, so.data(), nsp * 4));
-    CK(up(m.sp_local, sl.data(), nsp * 4));
-    CK(up(m.sp_kind, sk.data(), nsp * 4));
-    CK(up(m.sp_ref, sr.data(), nsp * 4));
-    CK(up(m.sp_rest, srest.data(), nsp * 8));
-    CK(up(m.sp_m2k, sm2k.data(), nsp * 8));
+  if (nspk) {
+    CK(up(m.sp_other, so.data(), nspk * 4));
+    CK(up(m.sp_local, sl.data(), nspk * 4));
+    CK(up(m.sp_kind, sk.data(), nspk * 4));
+    CK(up(m.sp_ref, sr.data(), nspk * 4));
+    CK(up(m.sp_rest, srest.data(), nspk * 8));
+    CK(up(m.sp_m2k, sm2k.data(), nspk * 8));
   }
+  CK(up(m.tile_react, tile_react.data(), m.ntiles * 4));
   if (!cd.empty()) {
     CK(up(m.cil, cd.data(), cd.size() * sizeof(CiliumDev)));
     CK(up(m.midpnt, mid.data(), cd.size() * 8));
@@ -521,7 +748,7 @@ int device_error(mpcd_engine* h) {
   if (e & kErrGammaMissing) msg += " injected gamma missing for a thermostatted cell;";
   if (e & kErrGammaLoop) msg += " Gamma sampler exceeded its iteration cap;";
   if (e & kErrBarrier) msg += " MD grid barrier timed out;";
-  if (e & kErrCellRange) msg += " cell index out of range;";
+  if (e & kErrCellRange) msg += " non-finite or out-of-range coordinate (unstable MD step?);";
   if (e & kErrCellOverflow) msg += " cell occupancy overflow;";
   cudaMemset(h->d_err, 0, sizeof(unsigned));
   return fail(h, MPCD_EDEVICE, msg);
@@ -597,6 +824,10 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
   for (int q = 0; q < 3; ++q) h->box.L[q] = p.sizes[q];
   h->ncell = (long)p.sizes[0] * p.sizes[1] * p.sizes[2];
   h->nsub = (int)((p.tstep + 0.00000001) / p.ststep);
+  if (h->nsub < 1 || h->nsub > 511) {
+    delete h;
+    return MPCD_EINVAL;  // 1 .. 511 MD substeps per MPC step
+  }
   auto bail = [&](cudaError_t e, const char* what) {
     fprintf(stderr, "mpcd_create: %s: %s\n", what, cudaGetErrorString(e));
     mpcd_destroy(h);
@@ -683,6 +914,10 @@ long mpcd_fluid_count(const mpcd_engine* h) {
 
 int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel) {
   if (!h || n < 0 || (n > 0 && (!pos || !vel))) return fail(h, MPCD_EINVAL, "set_fluid: bad arguments");
+  if (n > 0x7fffffffL) return fail(h, MPCD_EINVAL, "set_fluid: more than 2^31 - 1 particles");
+  for (long i = 0; i < 3 * n; ++i)
+    if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || std::fabs(pos[i]) > 1e12)
+      return fail(h, MPCD_EINVAL, "set_fluid: non-finite or out-of-range position or velocity");
   int rc = alloc_fluid(h, n);
   if (rc) return rc;
   const int* L = h->box.L;
@@ -819,6 +1054,9 @@ int mpcd_get_time(mpcd_engine* h, double* t) {
 
 int mpcd_set_beads(mpcd_engine* h, long nb, const double* pos, const double* vel, const int* moves) {
   if (!h || nb < 0 || (nb > 0 && (!pos || !vel))) return fail(h, MPCD_EINVAL, "set_beads: bad arguments");
+  for (long i = 0; i < 3 * nb; ++i)
+    if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || std::fabs(pos[i]) > 1e12)
+      return fail(h, MPCD_EINVAL, "set_beads: non-finite or out-of-range position or velocity");
   if (h->nb != nb) {
     h->md_dirty = true;
     h->nb = nb;
@@ -973,6 +1211,16 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
   ma.dt = h->p.ststep;
   ma.tstep = h->p.tstep;
   ma.n = h->nsub;
+  ma.t_end = t_move;
+  // rest-length refresh schedule of the force evaluations (src/cilia.cpp:206-215):
+  // evaluation 0 and 1 at t0, evaluation k+1 after k additions of ststep
+  {
+    double te = t0;
+    for (int e = 0; e <= h->nsub && e < 512; ++e) {
+      if (e >= 2) te += h->p.ststep;
+      if (std::fmod(te + h->p.ststep / 10., 0.01) < h->p.ststep) ma.refresh[e >> 6] |= 1ull << (e & 63);
+    }
+  }
   ma.box = h->box;
   for (int q = 0; q < 3; ++q) {
     ma.a_cur[q] = h->a[q];
@@ -998,8 +1246,12 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
                          : launch_bead_collide_f32(h->md, h->c32, s, h->stream);
     }
     ProfScope ps(h, MPCD_K_MD);
-    h->launches += f64 ? launch_md_f64(h->md, h->c64, ma, h->stream, &coop)
-                       : launch_md_f32cells(h->md, h->c32, ma, h->stream, &coop);
+    if (h->md.cluster)
+      h->launches += f64 ? launch_md_cluster_f64cells(h->md, h->c64, ma, h->stream, &coop)
+                         : launch_md_cluster_f32cells(h->md, h->c32, ma, h->stream, &coop);
+    else
+      h->launches += f64 ? launch_md_f64(h->md, h->c64, ma, h->stream, &coop)
+                         : launch_md_f32cells(h->md, h->c32, ma, h->stream, &coop);
   }
   if (coop != cudaSuccess) return cuda_fail(h, coop, "cooperative MD launch");
   int rc = check_launch(h, "step");

@@ -61,13 +61,20 @@ struct StepArgs {
   const double* inj_axis;   // device, or nullptr
   unsigned* err;
   double* diss;       // accumulated dissipated energy (float64)
+  // float copies for the split-precision kernels (no conversions per thread)
+  float fta_cur[3], fta_next[3], fh, fgkick, fbead_mass;
 };
 
 // ------------------------------------------------------------------- MD ---
+// spring kind flag: the spring's force, negated, is also owed to its other
+// bead (a hub whose own list was dropped); only in the cluster layout
+constexpr int kSpringReact = 8;
 int md_max_coresident_blocks(const struct MDState& m, int f32cells);
+int md_cluster_feasible(const struct MDState& m);
 
 struct CiliumDev {
   int kind, len, num_anker, slot0, bond_base;
+  int stride;  // slots per bead (every bead of a cilium owns the same number of slots)
   double beatstrength, bending, max_bend, m_speed, power_dur, recovery_dur, start;
 };
 
@@ -86,6 +93,7 @@ struct MDState {
   int* prim = nullptr;   // helper slot -> primary slot of its bead; primary -> itself
   int* nhelp = nullptr;  // primary slot -> number of helper slots following it
   int* tile_help = nullptr;  // per tile: 1 if it holds helper slots
+  int* tile_react = nullptr; // per tile: local slot of a hub fed by reactions, or -1
   // springs in CSR by target slot
   int* sp_start = nullptr;
   int* sp_other = nullptr;
@@ -95,6 +103,10 @@ struct MDState {
   int hmax = 0;              // largest halo of any tile
   double* diag = nullptr;    // per bond: diagonal rest length sqrt(0.5^2 + 0.5 newlength)
   int split = 0;             // 1: float spring arithmetic on hi/lo position pairs
+  int cluster = 0;           // 1: whole bead set in one thread-block cluster (md_cluster.cu)
+  int cl_nsp_max = 0;        // cluster layout: most springs of one tile
+  int cl_nbond_max = 0;      // cluster layout: most bond-table entries of one tile
+  int cl_lanes = 2;          // cluster layout: threads per slot (1 or 2)
   int* sp_kind = nullptr;
   int* sp_ref = nullptr;
   double* sp_rest = nullptr;
@@ -112,6 +124,8 @@ struct MDState {
 
 struct MDStepArgs {
   double t0, dt, tstep;
+  double t_end;           // simulation time after the n substeps
+  uint64_t refresh[8];    // bit e: force evaluation e (0 .. n) refreshes the beat rest lengths
   int n;
   Box box;
   double a_cur[3], a_next[3];
@@ -140,6 +154,10 @@ int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a
 int launch_bead_collide_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);
 int launch_bin_beads_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);
 int launch_md_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+int launch_md_cluster_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s,
+                               cudaError_t* st);
+int launch_md_cluster_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s,
+                               cudaError_t* st);
 int launch_observables_f32(const FluidF32& f, const MDState& m, double bead_mass, double* out, cudaStream_t s);
 int launch_sort_f32(FluidF32& f, FluidF32& tmp, const Box& box, uint32_t* count, uint32_t* start,
                     uint32_t* rank, uint32_t* blocksums, cudaStream_t s);

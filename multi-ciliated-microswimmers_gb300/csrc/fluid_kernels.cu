@@ -21,11 +21,39 @@ namespace {
 
 constexpr int kThreads = 256;
 
-inline int grid_for(long n, int threads = kThreads) {
+// Persistent grid-stride sizing: a few resident CTAs per SM, every thread
+// handling many particles, so per-thread set-up and reductions amortise.
+inline int sm_count() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+inline int grid_for(long n, int threads = kThreads, int per_sm = 4) {
   long g = (n + threads - 1) / threads;
   if (g < 1) g = 1;
-  if (g > 152L * 64) g = 152L * 64;  // grid-stride beyond this
-  return (int)g;
+  const long cap = (long)sm_count() * per_sm;
+  return (int)(g < cap ? g : cap);
+}
+
+// sum over the block, float lanes, one float64 result (thread 0)
+__device__ __forceinline__ double block_sum_f32(float v) {
+  __shared__ double red32[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red32[wid] = (double)v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += red32[w];
+  return r;
 }
 
 __device__ __forceinline__ double block_sum_f64(double v) {
@@ -54,9 +82,14 @@ __device__ __forceinline__ int shifted(int i, double o, long long ta_bits, int L
 }
 
 // reduce an offset that left [0,1) back into the cell (rare path)
-__device__ __forceinline__ void rewrap(double& o, int& i, int L) {
+__device__ __forceinline__ void rewrap(double& o, int& i, int L, unsigned& bad) {
   long long b = __double_as_longlong(o);
   if (b < 0 || b >= 0x3FF0000000000000LL) {
+    if (!(o > -1.0e9 && o < 1.0e9)) {  // non-finite: keep the particle in its cell and report
+      o = 0.5;
+      bad |= kErrCellRange;
+      return;
+    }
     double fl = floor(o);
     o -= fl;
     i += (int)fl;
@@ -69,22 +102,14 @@ __device__ __forceinline__ void rewrap(double& o, int& i, int L) {
   }
 }
 
-// the reference's cell of an unwrapped coordinate: floor(x+a) - floor((x+a)/L) L
-__device__ __forceinline__ int ref_cell_axis(double x, double a, int L) {
-  double xa = x + a;
-  int c = (int)(floor(xa) - floor(xa / L) * L);
-  if (c < 0) c += L;  // guards the rounding edge where (x+a)/L rounds up to an integer
-  if (c >= L) c -= L;
-  return c;
-}
-
 __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, const StepArgs& a, double* A,
                                               double* b, double& ldiss, unsigned& errbits, bool& gfail) {
   const int nf = cnt_fluid(w), nb = cnt_beads(w);
   const int num = nf + nb;
   const double M = (double)nf + (double)nb * a.bead_mass;
-  const double ux = s.x / M, uy = s.y / M, uz = s.z / M;
-  const double erel = s.w - (ux * ux + uy * uy + uz * uz) * M;
+  const double inv = 1.0 / M;
+  const double ux = s.x * inv, uy = s.y * inv, uz = s.z * inv;
+  const double erel = s.w - (ux * s.x + uy * s.y + uz * s.z);  // K - M u^2
   double sc = 1.0;
   if (erel > 0 && num > 1) {
     double g;
@@ -105,7 +130,19 @@ __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, c
     ry = a.inj_axis[3 * cid + 1];
     rz = a.inj_axis[3 * cid + 2];
   } else {
-    random_axis(a.seed, a.step, (uint32_t)cid, rx, ry, rz);
+    // direction drawn in float, normalised in float64 so that R is orthogonal to float64 precision
+    const u32x4 r = draw4(a.seed, a.step, kStreamCell, (uint32_t)cid, 0u);
+    const float ct = 2.0f * u01_flt(r.y) - 1.0f;
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    float sp, cp;
+    sincospif(2.0f * u01_flt(r.x), &sp, &cp);
+    rx = (double)(st * cp);
+    ry = (double)(st * sp);
+    rz = (double)ct;
+    const double nrm = rsqrt(rx * rx + ry * ry + rz * rz);
+    rx *= nrm;
+    ry *= nrm;
+    rz *= nrm;
   }
   const double ca = kCosAlpha, sa = kSinAlpha, oc = 1.0 - kCosAlpha;
   // rotation about (rx, ry, rz) by alpha, entries as src/libcilia/mpcd.cpp:285-293
@@ -216,6 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
                   tnz = __double_as_longlong(a.ta_next[2]);
   const double h = a.h;
   double ke_after = 0.0;
+  unsigned bad = 0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
     const uint32_t cp = f.cell[i];
     int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
@@ -224,7 +262,8 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
     // collision with the map of the shifted cell
     const long cid = shifted(ix, ox, tcx, Lx) + (long)Lx * (shifted(iy, oy, tcy, Ly) + (long)Ly * shifted(iz, oz, tcz, Lz));
     apply_map_f64(c.par + 12 * cid, vx, vy, vz);
-    ke_after += vx * vx + vy * vy + vz * vz;
+    const double k_post = vx * vx + vy * vy + vz * vz;
+    ke_after += k_post;
     // streaming
     if (a.walls == 0) {
       ox = fma(vx, h, ox);
@@ -244,13 +283,13 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
       iy = (((int)fy % Ly) + Ly) % Ly;
       iz = (((int)fz % Lz) + Lz) % Lz;
     }
-    rewrap(ox, ix, Lx);
-    rewrap(oy, iy, Ly);
-    rewrap(oz, iz, Lz);
+    rewrap(ox, ix, Lx, bad);
+    rewrap(oy, iy, Ly, bad);
+    rewrap(oz, iz, Lz, bad);
     if (a.gkick != 0.0) vx += a.gkick;
     // bin with the next shift
     const long cn = shifted(ix, ox, tnx, Lx) + (long)Lx * (shifted(iy, oy, tny, Ly) + (long)Ly * shifted(iz, oz, tnz, Lz));
-    const double K = vx * vx + vy * vy + vz * vz;
+    const double K = (a.gkick != 0.0 || a.walls != 0) ? vx * vx + vy * vy + vz * vz : k_post;
     double* sp = reinterpret_cast<double*>(c.sum + cn);
     atomicAdd(sp + 0, vx);
     atomicAdd(sp + 1, vy);
@@ -265,6 +304,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
     f.vy[i] = vy;
     f.vz[i] = vz;
   }
+  if (bad) atomicOr(a.err, bad);
   const double tot = block_sum_f64(ke_after);
   if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, -tot);
 }
@@ -287,16 +327,15 @@ __global__ void k_bin_fluid_f64(FluidF64 f, CellsF64 c, StepArgs a) {
   }
 }
 
-__device__ __forceinline__ long bead_cell(const Box& box, const double* a, double x, double y, double z) {
-  return ref_cell_axis(x, a[0], box.L[0]) +
-         (long)box.L[0] * (ref_cell_axis(y, a[1], box.L[1]) + (long)box.L[1] * ref_cell_axis(z, a[2], box.L[2]));
-}
-
 __global__ void k_bead_collide_f64(MDState m, CellsF64 c, StepArgs a) {
   double ke_after = 0.0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
     if (m.moves[s] != 1) continue;
-    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    const long cid = unwrapped_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    if (cid < 0) {
+      atomicOr(a.err, kErrCellRange);
+      continue;
+    }
     double vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
     apply_map_f64(c.par + 12 * cid, vx, vy, vz);
     ke_after += a.bead_mass * (vx * vx + vy * vy + vz * vz);
@@ -311,7 +350,11 @@ __global__ void k_bead_collide_f64(MDState m, CellsF64 c, StepArgs a) {
 __global__ void k_bin_beads_f64(MDState m, CellsF64 c, StepArgs a) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
     if (m.moves[s] != 1) continue;
-    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    const long cid = unwrapped_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    if (cid < 0) {
+      atomicOr(a.err, kErrCellRange);
+      continue;
+    }
     const double mb = a.bead_mass, vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
     double* sp = reinterpret_cast<double*>(c.sum + cid);
     atomicAdd(sp + 0, vx * mb);
@@ -498,8 +541,13 @@ __device__ __forceinline__ int shifted_f(int i, float o, float ta, int L) {
   return s == L ? 0 : s;
 }
 
-__device__ __forceinline__ void rewrap_f(float& o, int& i, int L) {
+__device__ __forceinline__ void rewrap_f(float& o, int& i, int L, unsigned& bad) {
   if (o < 0.0f || o >= 1.0f) {
+    if (!(o > -1.0e9f && o < 1.0e9f)) {
+      o = 0.5f;
+      bad |= kErrCellRange;
+      return;
+    }
     float fl = floorf(o);
     o -= fl;
     i += (int)fl;
@@ -517,26 +565,70 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float4 v) {
                : "memory");
 }
 
+// Split-precision collision map: everything per cell in float (the sums
+// are float); the dissipated-energy bookkeeping accumulates in float64.
 __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
-  double ldiss = 0.0;
+  float ldiss = 0.0f;
   unsigned errbits = 0;
   bool gfail = false;
+  const float mb = a.fbead_mass;
+  const float ca = (float)kCosAlpha, sa = (float)kSinAlpha, oc = 1.0f - (float)kCosAlpha;
   for (long cid = (long)blockIdx.x * blockDim.x + threadIdx.x; cid < c.ncell; cid += (long)gridDim.x * blockDim.x) {
     const uint32_t w = c.cnt[cid];
     if (w == 0) continue;
-    const float4 sf = c.sum[cid];
+    const float4 s = c.sum[cid];
     c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
     c.cnt[cid] = 0u;
-    double A[9], b[3];
-    collision_map(make_double4(sf.x, sf.y, sf.z, sf.w), w, cid, a, A, b, ldiss, errbits, gfail);
+    const int nf = cnt_fluid(w), nb = cnt_beads(w);
+    const int num = nf + nb;
+    const float M = (float)nf + (float)nb * mb;
+    const float inv = 1.0f / M;
+    const float ux = s.x * inv, uy = s.y * inv, uz = s.z * inv;
+    const float erel = s.w - (ux * s.x + uy * s.y + uz * s.z);
+    float sc = 1.0f;
+    if (erel > 0.f && num > 1) {
+      float g;
+      if (a.inj_gamma) {
+        g = (float)a.inj_gamma[cid];
+        if (g < 0.f) {
+          errbits |= kErrGammaMissing;
+          g = 0.f;
+        }
+      } else {
+        g = gamma_mt(num, a.seed, a.step, (uint32_t)cid, &gfail);
+      }
+      sc = sqrtf(2.0f * g / erel);
+    }
+    float rx, ry, rz;
+    if (a.inj_axis) {
+      rx = (float)a.inj_axis[3 * cid + 0];
+      ry = (float)a.inj_axis[3 * cid + 1];
+      rz = (float)a.inj_axis[3 * cid + 2];
+    } else {
+      const u32x4 r = draw4(a.seed, a.step, kStreamCell, (uint32_t)cid, 0u);
+      const float ct = 2.0f * u01_flt(r.y) - 1.0f;
+      const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+      float sp, cp;
+      sincospif(2.0f * u01_flt(r.x), &sp, &cp);
+      rx = st * cp;
+      ry = st * sp;
+      rz = ct;
+    }
+    const float A00 = sc * (rx * rx + (1.0f - rx * rx) * ca), A01 = sc * (rx * ry * oc - rz * sa),
+                A02 = sc * (rx * rz * oc + ry * sa);
+    const float A10 = sc * (rx * ry * oc + rz * sa), A11 = sc * (ry * ry + (1.0f - ry * ry) * ca),
+                A12 = sc * (ry * rz * oc - rx * sa);
+    const float A20 = sc * (rx * rz * oc - ry * sa), A21 = sc * (ry * rz * oc + rx * sa),
+                A22 = sc * (rz * rz + (1.0f - rz * rz) * ca);
     float4* p = c.par + 3 * cid;
-    p[0] = make_float4((float)A[0], (float)A[1], (float)A[2], (float)b[0]);
-    p[1] = make_float4((float)A[3], (float)A[4], (float)A[5], (float)b[1]);
-    p[2] = make_float4((float)A[6], (float)A[7], (float)A[8], (float)b[2]);
+    p[0] = make_float4(A00, A01, A02, ux - (A00 * ux + A01 * uy + A02 * uz));
+    p[1] = make_float4(A10, A11, A12, uy - (A10 * ux + A11 * uy + A12 * uz));
+    p[2] = make_float4(A20, A21, A22, uz - (A20 * ux + A21 * uy + A22 * uz));
+    ldiss += s.w;
   }
   if (gfail) errbits |= kErrGammaLoop;
   if (errbits) atomicOr(a.err, errbits);
-  double tot = block_sum_f64(ldiss);
+  const double tot = block_sum_f32(ldiss);
   if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
 }
 
@@ -552,10 +644,11 @@ __device__ __forceinline__ void apply_map_f32(const float4* par, float& vx, floa
 
 __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF32 c, StepArgs a) {
   const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
-  const float tcx = (float)a.ta_cur[0], tcy = (float)a.ta_cur[1], tcz = (float)a.ta_cur[2];
-  const float tnx = (float)a.ta_next[0], tny = (float)a.ta_next[1], tnz = (float)a.ta_next[2];
-  const float h = (float)a.h, gk = (float)a.gkick;
+  const float tcx = a.fta_cur[0], tcy = a.fta_cur[1], tcz = a.fta_cur[2];
+  const float tnx = a.fta_next[0], tny = a.fta_next[1], tnz = a.fta_next[2];
+  const float h = a.fh, gk = a.fgkick;
   float ke_after = 0.0f;
+  unsigned bad = 0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
     const float4 p = f.pos[i];
     const float4 v = f.vel[i];
@@ -587,23 +680,24 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF3
       vy = (float)dvy;
       vz = (float)dvz;
     }
-    rewrap_f(ox, ix, Lx);
-    rewrap_f(oy, iy, Ly);
-    rewrap_f(oz, iz, Lz);
-    vx += gk;
+    rewrap_f(ox, ix, Lx, bad);
+    rewrap_f(oy, iy, Ly, bad);
+    rewrap_f(oz, iz, Lz, bad);
+    if (gk != 0.0f) vx += gk;
     const long cn = shifted_f(ix, ox, tnx, Lx) + (long)Lx * (shifted_f(iy, oy, tny, Ly) + (long)Ly * shifted_f(iz, oz, tnz, Lz));
     red_add_v4(c.sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
     atomicAdd(c.cnt + cn, 1u);
     f.pos[i] = make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz)));
     f.vel[i] = make_float4(vx, vy, vz, 0.f);
   }
-  const double tot = block_sum_f64((double)ke_after);
+  if (bad) atomicOr(a.err, bad);
+  const double tot = block_sum_f32(ke_after);
   if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, -tot);
 }
 
 __global__ void k_bin_fluid_f32(FluidF32 f, CellsF32 c, StepArgs a) {
   const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
-  const float tcx = (float)a.ta_cur[0], tcy = (float)a.ta_cur[1], tcz = (float)a.ta_cur[2];
+  const float tcx = a.fta_cur[0], tcy = a.fta_cur[1], tcz = a.fta_cur[2];
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
     const float4 p = f.pos[i];
     const float4 v = f.vel[i];
@@ -619,7 +713,11 @@ __global__ void k_bead_collide_f32(MDState m, CellsF32 c, StepArgs a) {
   double ke_after = 0.0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
     if (m.moves[s] != 1) continue;
-    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    const long cid = unwrapped_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    if (cid < 0) {
+      atomicOr(a.err, kErrCellRange);
+      continue;
+    }
     float vx = (float)m.vx[s], vy = (float)m.vy[s], vz = (float)m.vz[s];
     apply_map_f32(c.par + 3 * cid, vx, vy, vz);
     ke_after += a.bead_mass * ((double)vx * vx + (double)vy * vy + (double)vz * vz);
@@ -634,7 +732,11 @@ __global__ void k_bead_collide_f32(MDState m, CellsF32 c, StepArgs a) {
 __global__ void k_bin_beads_f32(MDState m, CellsF32 c, StepArgs a) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
     if (m.moves[s] != 1) continue;
-    const long cid = bead_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    const long cid = unwrapped_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    if (cid < 0) {
+      atomicOr(a.err, kErrCellRange);
+      continue;
+    }
     const float mb = (float)a.bead_mass;
     const float vx = (float)m.vx[s], vy = (float)m.vy[s], vz = (float)m.vz[s];
     red_add_v4(c.sum + cid, make_float4(vx * mb, vy * mb, vz * mb, mb * (vx * vx + vy * vy + vz * vz)));

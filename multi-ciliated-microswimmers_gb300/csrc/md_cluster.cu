@@ -1,0 +1,490 @@
+// Split-precision MD substeps on one thread-block cluster per swimmer.
+//
+// The same physics as md_kernels.cu (src/libcilia/mdobject.cpp:36-72,
+// src/cilia.cpp:79-239, src/sphere.cpp:87-119, src/clami.cpp:188-198,
+// src/simulation.cpp:217-265), laid out for a cluster of up to 16 CTAs:
+//  - every CTA owns one tile of bead slots (two lanes per slot) and keeps its
+//    springs, its cilia's bond tables and two buffers of positions (float
+//    hi/lo pairs) in shared memory for the whole launch;
+//  - beads of other CTAs that a tile's springs reach are read through
+//    distributed shared memory from the owner's current position buffer;
+//  - one hardware cluster barrier per substep orders the position writes of
+//    substep k before the reads of substep k+1 (the buffers alternate, so
+//    nobody overwrites what another CTA may still be reading).
+// Nothing goes through global memory between substeps.  State (positions,
+// velocities) and the integration stay float64 in registers.
+#include <cooperative_groups.h>
+
+#include "engine_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace mpcd {
+
+namespace {
+
+
+// Cilia::length(i) (src/cilia.cpp:79-121) in float arithmetic
+__device__ float cl_cilium_length(const CiliumDev& cl, int i, float midpnt, float oldlen, float tl) {
+  const float bondlength = 0.5f, beat = (float)cl.beatstrength, bend = (float)cl.bending;
+  float l;
+  if ((float)i < midpnt - 2.0f) {
+    const float base = 1.0f - ((float)i - cl.num_anker - 1.0f) / (float)(cl.len - cl.num_anker - 1);
+    l = bondlength + beat * (base * base * sqrtf(base)) * 0.5f * (1.0f - 1.0f / (midpnt - (float)i - 1.0f));
+  } else {
+    const float di = (float)i - midpnt;
+    l = bondlength - 2.0f * beat / (di * di + 1.0f);
+  }
+  if (fabsf(l - tl) > bend) {
+    tl = tl + bend - 2.0f * bend * (l < tl ? 1.0f : 0.0f);
+    l = (l - oldlen) * (tl - oldlen) > 0.0f ? tl : oldlen;
+  }
+  return l;
+}
+
+// one position buffer: six float arrays of length np (hi x,y,z then lo x,y,z)
+struct PBuf {
+  float* p;
+  int np;
+  __device__ float* hx() const { return p; }
+  __device__ void put(int i, const float* h, const float* l) const {
+    p[i] = h[0];
+    p[np + i] = h[1];
+    p[2 * np + i] = h[2];
+    p[3 * np + i] = l[0];
+    p[4 * np + i] = l[1];
+    p[5 * np + i] = l[2];
+  }
+  // |x_i - x_j| from the hi/lo pairs, in float
+  __device__ float dist(int i, int j) const {
+    const float dx = (p[i] - p[j]) + (p[3 * np + i] - p[3 * np + j]);
+    const float dy = (p[np + i] - p[np + j]) + (p[4 * np + i] - p[4 * np + j]);
+    const float dz = (p[2 * np + i] - p[2 * np + j]) + (p[5 * np + i] - p[5 * np + j]);
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+  }
+};
+
+struct ClusterLayout {
+  int np, nsp_max, nbond_max;
+  __host__ __device__ size_t bytes(int T) const {
+    size_t b = 2 * 6 * sizeof(float) * (size_t)np;           // two position buffers
+    b += (size_t)nsp_max * (sizeof(uint32_t) + 2 * sizeof(float));  // springs
+    b += (size_t)nbond_max * 3 * sizeof(float);                      // bond tables
+    b = (b + 15) & ~(size_t)15;
+    b += 3 * sizeof(float) * (size_t)T;                         // helper partial forces
+    return b;
+  }
+};
+
+template <int kCLanes, typename Bin>
+__global__ void __launch_bounds__(1024, 1) k_md_cluster(MDState m, MDStepArgs a, Bin bin, ClusterLayout lay) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int T = m.tile;
+  const int np = lay.np;
+  const int tile = blockIdx.x;
+  const int first_tile = tile - (int)cluster.block_rank();
+  const int base = tile * T;
+  // carve shared memory
+  unsigned char* ptr = smem;
+  float* const pbase = reinterpret_cast<float*>(ptr);  // buffer b at pbase + b * 6 * np
+  auto buf = [&](int b) { return PBuf{pbase + b * 6 * np, np}; };
+  ptr += 2 * 6 * sizeof(float) * (size_t)np;
+  uint32_t* sw = reinterpret_cast<uint32_t*>(ptr);
+  float* srest = reinterpret_cast<float*>(sw + lay.nsp_max);
+  float* sm2k = srest + lay.nsp_max;
+  ptr = reinterpret_cast<unsigned char*>(sm2k + lay.nsp_max);
+  float* bnew = reinterpret_cast<float*>(ptr);
+  float* bold = bnew + lay.nbond_max;
+  float* bdiag = bold + lay.nbond_max;
+  ptr = reinterpret_cast<unsigned char*>(bdiag + lay.nbond_max);
+  float* part = reinterpret_cast<float*>(((uintptr_t)ptr + 15) & ~(uintptr_t)15);
+
+  // per-tile constants
+  const int sp0 = m.sp_start[base], sp1 = m.sp_start[base + T];
+  const int c0 = m.tile_cil[tile], c1 = m.tile_cil[tile + 1];
+  const int bond0 = c1 > c0 ? m.cil[c0].bond_base : 0;
+  const int nbond = c1 > c0 ? m.cil[c1 - 1].bond_base + m.cil[c1 - 1].len - bond0 : 0;
+  const int h0 = m.halo_start[tile], hn = m.halo_start[tile + 1] - h0;
+  // stage springs and bond tables
+  for (int s = sp0 + (int)threadIdx.x; s < sp1; s += blockDim.x) {
+    const int k = s - sp0;
+    const int kraw = m.sp_kind[s];
+    const int kind = kraw & 3;
+    // bond-table index for BOND/DIAG springs; bit 13 marks a reaction owed to a hub
+    const int bl = kind >= 2 ? m.sp_ref[s] - bond0 : ((kraw & kSpringReact) ? 0x2000 : 0);
+    sw[k] = (uint32_t)m.sp_local[s] | ((uint32_t)bl << 16) | ((uint32_t)kind << 30);
+    srest[k] = (float)m.sp_rest[s];
+    sm2k[k] = (float)m.sp_m2k[s];
+  }
+  for (int k = threadIdx.x; k < nbond; k += blockDim.x) {
+    bnew[k] = (float)m.newlen[bond0 + k];
+    bold[k] = (float)m.oldlen[bond0 + k];
+    bdiag[k] = (float)m.diag[bond0 + k];
+  }
+  const int q = threadIdx.x / kCLanes, lane = threadIdx.x % kCLanes;  // kCLanes lanes per slot
+  const int slot = base + q;
+  const bool valid = q < T;
+  const int mv = valid ? m.moves[slot] : -1;
+  const bool moves = mv == 1;
+  const bool primary = mv == 0 || mv == 1;
+  const int me = valid && mv >= 0 ? m.prim[slot] - base : 0;
+  const int nh = primary ? m.nhelp[slot] : 0;
+  const int s0 = valid ? m.sp_start[slot] - sp0 : 0, s1 = valid ? m.sp_start[slot + 1] - sp0 : 0;
+  const bool helpers = m.tile_help[tile] != 0;
+  const int hub_local = m.tile_react[tile];
+  const float fdt = (float)a.dt;
+  // position as float hi + lo (x = hi + lo to ~48 bits), velocity and force float
+  float xh[3] = {0.f, 0.f, 0.f}, xl[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  if (primary) {
+    const double X[3] = {m.x[0][slot], m.y[0][slot], m.z[0][slot]};
+    for (int d = 0; d < 3; ++d) {
+      xh[d] = (float)X[d];
+      xl[d] = (float)(X[d] - (double)xh[d]);
+    }
+    v[0] = (float)m.vx[slot];
+    v[1] = (float)m.vy[slot];
+    v[2] = (float)m.vz[slot];
+    if (lane == 0) buf(0).put(q, xh, xl);
+  }
+  int cur = 0;
+  int eval = 0;  // index of the force evaluation within this MPC step
+  cluster.sync();  // every CTA's first buffer is filled
+
+  auto evaluate = [&]() {
+    const PBuf B = buf(cur);
+    // halo: beads of other CTAs, from their current buffer
+    for (int i = threadIdx.x; i < hn; i += blockDim.x) {
+      const int g = m.halo[h0 + i];
+      const int r = g / T - first_tile, j = g % T;
+      const float* rp = cluster.map_shared_rank(B.p, r);
+      float* dst = B.p + T + i;
+      dst[0] = rp[j];
+      dst[np] = rp[np + j];
+      dst[2 * np] = rp[2 * np + j];
+      dst[3 * np] = rp[3 * np + j];
+      dst[4 * np] = rp[4 * np + j];
+      dst[5 * np] = rp[5 * np + j];
+    }
+    __syncthreads();
+    const bool due = (a.refresh[eval >> 6] >> (eval & 63)) & 1ull;  // refresh (src/cilia.cpp:206-215)
+    ++eval;
+    if (c1 > c0 && due) {
+      int off = 0;
+      for (int c = c0; c < c1; ++c) {
+        const CiliumDev cl = m.cil[c];
+        const int nb = cl.len - cl.num_anker;
+        const int w = (int)threadIdx.x - off;
+        if (w >= 0 && w < nb) {
+          const int i = cl.num_anker - 1 + w;
+          const int k = cl.bond_base - bond0 + i;
+          const int l0 = cl.slot0 - base;
+          const int sd = cl.stride;
+          const float l = cl_cilium_length(cl, i, (float)m.midpnt[c], bold[k], B.dist(l0 + sd * i, l0 + sd * (i + 1)));
+          bnew[k] = l;
+          bold[k] = l;
+          bdiag[k] = sqrtf(0.25f + 0.5f * l);
+        }
+        off += nb;
+      }
+      __syncthreads();
+    }
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    float rx = 0.f, ry = 0.f, rz = 0.f;  // reactions owed to the tile's hub
+    if (mv >= 0) {
+      const float* hx = B.p;
+      const float* hy = hx + np;
+      const float* hz = hy + np;
+      const float* lx = hz + np;
+      const float* ly = lx + np;
+      const float* lz = ly + np;
+      const float mhx = hx[me], mhy = hy[me], mhz = hz[me], mlx = lx[me], mly = ly[me], mlz = lz[me];
+      // two springs per iteration into independent accumulators (more ILP)
+      float bx = 0.f, by = 0.f, bz = 0.f;
+      auto one = [&](int s, float& cx, float& cy, float& cz) {
+        const uint32_t w = sw[s];
+        const int o = (int)(w & 0xffffu);
+        const int kind = (int)(w >> 30);
+        const int bl = (int)((w >> 16) & 0x3fffu);
+        const float b = kind <= 1 ? srest[s] : (kind == 2 ? bnew[bl] : bdiag[bl]);
+        const float dx = (mhx - hx[o]) + (mlx - lx[o]);
+        const float dy = (mhy - hy[o]) + (mly - ly[o]);
+        const float dz = (mhz - hz[o]) + (mlz - lz[o]);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float fac = (kind == 1 && d2 == 0.0f) ? 0.0f : sm2k[s] * (1.0f - b * rsqrtf(d2));
+        cx = fmaf(dx, fac, cx);
+        cy = fmaf(dy, fac, cy);
+        cz = fmaf(dz, fac, cz);
+        if (kind == 0 && (bl & 0x2000)) {
+          rx = fmaf(-dx, fac, rx);
+          ry = fmaf(-dy, fac, ry);
+          rz = fmaf(-dz, fac, rz);
+        }
+      };
+      int s = s0 + lane;
+      for (; s + kCLanes < s1; s += 2 * kCLanes) {
+        one(s, ax, ay, az);
+        one(s + kCLanes, bx, by, bz);
+      }
+      if (s < s1) one(s, ax, ay, az);
+      ax += bx;
+      ay += by;
+      az += bz;
+    }
+    if (kCLanes == 2) {
+      ax += __shfl_xor_sync(0xffffffffu, ax, 1);
+      ay += __shfl_xor_sync(0xffffffffu, ay, 1);
+      az += __shfl_xor_sync(0xffffffffu, az, 1);
+    }
+    fx = ax;
+    fy = ay;
+    fz = az;
+    if (helpers) {  // partial sums of helper slots, in order
+      if (lane == 0 && valid) {
+        part[3 * q] = fx;
+        part[3 * q + 1] = fy;
+        part[3 * q + 2] = fz;
+      }
+      __syncthreads();
+      if (primary && lane == 0)
+        for (int k = 1; k <= nh; ++k) {
+          fx += part[3 * (q + k)];
+          fy += part[3 * (q + k) + 1];
+          fz += part[3 * (q + k) + 2];
+        }
+    }
+    if (hub_local >= 0) {  // the hub's force: negated partner forces, summed over the tile
+      __shared__ float red[3 * 32];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        rx += __shfl_xor_sync(0xffffffffu, rx, o);
+        ry += __shfl_xor_sync(0xffffffffu, ry, o);
+        rz += __shfl_xor_sync(0xffffffffu, rz, o);
+      }
+      const int wid = threadIdx.x >> 5;
+      if ((threadIdx.x & 31) == 0) {
+        red[3 * wid] = rx;
+        red[3 * wid + 1] = ry;
+        red[3 * wid + 2] = rz;
+      }
+      __syncthreads();
+      if (q == hub_local && lane == 0) {
+        const int nw = (int)((blockDim.x + 31) >> 5);
+        for (int w = 0; w < nw; ++w) {
+          fx += red[3 * w];
+          fy += red[3 * w + 1];
+          fz += red[3 * w + 2];
+        }
+      }
+      __syncthreads();
+    }
+  };
+  // v += F kick; x += v dt with x kept as an unevaluated float sum hi + lo
+  auto advance = [&](float kick) {
+    if (moves && lane == 0) {
+      const float f[3] = {fx, fy, fz};
+      for (int d = 0; d < 3; ++d) {
+        v[d] = fmaf(f[d], kick, v[d]);
+        // TwoSum (Knuth) then Fast2Sum; the _rn intrinsics keep every rounding explicit
+        const float dx = __fmul_rn(v[d], fdt);
+        const float sum = __fadd_rn(xh[d], dx);
+        const float bv = __fsub_rn(sum, xh[d]);
+        const float err = __fadd_rn(__fsub_rn(xh[d], __fsub_rn(sum, bv)), __fsub_rn(dx, bv));
+        const float lo = __fadd_rn(xl[d], err);
+        xh[d] = __fadd_rn(sum, lo);
+        xl[d] = __fsub_rn(lo, __fsub_rn(xh[d], sum));
+      }
+    }
+    if (primary && lane == 0) buf(cur ^ 1).put(q, xh, xl);
+    cluster.sync();
+    cur ^= 1;
+  };
+
+  evaluate();
+  advance(0.5f * fdt);  // md_loop_start
+  evaluate();
+  for (int k = 1; k < a.n; ++k) {  // md_loop
+    advance(fdt);
+    evaluate();
+  }
+  const double t = a.t_end;
+  if (moves && lane == 0) {  // md_loop_stop
+    v[0] = fmaf(fx, 0.5f * fdt, v[0]);
+    v[1] = fmaf(fy, 0.5f * fdt, v[1]);
+    v[2] = fmaf(fz, 0.5f * fdt, v[2]);
+  }
+  if (primary && lane == 0) {
+    const double x = (double)xh[0] + (double)xl[0], y = (double)xh[1] + (double)xl[1],
+                 z = (double)xh[2] + (double)xl[2];
+    m.x[0][slot] = x;
+    m.y[0][slot] = y;
+    m.z[0][slot] = z;
+    m.vx[slot] = v[0];
+    m.vy[slot] = v[1];
+    m.vz[slot] = v[2];
+    if (moves) bin(x, y, z, (double)v[0], (double)v[1], (double)v[2]);
+  }
+  for (int k = threadIdx.x; k < nbond; k += blockDim.x) {
+    m.newlen[bond0 + k] = (double)bnew[k];
+    m.oldlen[bond0 + k] = (double)bold[k];
+    m.diag[bond0 + k] = (double)bdiag[k];
+  }
+  // switch_logic (src/cilia.cpp:241-258, src/ConstantBeatCilia.cpp:8-23)
+  for (int c = c0 + (int)threadIdx.x; c < c1; c += (int)blockDim.x) {
+    const CiliumDev cl = m.cil[c];
+    double mp = m.midpnt[c], ts = m.tstroke[c];
+    if (cl.kind == 1) {
+      if (t - ts >= cl.power_dur && mp == cl.start) mp += 1;
+      if (t - ts - cl.power_dur >= cl.recovery_dur && mp > cl.start) {
+        ts = t;
+        mp = cl.start;
+      }
+    } else {
+      if (mp == cl.start && t - ts > 100.0) mp += 1;
+      const int l0 = cl.slot0 - base;
+      double lb = 0.0;
+      const PBuf B = buf(cur);
+      const int sd = cl.stride;
+      for (int i = 0; i < cl.len - 1; ++i)
+        lb += 2.0f * B.dist(l0 + sd * i, l0 + sd * (i + 1)) -
+              B.dist(l0 + sd * (cl.len + i), l0 + sd * (cl.len + i + 1)) -
+              B.dist(l0 + sd * (2 * cl.len + i), l0 + sd * (2 * cl.len + i + 1));
+      if (lb > (float)cl.max_bend && mp > cl.start) {
+        ts = t;
+        mp = cl.start;
+      }
+    }
+    if (mp > cl.start) mp += a.tstep / cl.m_speed;
+    m.midpnt[c] = mp;
+    m.tstroke[c] = ts;
+  }
+  cluster.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+struct ClBinF64 {
+  CellsF64 c;
+  Box box;
+  double an[3];
+  double mb;
+  unsigned* err;
+  __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
+    const long cid = unwrapped_cell(box, an, x, y, z);
+    if (cid < 0) {
+      atomicOr(err, kErrCellRange);
+      return;
+    }
+    double* sp = reinterpret_cast<double*>(c.sum + cid);
+    atomicAdd(sp + 0, vx * mb);
+    atomicAdd(sp + 1, vy * mb);
+    atomicAdd(sp + 2, vz * mb);
+    atomicAdd(sp + 3, mb * (vx * vx + vy * vy + vz * vz));
+    atomicAdd(c.cnt + cid, 1u << 16);
+  }
+};
+
+struct ClBinF32 {
+  CellsF32 c;
+  Box box;
+  double an[3];
+  float mb;
+  unsigned* err;
+  __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
+    const long cid = unwrapped_cell(box, an, x, y, z);
+    if (cid < 0) {
+      atomicOr(err, kErrCellRange);
+      return;
+    }
+    const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+    float* sp = reinterpret_cast<float*>(c.sum + cid);
+    atomicAdd(sp + 0, fvx * mb);
+    atomicAdd(sp + 1, fvy * mb);
+    atomicAdd(sp + 2, fvz * mb);
+    atomicAdd(sp + 3, mb * (fvx * fvx + fvy * fvy + fvz * fvz));
+    atomicAdd(c.cnt + cid, 1u << 16);
+  }
+};
+
+template <int L, typename Bin>
+cudaError_t launch_cluster_l(const MDState& m, const MDStepArgs& a, const Bin& bin, cudaStream_t s) {
+  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max};
+  const size_t smem = lay.bytes(m.tile);
+  auto kern = k_md_cluster<L, Bin>;
+  cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(m.ntiles);
+  cfg.blockDim = dim3(L * m.tile);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = m.ntiles;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, m, a, bin, lay);
+}
+
+template <typename Bin>
+cudaError_t launch_cluster(const MDState& m, const MDStepArgs& a, const Bin& bin, cudaStream_t s) {
+  return m.cl_lanes == 2 ? launch_cluster_l<2>(m, a, bin, s) : launch_cluster_l<1>(m, a, bin, s);
+}
+
+}  // namespace
+
+size_t md_cluster_smem(const MDState& m) {
+  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max};
+  return lay.bytes(m.tile);
+}
+
+// 1 when a cluster of m.ntiles CTAs with this layout can be scheduled
+template <int L>
+int cluster_feasible_l(const MDState& m) {
+  if (m.ntiles < 1 || m.ntiles > 16 || L * m.tile > 1024) return 0;
+  const size_t smem = md_cluster_smem(m);
+  if (smem > 227 * 1024) return 0;
+  auto kern = k_md_cluster<L, ClBinF32>;
+  cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(m.ntiles);
+  cfg.blockDim = dim3(L * m.tile);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = m.ntiles;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return nclusters >= 1;
+}
+
+int md_cluster_feasible(const MDState& m) {
+  return m.cl_lanes == 2 ? cluster_feasible_l<2>(m) : cluster_feasible_l<1>(m);
+}
+
+int launch_md_cluster_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s,
+                               cudaError_t* st) {
+  if (m.nslots == 0) return 0;
+  ClBinF64 bin{c, a.box, {a.a_next[0], a.a_next[1], a.a_next[2]}, a.bead_mass, a.err};
+  *st = launch_cluster(m, a, bin, s);
+  return 1;
+}
+
+int launch_md_cluster_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s,
+                               cudaError_t* st) {
+  if (m.nslots == 0) return 0;
+  ClBinF32 bin{c, a.box, {a.a_next[0], a.a_next[1], a.a_next[2]}, (float)a.bead_mass, a.err};
+  *st = launch_cluster(m, a, bin, s);
+  return 1;
+}
+
+}  // namespace mpcd

@@ -31,9 +31,9 @@ __device__ double cilium_length(const CiliumDev& cl, int i, double midpnt, doubl
   const double bondlength = 0.5;
   double l;
   if (i < midpnt - 2.0) {
-    l = bondlength + cl.beatstrength *
-                         pow(1.0 - (i - cl.num_anker - 1.0) / (cl.len - cl.num_anker - 1.0), 2.5) * 0.5 *
-                         (1.0 - 1.0 / (midpnt - i - 1.0));
+    // base^2.5 as base^2 sqrt(base) (base > 0 for every refreshed bond)
+    const double base = 1.0 - (i - cl.num_anker - 1.0) / (cl.len - cl.num_anker - 1.0);
+    l = bondlength + cl.beatstrength * (base * base * sqrt(base)) * 0.5 * (1.0 - 1.0 / (midpnt - i - 1.0));
   } else {
     const double di = i - midpnt;
     l = bondlength - 2.0 * cl.beatstrength / (di * di + 1.0);
@@ -49,8 +49,9 @@ __device__ double cilium_length(const CiliumDev& cl, int i, double midpnt, doubl
   return l;
 }
 
-// refresh every 0.01 time units (src/cilia.cpp:206-215)
-__device__ __forceinline__ bool refresh_due(double t, double dt) { return fmod(t + dt / 10., 0.01) < dt; }
+// refresh every 0.01 time units (src/cilia.cpp:206-215); the schedule of the
+// step's force evaluations is computed on the host
+__device__ __forceinline__ bool refresh_due(const MDStepArgs& a, int e) { return (a.refresh[e >> 6] >> (e & 63)) & 1ull; }
 
 // Positions of one tile (own slots, then halo) in shared memory.
 template <bool kSplit>
@@ -165,10 +166,11 @@ __device__ __forceinline__ void springs_split(const MDState& m, const Stage<true
 template <bool kSplit>
 __device__ double cilium_localbend(const CiliumDev& cl, int l0, const Stage<kSplit>& st) {
   double l = 0.0;
+  const int sd = cl.stride;
   for (int i = 0; i < cl.len - 1; ++i) {
-    l += 2.0 * st.dist(l0 + i, l0 + i + 1);
-    l -= st.dist(l0 + cl.len + i, l0 + cl.len + i + 1);
-    l -= st.dist(l0 + 2 * cl.len + i, l0 + 2 * cl.len + i + 1);
+    l += 2.0 * st.dist(l0 + sd * i, l0 + sd * (i + 1));
+    l -= st.dist(l0 + sd * (cl.len + i), l0 + sd * (cl.len + i + 1));
+    l -= st.dist(l0 + sd * (2 * cl.len + i), l0 + sd * (2 * cl.len + i + 1));
   }
   return l;
 }
@@ -206,8 +208,10 @@ __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     vz = m.vz[slot];
   }
   const unsigned nblocks = gridDim.x;
+  unsigned barriers = 0;  // barriers passed in this launch
   double t = a.t0;
   int cur = 0;
+  int eval = 0;  // index of the force evaluation within this MPC step
 
   auto stage = [&](int b) {
     if (primary && lane == 0) st.put(q, x, y, z);
@@ -218,7 +222,8 @@ __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     __syncthreads();
   };
   auto evaluate = [&]() {
-    if (c1 > c0 && refresh_due(t, dt)) {
+    const bool due = refresh_due(a, eval++);
+    if (c1 > c0 && due) {
       // flatten (cilium, bond) pairs of this tile over the CTA's threads
       int off = 0;
       for (int c = c0; c < c1; ++c) {
@@ -229,7 +234,8 @@ __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
           const int i = cl.num_anker - 1 + w;
           const int k = cl.bond_base + i;
           const int l0 = cl.slot0 - base;
-          const double l = cilium_length(cl, i, m.midpnt[c], m.oldlen[k], st.dist(l0 + i, l0 + i + 1));
+          const double l =
+              cilium_length(cl, i, m.midpnt[c], m.oldlen[k], st.dist(l0 + cl.stride * i, l0 + cl.stride * (i + 1)));
           m.newlen[k] = l;
           m.oldlen[k] = l;
           m.diag[k] = sqrt(0.5 * 0.5 + 0.5 * l);
@@ -288,7 +294,7 @@ __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     z = fma(vz, dt, z);
   }
   publish(cur ^ 1);
-  if (!grid_sync(m.bar, nblocks, a.err)) return;
+  if (!grid_sync(m.bar, ++barriers * nblocks, a.err)) return;
   cur ^= 1;
   stage(cur);
   evaluate();
@@ -304,7 +310,7 @@ __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
       z = fma(vz, dt, z);
     }
     publish(cur ^ 1);
-    if (!grid_sync(m.bar, nblocks, a.err)) return;
+    if (!grid_sync(m.bar, ++barriers * nblocks, a.err)) return;
     cur ^= 1;
     stage(cur);
     evaluate();
@@ -348,21 +354,15 @@ __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   }
 }
 
-__device__ __forceinline__ int cell_axis(double x, double a, int L) {
-  double xa = x + a;
-  int c = (int)(floor(xa) - floor(xa / L) * L);
-  if (c < 0) c += L;
-  if (c >= L) c -= L;
-  return c;
-}
-
 struct BinF64 {
   CellsF64 c;
   const MDStepArgs* a;
   __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
-    const long cid = cell_axis(x, a->a_next[0], a->box.L[0]) +
-                     (long)a->box.L[0] * (cell_axis(y, a->a_next[1], a->box.L[1]) +
-                                          (long)a->box.L[1] * cell_axis(z, a->a_next[2], a->box.L[2]));
+    const long cid = unwrapped_cell(a->box, a->a_next, x, y, z);
+    if (cid < 0) {
+      atomicOr(a->err, kErrCellRange);
+      return;
+    }
     const double mb = a->bead_mass;
     double* sp = reinterpret_cast<double*>(c.sum + cid);
     atomicAdd(sp + 0, vx * mb);
@@ -377,9 +377,11 @@ struct BinF32 {
   CellsF32 c;
   const MDStepArgs* a;
   __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
-    const long cid = cell_axis(x, a->a_next[0], a->box.L[0]) +
-                     (long)a->box.L[0] * (cell_axis(y, a->a_next[1], a->box.L[1]) +
-                                          (long)a->box.L[1] * cell_axis(z, a->a_next[2], a->box.L[2]));
+    const long cid = unwrapped_cell(a->box, a->a_next, x, y, z);
+    if (cid < 0) {
+      atomicOr(a->err, kErrCellRange);
+      return;
+    }
     const float mb = (float)a->bead_mass;
     const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
     float* sp = reinterpret_cast<float*>(c.sum + cid);

@@ -16,7 +16,7 @@ enum : unsigned {
   kErrGammaMissing = 1u,   // injected Gamma < 0 for a cell that needs one
   kErrGammaLoop = 2u,      // Marsaglia-Tsang loop exceeded its iteration cap
   kErrBarrier = 4u,        // grid barrier wait exceeded its iteration cap
-  kErrCellRange = 8u,      // a particle's cell index was out of range
+  kErrCellRange = 8u,      // a non-finite or out-of-range coordinate (e.g. an unstable MD step)
   kErrCellOverflow = 16u,  // more than 65535 particles of one kind in a cell
 };
 
@@ -92,20 +92,6 @@ __device__ __forceinline__ float gamma_mt(int nc, uint64_t seed, uint64_t step, 
   return d;
 }
 
-// Uniform random axis from two uniforms (src/libcilia/mpcd.cpp:277-283), in double.
-__device__ __forceinline__ void random_axis(uint64_t seed, uint64_t step, uint32_t cell, double& rx, double& ry,
-                                            double& rz) {
-  u32x4 r = draw4(seed, step, kStreamCell, cell, 0u);
-  double phi = 2.0 * kPi * u01_dbl(r.x);
-  double ct = 2.0 * u01_dbl(r.y) - 1.0;
-  double st = sqrt(fmax(0.0, 1.0 - ct * ct));
-  double sp, cp;
-  sincos(phi, &sp, &cp);
-  rx = st * cp;
-  ry = st * sp;
-  rz = ct;
-}
-
 // ---------------------------------------------------------------- cells ---
 // A particle's cell is packed as ix | iy << 10 | iz << 20 (edges up to 1024).
 MPCD_HD uint32_t pack_cell(int ix, int iy, int iz) { return (uint32_t)ix | ((uint32_t)iy << 10) | ((uint32_t)iz << 20); }
@@ -118,17 +104,43 @@ struct Box {
   MPCD_HD int lin(int ix, int iy, int iz) const { return ix + L[0] * (iy + L[1] * iz); }
 };
 
+// Cell along one axis of an unwrapped coordinate, floor(x + a) - floor((x + a)/L) L
+// (src/libcilia/mpcd.cpp:130-138).  Returns -1 for a non-finite or absurdly
+// large coordinate, so that callers report an error instead of indexing with it.
+MPCD_HD int unwrapped_cell_axis(double x, double a, int L) {
+  const double xa = x + a;
+  if (!(xa > -1.0e15 && xa < 1.0e15)) return -1;
+  double c = floor(xa) - floor(xa / L) * L;
+  if (c < 0) c += L;  // rounding edge where (x + a)/L rounds to an integer
+  if (c >= L) c -= L;
+  if (!(c >= 0.0 && c < (double)L)) return -1;
+  return (int)c;
+}
+
+// linear cell of an unwrapped position, -1 if invalid
+MPCD_HD long unwrapped_cell(const Box& b, const double* a, double x, double y, double z) {
+  const int cx = unwrapped_cell_axis(x, a[0], b.L[0]);
+  const int cy = unwrapped_cell_axis(y, a[1], b.L[1]);
+  const int cz = unwrapped_cell_axis(z, a[2], b.L[2]);
+  if (cx < 0 || cy < 0 || cz < 0) return -1;
+  return cx + (long)b.L[0] * (cy + (long)b.L[1] * cz);
+}
+
 // Count word of a cell: fluid particles in the low 16 bits, beads in the high.
 MPCD_HD int cnt_fluid(uint32_t w) { return (int)(w & 0xffffu); }
 MPCD_HD int cnt_beads(uint32_t w) { return (int)(w >> 16); }
 
 // ----------------------------------------------------------- barriers ---
-// Grid-wide barrier for cooperative launches: one arrival counter and a
-// generation word.  Every wait is bounded; on timeout it sets kErrBarrier in
-// *err and returns false, and the caller leaves the kernel.
+// Grid-wide barrier for cooperative launches: a monotonic arrival counter,
+// reset to zero by the host before every launch.  The k-th barrier of a
+// launch (k = 1, 2, ...) waits until the counter reaches k * nblocks.  Each
+// CTA publishes its writes with a gpu-scope fence and one relaxed atomic add,
+// then polls with acquire loads.  Every wait is bounded: on timeout the CTA
+// sets kErrBarrier in *err and returns false, and the caller leaves the kernel
+// (the other CTAs then time out as well, so the launch always ends).
 struct GridBarrier {
   unsigned* count;
-  unsigned* gen;
+  unsigned* gen;  // unused word next to the counter (both cleared per launch)
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -136,34 +148,23 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
-__device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks, unsigned* err) {
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned target, unsigned* err) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = 1;
-    unsigned g = ld_acquire(b.gen);
     __threadfence();
-    unsigned arrived = atomicAdd(b.count, 1u);
-    if (arrived == nblocks - 1) {
-      atomicExch(b.count, 0u);
-      __threadfence();
-      st_release(b.gen, g + 1);
-    } else {
-      unsigned long long spins = 0;
-      while (ld_acquire(b.gen) == g) {
-        if (++spins > (1ull << 24)) {  // ~ seconds at the polling interval below
-          atomicOr(err, kErrBarrier);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
+    atomicAdd(b.count, 1u);
+    unsigned long long spins = 0;
+    while (ld_acquire(b.count) < target) {
+      if (++spins > (1ull << 22)) {  // bounded wait (a few seconds)
+        atomicOr(err, kErrBarrier);
+        ok = 0;
+        break;
       }
+      __nanosleep(20);
     }
-    if (ok && (ld_acquire(err) & kErrBarrier)) ok = 0;
   }
   __syncthreads();
   return ok != 0;

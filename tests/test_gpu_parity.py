@@ -166,3 +166,29 @@ def test_invalid_arguments_rejected():
         e.shift = [1.5, 0.0, 0.0]
     with pytest.raises(cg.MpcdError):
         cg.Sim("name = \"x\"; md_objects = ( );")  # missing root keys
+
+
+def test_non_finite_input_rejected():
+    e = cg.Engine((4, 4, 4))
+    pos = np.zeros((2, 3))
+    vel = np.zeros((2, 3))
+    pos[1, 0] = np.nan
+    with pytest.raises(cg.MpcdError, match="non-finite"):
+        e.set_fluid(pos, vel)
+
+
+def test_unstable_md_step_reports_error_without_fault():
+    """A too-large MD step lets the beads diverge; the kernels report it."""
+    import simcfg
+
+    cfg = simcfg.plain_fluid(12, name="unstable")
+    cfg["ststep"] = 0.02
+    cfg["md_objects"] = (simcfg.fibonacci_clami(6, radius=3.5, center=(6, 6, 6), rodlength=6,
+                                                springconstant=20000.0, seed=1),)
+    for prec in (cg.MPCD_FP64, cg.MPCD_FP32):
+        s = cg.Sim(simcfg.dumps(cfg), precision=prec, seed=2)
+        with pytest.raises(cg.MpcdError, match="non-finite"):
+            for _ in range(40):
+                s.next_tstep()
+            s.engine.sync()
+        s.close()
