@@ -186,6 +186,40 @@ int mpcd_timed_run(mpcd_engine* h, int nsteps, int flush_l2, double* step_ms);
 int mpcd_set_profiling(mpcd_engine* h, int on);
 int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* launches);
 
+/* ----------------------------------------------------------------------------
+ * mpcd_fluid_step_noalloc -- one split-precision MPC step of a plain fluid
+ * (collision, streaming, binning; no beads, no walls) that allocates no device
+ * memory.  It has no counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc themselves -- code that runs inside another runtime's
+ * memory pool or allocator, or a plug-in that is only handed device pointers
+ * and a stream.
+ *
+ * The caller passes the particles in device-accessible memory, in the engine's
+ * split layout, and gets them back in place:
+ *   pos[i] = float4(ox, oy, oz, c) with in-cell offsets in [0,1) and c the
+ *            bits of the uint32 cell index ix | iy << 10 | iz << 20
+ *   vel[i] = float4(vx, vy, vz, 0)
+ * On entry the particles are binned with the grid shift a_cur; the step
+ * collides them (thermostat and rotation axis from the counter-based generator
+ * at (seed, step), as mpcd_step draws them), streams them by tstep and leaves
+ * them for a next call with a_cur = a_next.  diss (host, may be NULL) receives
+ * the kinetic energy removed by the thermostat.  stream: a cudaStream_t (NULL
+ * for the default stream); the call returns after the stream has finished.
+ *
+ * Its per-cell scratch is a file-scope static device array for at most
+ * MPCD_NOALLOC_MAX_CELLS cells (about 4.5 MB), held by every GPU that loads the
+ * library until the process exits.  Larger boxes are rejected with
+ * MPCD_EINVAL.  The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race, and the array keeps the last call's contents.
+ * Returns MPCD_OK, MPCD_EINVAL, MPCD_ECUDA, or MPCD_EDEVICE (a device-side check failed).
+ * -------------------------------------------------------------------------- */
+#define MPCD_NOALLOC_MAX_CELLS 65536
+int mpcd_fluid_step_noalloc(const int* sizes, long n, void* pos, void* vel, double tstep, const double* a_cur,
+                            const double* a_next, unsigned long long seed, unsigned long long step, double* diss,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,8 @@ def lib():
             "mpcd_timed_run": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, _DP]),
             "mpcd_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
             "mpcd_kernel_time": (ctypes.c_int, [P, ctypes.c_int, _DP, ctypes.POINTER(ctypes.c_longlong)]),
+            "mpcd_fluid_step_noalloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.c_long, P, P, _D, _DP, _DP,
+                                                       ctypes.c_ulonglong, ctypes.c_ulonglong, _DP, P]),
             "cilia_sim_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
                                                 ctypes.POINTER(P)]),
             "cilia_sim_destroy": (ctypes.c_int, [P]),

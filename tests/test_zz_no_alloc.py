@@ -1,0 +1,116 @@
+"""mpcd_fluid_step_noalloc: the fluid step for callers that cannot allocate
+device memory (code living inside another runtime's memory pool, or a plug-in
+handed only pointers and a stream).  This test acts as such a caller: the
+particle buffers come from torch's allocator and the call runs on torch's
+stream.  Two calls in a row are checked against the engine's regular
+split-precision step (mpcd_set_fluid + mpcd_step) on the same particles,
+shifts and generator counters.
+
+Both paths run the same kernels; they differ only in the order of the float
+atomic additions into the cell sums, so the results agree to float rounding:
+at least 99.9 % of the particles within 1e-4 in position and velocity, and
+the dissipated energy within 1e-4 relative (the tolerances of the split
+precision tests).  Runs alone in a fresh process as well as after the rest of
+the suite (the static scratch keeps nothing a call depends on).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cilia_gpu as cg
+
+pytestmark = pytest.mark.gpu
+
+
+def pack_split(pos, vel, L):
+    """Host arrays -> the split layout, rounding as mpcd_set_fluid does."""
+    n = pos.shape[0]
+    P = np.zeros((n, 4), dtype=np.float32)
+    cells = np.zeros((n, 3), dtype=np.int64)
+    for q in range(3):
+        x = pos[:, q]
+        xw = x - np.floor(x / L[q]) * L[q]
+        xw = np.where(xw >= L[q], xw - L[q], xw)
+        xw = np.where(xw < 0, xw + L[q], xw)
+        fi = np.floor(xw)
+        i = fi.astype(np.int64)
+        o = xw - fi
+        i = np.where(i >= L[q], i - L[q], i)
+        wrap = o >= 1.0
+        o = np.where(wrap, 0.0, o)
+        i = np.where(wrap, (i + 1) % L[q], i)
+        f = o.astype(np.float32)
+        up = f >= np.float32(1.0)
+        f = np.where(up, np.float32(0.0), f)
+        i = np.where(up, (i + 1) % L[q], i)
+        P[:, q] = f
+        cells[:, q] = i
+    packed = (cells[:, 0] | (cells[:, 1] << 10) | (cells[:, 2] << 20)).astype(np.uint32)
+    P[:, 3] = packed.view(np.float32)
+    V = np.zeros((n, 4), dtype=np.float32)
+    V[:, :3] = vel.astype(np.float32)
+    return P, V
+
+
+def unpack_split(P, V):
+    c = P[:, 3].view(np.uint32).astype(np.int64)
+    cells = np.stack([c & 1023, (c >> 10) & 1023, (c >> 20) & 1023], axis=1)
+    return cells + P[:, :3].astype(np.float64), V[:, :3].astype(np.float64)
+
+
+def periodic_diff(a, b, L):
+    d = a - b
+    L = np.asarray(L, dtype=float)
+    return d - np.round(d / L) * L
+
+
+def test_noalloc_step_matches_engine_on_two_calls():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    L = (16, 16, 16)
+    n = L[0] * L[1] * L[2] * 10
+    rng = np.random.default_rng(11)
+    pos = rng.uniform(0, 16, (n, 3))
+    vel = rng.normal(size=(n, 3))
+    vel -= vel.mean(axis=0)
+    seed = 1234
+    e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=cg.MPCD_FP32, seed=seed)
+    e.set_fluid(pos, vel)
+    a_cur = np.ascontiguousarray(e.shift)
+    P, V = pack_split(pos, vel, L)
+    dP = torch.from_numpy(P).cuda()
+    dV = torch.from_numpy(V).cuda()
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    sizes = (ctypes.c_int * 3)(*L)
+    lib = cg.lib()
+    diss_prev = 0.0
+    for step in (1, 2):
+        e.step()
+        a_next = np.ascontiguousarray(e.shift)
+        diss = ctypes.c_double(0.0)
+        rc = lib.mpcd_fluid_step_noalloc(sizes, n, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(dV.data_ptr()),
+                                         0.1, a_cur.ctypes.data_as(cg._DP), a_next.ctypes.data_as(cg._DP),
+                                         seed, step, ctypes.byref(diss), ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, rc  # MPCD_OK
+        pe, ve = e.fluid()
+        ps, vs = unpack_split(dP.cpu().numpy(), dV.cpu().numpy())
+        dp = np.abs(periodic_diff(ps, pe, L)).max(axis=1)
+        dv = np.abs(vs - ve).max(axis=1)
+        assert np.mean(dp < 1e-4) > 0.999, (step, np.sort(dp)[-5:])
+        assert np.mean(dv < 1e-4) > 0.999, (step, np.sort(dv)[-5:])
+        d_engine = e.observables()["diss_energy"] - diss_prev
+        diss_prev += d_engine
+        assert abs(diss.value - d_engine) <= 1e-4 * max(1.0, abs(d_engine)), (step, diss.value, d_engine)
+        a_cur = a_next
+
+
+def test_noalloc_rejects_boxes_beyond_the_static_scratch():
+    lib = cg.lib()
+    sizes = (ctypes.c_int * 3)(64, 64, 64)  # 262144 cells > the 65536-cell scratch
+    a = np.full(3, 0.5)
+    rc = lib.mpcd_fluid_step_noalloc(sizes, 0, None, None, 0.1, a.ctypes.data_as(cg._DP), a.ctypes.data_as(cg._DP),
+                                     1, 1, None, None)
+    assert rc == 1  # MPCD_EINVAL
