@@ -42,6 +42,10 @@ for _p in (PKG, os.path.join(REPO, "oracle")):
 import simcfg  # noqa: E402
 
 METRIC = "MPCD particle-steps/s"
+# DRAM bytes (read + write) per fluid particle of one fluid_step launch, from
+# one ncu capture on swimmer64 (profiles/fluid_step_swimmer64.md); the traffic
+# grows in proportion to the particles, so it is scaled to the workload.
+TRAFFIC_B_PER_PARTICLE = {"fp64": 99.6, "fp32": 50.3}
 UNIT = "particle-steps/s"
 
 
@@ -69,7 +73,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -291,7 +295,10 @@ def main():
                    "l2": "flushed between timed steps (256 MB write, outside the timed events)",
                    "parallelism": f"replicas{args.gpus}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved / hbm,
+                     "traffic": TRAFFIC_B_PER_PARTICLE[args.precision] * g["nf"],
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, swimmer64 capture, "
+                                       "scaled by particles", "peak_kind": peak_kind,
                      "kernel": "fluid_step (collide + stream + bin)",
                      "bytes_per_particle_step": bpp, "avg_launch_ms": avg_fluid_ms},
         "kernels_ms_per_step": {k: v[0] / max(g["prof_steps"], 1) for k, v in g["kernels"].items()},
