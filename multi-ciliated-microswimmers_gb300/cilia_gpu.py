@@ -1,7 +1,9 @@
-"""ctypes binding of libmpcd_gpu.so (include/mpcd_gpu.h, include/cilia_host.h).
+"""ctypes binding of libmpcd_gpu.so (include/mpcd_gpu.h, include/cilia_host.h,
+include/mpcd_batch.h).
 
 `Engine` wraps one mpcd_engine (a box of MPCD fluid plus MD beads on the GPU);
-`Sim` wraps one cilia_sim (the reference's Simulation built from a sim.cfg).
+`Sim` wraps one cilia_sim (the reference's Simulation built from a sim.cfg);
+`Batch` wraps one mpcd_batch (many independent boxes advanced together).
 There is no CPU fallback: if the library or a GPU is missing, construction
 raises.
 """
@@ -55,6 +57,19 @@ class CiliaOptions(ctypes.Structure):
                 ("walls", ctypes.c_int), ("gravity", _D), ("bead_mass", _D), ("sort_interval", ctypes.c_int)]
 
 
+class MpcdBatchParams(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("max_replicas", ctypes.c_int), ("max_particles", ctypes.c_long),
+                ("max_cells", ctypes.c_long), ("max_slots", ctypes.c_long), ("max_springs", ctypes.c_long),
+                ("max_halo", ctypes.c_long), ("max_cilia", ctypes.c_int), ("max_bonds", ctypes.c_long),
+                ("md_lanes", ctypes.c_int), ("md_tile", ctypes.c_int), ("sort_interval", ctypes.c_int),
+                ("sorts_per_graph", ctypes.c_int)]
+
+
+class MpcdBatchTuning(ctypes.Structure):
+    _fields_ = [("fluid_threads", ctypes.c_int), ("fluid_blocks", ctypes.c_int), ("cell_threads", ctypes.c_int),
+                ("cell_blocks", ctypes.c_int), ("sort_interval", ctypes.c_int)]
+
+
 class MpcdError(RuntimeError):
     pass
 
@@ -99,6 +114,37 @@ def lib():
             "mpcd_kernel_time": (ctypes.c_int, [P, ctypes.c_int, _DP, ctypes.POINTER(ctypes.c_longlong)]),
             "mpcd_fluid_step_noalloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.c_long, P, P, _D, _DP, _DP,
                                                        ctypes.c_ulonglong, ctypes.c_ulonglong, _DP, P]),
+            "mpcd_batch_create": (ctypes.c_int, [ctypes.POINTER(MpcdBatchParams), ctypes.POINTER(P)]),
+            "mpcd_batch_destroy": (ctypes.c_int, [P]),
+            "mpcd_batch_last_error": (ctypes.c_char_p, [P]),
+            "mpcd_batch_add": (ctypes.c_int, [P, ctypes.POINTER(MpcdParams), _IP]),
+            "mpcd_batch_add_engine": (ctypes.c_int, [P, P, _IP]),
+            "mpcd_batch_set_fluid": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_long, _DP, _DP]),
+            "mpcd_batch_set_shift": (ctypes.c_int, [P, ctypes.c_int, _DP]),
+            "mpcd_batch_set_time": (ctypes.c_int, [P, ctypes.c_int, _D]),
+            "mpcd_batch_set_beads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_long, _DP, _DP, _IP]),
+            "mpcd_batch_set_springs": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_long, _IP, _IP, _IP, _IP, _DP, _DP]),
+            "mpcd_batch_set_cilia": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(MpcdCilium), _DP,
+                                                    _DP]),
+            "mpcd_batch_footprint": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
+            "mpcd_batch_admit": (ctypes.c_int, [P, ctypes.c_int]),
+            "mpcd_batch_set_steps": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_longlong]),
+            "mpcd_batch_run": (ctypes.c_int, [P, ctypes.c_int]),
+            "mpcd_batch_timed_run": (ctypes.c_int, [P, ctypes.c_int, _DP]),
+            "mpcd_batch_sync": (ctypes.c_int, [P]),
+            "mpcd_batch_status": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
+                                                 ctypes.POINTER(ctypes.c_longlong), _DP,
+                                                 ctypes.POINTER(ctypes.c_uint)]),
+            "mpcd_batch_get_fluid": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_long, _DP, _DP]),
+            "mpcd_batch_get_beads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_long, _DP, _DP]),
+            "mpcd_batch_get_shift": (ctypes.c_int, [P, ctypes.c_int, _DP]),
+            "mpcd_batch_observables": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdObs)]),
+            "mpcd_batch_remove": (ctypes.c_int, [P, ctypes.c_int]),
+            "mpcd_batch_resident": (ctypes.c_int, [P]),
+            "mpcd_batch_autotune": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdBatchTuning)]),
+            "mpcd_batch_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(MpcdBatchTuning)]),
+            "mpcd_batch_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(MpcdBatchTuning)]),
+            "mpcd_batch_launch_count": (ctypes.c_longlong, [P]),
             "cilia_sim_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
                                                 ctypes.POINTER(P)]),
             "cilia_sim_destroy": (ctypes.c_int, [P]),
@@ -326,3 +372,138 @@ class Sim:
 
     def write_cfg(self, path):
         self._ck(lib().cilia_sim_write_cfg(self._h, path.encode()), "write_cfg")
+
+
+class Batch:
+    """Many independent split-precision boxes advanced together (mpcd_batch)."""
+
+    def __init__(self, *, max_replicas, max_particles, max_cells, max_slots=0, max_springs=0, max_halo=0,
+                 max_cilia=0, max_bonds=0, md_lanes=0, md_tile=0, sort_interval=0, sorts_per_graph=0, device=0):
+        p = MpcdBatchParams(device, max_replicas, max_particles, max_cells, max_slots, max_springs, max_halo,
+                            max_cilia, max_bonds, md_lanes, md_tile, sort_interval, sorts_per_graph)
+        h = ctypes.c_void_p()
+        rc = lib().mpcd_batch_create(ctypes.byref(p), ctypes.byref(h))
+        if rc:
+            raise MpcdError(f"mpcd_batch_create failed with code {rc}")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mpcd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _ck(self, rc, what):
+        if rc:
+            msg = lib().mpcd_batch_last_error(self._h)
+            raise MpcdError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def add(self, L, *, tstep=0.1, ststep=0.002, bead_mass=5.0, seed=1, gravity=0.0, omega=0.0):
+        if isinstance(L, int):
+            L = (L, L, L)
+        p = MpcdParams()
+        p.sizes[:] = [int(x) for x in L]
+        p.tstep, p.ststep, p.precision, p.walls = tstep, ststep, MPCD_FP32, WALLS_NONE
+        p.gravity, p.omega, p.bead_mass, p.seed = gravity, omega, bead_mass, seed
+        r = ctypes.c_int()
+        self._ck(lib().mpcd_batch_add(self._h, ctypes.byref(p), ctypes.byref(r)), "batch_add")
+        return r.value
+
+    def add_engine(self, engine):
+        r = ctypes.c_int()
+        self._ck(lib().mpcd_batch_add_engine(self._h, engine.handle, ctypes.byref(r)), "batch_add_engine")
+        return r.value
+
+    def set_fluid(self, r, pos, vel):
+        pos, vel = _f64(pos), _f64(vel)
+        self._ck(lib().mpcd_batch_set_fluid(self._h, r, pos.shape[0], _dp(pos), _dp(vel)), "batch_set_fluid")
+
+    def set_shift(self, r, a):
+        a = _f64(a)
+        self._ck(lib().mpcd_batch_set_shift(self._h, r, _dp(a)), "batch_set_shift")
+
+    def shift(self, r):
+        a = np.zeros(3)
+        self._ck(lib().mpcd_batch_get_shift(self._h, r, _dp(a)), "batch_get_shift")
+        return a
+
+    def footprint(self, r):
+        v = ctypes.c_longlong()
+        self._ck(lib().mpcd_batch_footprint(self._h, r, ctypes.byref(v)), "batch_footprint")
+        return v.value
+
+    def admit(self, r):
+        self._ck(lib().mpcd_batch_admit(self._h, r), "batch_admit")
+
+    def try_admit(self, r):
+        return lib().mpcd_batch_admit(self._h, r) == 0
+
+    def set_steps(self, r, n):
+        self._ck(lib().mpcd_batch_set_steps(self._h, r, int(n)), "batch_set_steps")
+
+    def run(self, nsteps):
+        self._ck(lib().mpcd_batch_run(self._h, int(nsteps)), "batch_run")
+
+    def timed_run(self, nsteps):
+        ms = ctypes.c_double()
+        self._ck(lib().mpcd_batch_timed_run(self._h, int(nsteps), ctypes.byref(ms)), "batch_timed_run")
+        return ms.value
+
+    def sync(self):
+        self._ck(lib().mpcd_batch_sync(self._h), "batch_sync")
+
+    def status(self, r):
+        d, left, err = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_uint()
+        t = ctypes.c_double()
+        self._ck(lib().mpcd_batch_status(self._h, r, ctypes.byref(d), ctypes.byref(left), ctypes.byref(t),
+                                         ctypes.byref(err)), "batch_status")
+        return dict(steps=d.value, steps_left=left.value, globalt=t.value, err=err.value)
+
+    def fluid(self, r, n):
+        pos = np.zeros((n, 3))
+        vel = np.zeros((n, 3))
+        self._ck(lib().mpcd_batch_get_fluid(self._h, r, n, _dp(pos), _dp(vel)), "batch_get_fluid")
+        return pos, vel
+
+    def beads(self, r, n):
+        pos = np.zeros((n, 3))
+        vel = np.zeros((n, 3))
+        self._ck(lib().mpcd_batch_get_beads(self._h, r, n, _dp(pos), _dp(vel)), "batch_get_beads")
+        return pos, vel
+
+    def observables(self, r):
+        o = MpcdObs()
+        self._ck(lib().mpcd_batch_observables(self._h, r, ctypes.byref(o)), "batch_observables")
+        return dict(momentum=np.array(o.momentum[:]), n=o.n, mass=o.mass, kT=o.kT, fluid_T=o.fluid_T,
+                    diss_energy=o.diss_energy, globalt=o.globalt, energy_fluid=o.energy_fluid)
+
+    def remove(self, r):
+        self._ck(lib().mpcd_batch_remove(self._h, r), "batch_remove")
+
+    @property
+    def resident(self):
+        return lib().mpcd_batch_resident(self._h)
+
+    def autotune(self, trial_steps=50):
+        t = MpcdBatchTuning()
+        self._ck(lib().mpcd_batch_autotune(self._h, int(trial_steps), ctypes.byref(t)), "batch_autotune")
+        return dict(fluid_threads=t.fluid_threads, fluid_blocks=t.fluid_blocks, cell_threads=t.cell_threads,
+                    cell_blocks=t.cell_blocks, sort_interval=t.sort_interval)
+
+    def tuning(self):
+        t = MpcdBatchTuning()
+        self._ck(lib().mpcd_batch_get_tuning(self._h, ctypes.byref(t)), "batch_get_tuning")
+        return dict(fluid_threads=t.fluid_threads, fluid_blocks=t.fluid_blocks, cell_threads=t.cell_threads,
+                    cell_blocks=t.cell_blocks, sort_interval=t.sort_interval)
+
+    def set_tuning(self, **kw):
+        cur = self.tuning()
+        cur.update(kw)
+        t = MpcdBatchTuning(cur["fluid_threads"], cur["fluid_blocks"], cur["cell_threads"], cur["cell_blocks"],
+                            cur["sort_interval"])
+        self._ck(lib().mpcd_batch_set_tuning(self._h, ctypes.byref(t)), "batch_set_tuning")
+
+    def launch_count(self):
+        return lib().mpcd_batch_launch_count(self._h)

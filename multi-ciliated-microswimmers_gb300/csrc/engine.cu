@@ -20,6 +20,8 @@
 
 #include "../../include/mpcd_gpu.h"
 #include "engine_internal.h"
+#include "md_plan.h"
+#include "engine_export.h"
 
 
 using namespace mpcd;
@@ -247,387 +249,49 @@ int check_launch(mpcd_engine* h, const char* what) {
   return MPCD_OK;
 }
 
-// Build the MD device layout: tiles of `tile` slots, one CTA each.  A bead
-// owns 1 + h consecutive slots (h helper slots when its spring list is longer
-// than kChunk, each helper summing one chunk).  Every cilium occupies
-// contiguous slots of one tile; the other beads fill the remaining space.
-int build_md(mpcd_engine* h, bool allow_cluster = true, bool no_react = false) {
-  // springs per helper slot: the longest serial spring chain of any thread.
-  // Odd, so that the helper slots' spring lists start in different
-  // shared-memory banks.
-  int kChunk = 31;
-  if (const char* env = std::getenv("MPCD_MD_CHUNK")) kChunk = std::max(2, std::min(256, std::atoi(env)));
+// Build the MD device layout (md_plan.cu plans it on the host; this uploads
+// it into freshly allocated device arrays).
+int build_md(mpcd_engine* h) {
   free_md(h->md);
   MDState& m = h->md;
   if (h->nb == 0) {
     h->md_dirty = false;
     return MPCD_OK;
   }
-  const long nb = h->nb;
-  const long nsp = (long)h->sp_t.size();
-  std::vector<int> nspr(nb, 0);
-  for (long i = 0; i < nsp; ++i) {
-    if (h->sp_t[i] < 0 || h->sp_t[i] >= nb || h->sp_o[i] < 0 || h->sp_o[i] >= nb)
-      return fail(h, MPCD_EINVAL, "spring bead index out of range");
-    nspr[h->sp_t[i]]++;
-  }
-  std::vector<int> width(nb);
-  for (long b = 0; b < nb; ++b) width[b] = 1 + (nspr[b] > kChunk ? (nspr[b] + kChunk - 1) / kChunk - 1 : 0);
-  std::vector<int> owner(nb, -1);  // cilium owning the bead
-  for (size_t c = 0; c < h->cil.size(); ++c)
-    for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) {
-      const long b = (long)h->cil[c].bead0 + k;
-      if (b < 0 || b >= nb) return fail(h, MPCD_EINVAL, "cilium bead range outside the bead array");
-      if (owner[b] >= 0) return fail(h, MPCD_EINVAL, "beads shared by two cilia");
-      owner[b] = (int)c;
-    }
-  // Hubs (a sphere's centre: one spring to every surface bead).  When every
-  // spring of a hub has an exact reverse partner inside the same run of
-  // non-cilium beads, the cluster layout drops the hub's own list and sums the
-  // partners' forces, negated, over the tile (react[j] marks the partners).
-  std::vector<int> run_id(nb, -1);
-  for (long b = 0, r = 0; b < nb; ++b)
-    if (owner[b] < 0) run_id[b] = (b > 0 && owner[b - 1] < 0) ? run_id[b - 1] : (int)r++;
-  std::vector<int> bstart(nb + 1, 0), blist(nsp);
-  for (long i = 0; i < nsp; ++i) bstart[h->sp_t[i] + 1]++;
-  for (long b = 0; b < nb; ++b) bstart[b + 1] += bstart[b];
-  {
-    std::vector<int> fillp(bstart.begin(), bstart.end() - 1);
-    for (long i = 0; i < nsp; ++i) blist[fillp[h->sp_t[i]]++] = (int)i;
-  }
-  std::vector<char> hub(nb, 0), react(nsp, 0), dropped(nsp, 0);
-  if (!no_react) {
-    for (long b = 0; b < nb; ++b) {
-      if (owner[b] >= 0 || nspr[b] <= kChunk) continue;
-      std::vector<int> partners;
-      bool ok = true;
-      for (int q = bstart[b]; q < bstart[b + 1] && ok; ++q) {
-        const int i = blist[q];
-        const int o = h->sp_o[i];
-        if (h->sp_k[i] != MPCD_SPRING_CONST || run_id[o] != run_id[b] || o == b) {
-          ok = false;
-          break;
-        }
-        int found = -1;
-        for (int r = bstart[o]; r < bstart[o + 1]; ++r) {
-          const int j = blist[r];
-          if (h->sp_o[j] == b && h->sp_k[j] == MPCD_SPRING_CONST && h->sp_rest[j] == h->sp_rest[i] &&
-              h->sp_kk[j] == h->sp_kk[i] && !react[j]) {
-            found = j;
-            break;
-          }
-        }
-        if (found < 0) ok = false;
-        else partners.push_back(found);
-      }
-      if (!ok) continue;
-      hub[b] = 1;
-      for (int j : partners) react[j] = 1;
-      for (int q = bstart[b]; q < bstart[b + 1]; ++q) dropped[blist[q]] = 1;
-    }
-  }
-  // every bead of a cilium owns the same number of slots (the kernels address
-  // a cilium's beads as slot0 + stride * (filament * rodlength + bead))
-  auto pad_cilia = [&]() {
-    for (size_t c = 0; c < h->cil.size(); ++c) {
-      int wmax = 1;
-      for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) wmax = std::max(wmax, width[h->cil[c].bead0 + k]);
-      for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) width[h->cil[c].bead0 + k] = wmax;
-    }
-  };
-  pad_cilia();
-  std::vector<int> width_grid = width;
-  int cl_chunk = kChunk;  // springs per slot of the chosen layout
-  int maxw = 0;
-  for (size_t c = 0; c < h->cil.size(); ++c) {
-    const mpcd_cilium& cl = h->cil[c];
-    int w = 0;
-    for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[(long)cl.bead0 + k];
-    maxw = std::max(maxw, w);
-  }
-  for (long b = 0; b < nb; ++b)
-    if (owner[b] < 0) maxw = std::max(maxw, width[b]);
-  // Pack: cilia first (each contiguous in one tile), then the other beads in
-  // the remaining space.  Returns the number of tiles.
-  std::vector<int> fill, slot_of(nb, -1), cil_tile(h->cil.size());
-  auto pack = [&](int tile) {
-    fill.clear();
-    std::fill(slot_of.begin(), slot_of.end(), -1);
-    for (size_t c = 0; c < h->cil.size(); ++c) {
-      const mpcd_cilium& cl = h->cil[c];
-      int w = 0;
-      for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[cl.bead0 + k];
-      if (fill.empty() || fill.back() + w > tile) fill.push_back(0);
-      const int t = (int)fill.size() - 1;
-      cil_tile[c] = t;
-      for (int k = 0; k < 3 * cl.rodlength; ++k) {
-        slot_of[cl.bead0 + k] = t * tile + fill[t];
-        fill[t] += width[cl.bead0 + k];
-      }
-    }
-    size_t tcur = 0;
-    for (long b = 0; b < nb; ++b) {
-      if (owner[b] >= 0) continue;
-      while (tcur < fill.size() && fill[tcur] + width[b] > tile) ++tcur;
-      if (tcur == fill.size()) fill.push_back(0);
-      slot_of[b] = (int)tcur * tile + fill[tcur];
-      fill[tcur] += width[b];
-    }
-    return (int)fill.size();
-  };
-  m.split = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 0) : (h->p.md_split ? 1 : 0);
-  // Cluster packing (split arithmetic): runs of consecutive non-cilium beads
-  // wider than 64 slots (a sphere, whose centre bead reaches every surface
-  // bead) each stay whole in one tile; cilia follow in order (next fit, so a
-  // tile's cilia have contiguous bond tables); the remaining beads fill gaps.
-  bool keep_hubs_whole = false;  // one-lane layout: hub runs stay in one tile (reactions)
-  auto pack_cluster = [&](int tile) {
-    fill.clear();
-    std::fill(slot_of.begin(), slot_of.end(), -1);
-    std::vector<std::pair<long, long>> runs;  // [begin, end) of non-cilium beads
-    for (long b = 0; b < nb;) {
-      if (owner[b] >= 0) {
-        ++b;
-        continue;
-      }
-      long e = b;
-      while (e < nb && owner[e] < 0) ++e;
-      runs.push_back({b, e});
-      b = e;
-    }
-    std::vector<char> placed(nb, 0);
-    for (auto& r : runs) {
-      long w = 0;
-      bool has_hub = false;
-      for (long b = r.first; b < r.second; ++b) {
-        w += width[b];
-        has_hub = has_hub || hub[b];
-      }
-      if (has_hub && keep_hubs_whole && w > tile) return 1 << 20;  // a hub's run must stay whole
-      if (w <= 64 || w > tile) continue;
-      fill.push_back(0);
-      const int t = (int)fill.size() - 1;
-      for (long b = r.first; b < r.second; ++b) {
-        slot_of[b] = t * tile + fill[t];
-        fill[t] += width[b];
-        placed[b] = 1;
-      }
-    }
-    const int first_cil_tile = (int)fill.size();
-    for (size_t c = 0; c < h->cil.size(); ++c) {
-      const mpcd_cilium& cl = h->cil[c];
-      int w = 0;
-      for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[cl.bead0 + k];
-      if ((int)fill.size() == first_cil_tile || fill.back() + w > tile) fill.push_back(0);
-      const int t = (int)fill.size() - 1;
-      cil_tile[c] = t;
-      for (int k = 0; k < 3 * cl.rodlength; ++k) {
-        slot_of[cl.bead0 + k] = t * tile + fill[t];
-        fill[t] += width[cl.bead0 + k];
-      }
-    }
-    for (long b = 0; b < nb; ++b) {
-      if (owner[b] >= 0 || placed[b]) continue;
-      size_t t = 0;
-      while (t < fill.size() && fill[t] + width[b] > tile) ++t;
-      if (t == fill.size()) fill.push_back(0);
-      slot_of[b] = (int)t * tile + fill[t];
-      fill[t] += width[b];
-    }
-    return (int)fill.size();
-  };
-  int tile = 0;
-  m.cluster = 0;
-  if (m.split && allow_cluster) {
-    int lanes_hi = 2, lanes_lo = 1;
-    if (const char* env = std::getenv("MPCD_MD_LANES")) lanes_hi = lanes_lo = std::max(1, std::min(2, std::atoi(env)));
-    for (int lanes = lanes_hi; lanes >= lanes_lo && !m.cluster; --lanes) {
-      // one lane per slot: short chunks (two slots per cilium bead) keep the
-      // serial spring chains short; hubs take their force from reactions
-      const int chunk = lanes == 2 ? kChunk : std::min(kChunk, 11);
-      keep_hubs_whole = lanes == 1;
-      for (long b = 0; b < nb; ++b)
-        width[b] = (hub[b] && keep_hubs_whole) ? 1
-                                               : 1 + (nspr[b] > chunk ? (nspr[b] + chunk - 1) / chunk - 1 : 0);
-      cl_chunk = chunk;
-      pad_cilia();
-      int maxw_cl = 0;
-      for (size_t c = 0; c < h->cil.size(); ++c) {
-        int w = 0;
-        for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) w += width[h->cil[c].bead0 + k];
-        maxw_cl = std::max(maxw_cl, w);
-      }
-      for (long b = 0; b < nb; ++b)
-        if (owner[b] < 0) maxw_cl = std::max(maxw_cl, width[b]);
-      maxw = maxw_cl;
-      const int tmax = 1024 / lanes;
-      for (int t = std::max(32, ((maxw + 31) / 32) * 32); t <= tmax; t += 32)
-        if (pack_cluster(t) <= 16) {
-          tile = t;
-          m.cluster = 1;
-          m.cl_lanes = lanes;
-          break;
-        }
-    }
-  }
-  if (m.cluster && !keep_hubs_whole) {  // two-lane layout: hubs keep their own lists and helpers
-    std::fill(hub.begin(), hub.end(), 0);
-    std::fill(react.begin(), react.end(), 0);
-    std::fill(dropped.begin(), dropped.end(), 0);
-  }
-  if (!m.cluster) {
-    width = width_grid;
-    cl_chunk = kChunk;
-    std::fill(hub.begin(), hub.end(), 0);
-    std::fill(react.begin(), react.end(), 0);
-    std::fill(dropped.begin(), dropped.end(), 0);
-    maxw = 0;
-    for (size_t c = 0; c < h->cil.size(); ++c) {
-      int w = 0;
-      for (int k = 0; k < 3 * h->cil[c].rodlength; ++k) w += width[h->cil[c].bead0 + k];
-      maxw = std::max(maxw, w);
-    }
-    for (long b = 0; b < nb; ++b)
-      if (owner[b] < 0) maxw = std::max(maxw, width[b]);
-    tile = std::max(32, ((maxw + 15) / 16) * 16);
-    if (tile > 1024) return fail(h, MPCD_EINVAL, "an MD group needs more than 1024 slots");
-    pack(tile);
-  }
-  // a hub and all its partners must share one tile, one hub per tile
-  std::vector<int> tile_react;
-  {
-    const int nt = (int)fill.size();
-    tile_react.assign(nt, -1);
-    bool bad = false;
-    for (long b = 0; b < nb && !bad; ++b) {
-      if (!hub[b]) continue;
-      const int t = slot_of[b] / tile;
-      if (tile_react[t] >= 0) bad = true;
-      tile_react[t] = slot_of[b] - t * tile;
-    }
-    for (long i = 0; i < nsp && !bad; ++i)
-      if (react[i] && slot_of[h->sp_t[i]] / tile != slot_of[h->sp_o[i]] / tile) bad = true;
-    if (bad) return build_md(h, allow_cluster, true);
-  }
-  m.tile = tile;
-  m.ntiles = (int)fill.size();
-  m.nslots = m.ntiles * tile;
+  MDInput in;
+  in.nb = h->nb;
+  in.bpos = h->bpos.data();
+  in.bvel = h->bvel.data();
+  in.bmoves = h->bmoves.data();
+  in.nsp = (long)h->sp_t.size();
+  in.sp_t = h->sp_t.data();
+  in.sp_o = h->sp_o.data();
+  in.sp_k = h->sp_k.data();
+  in.sp_r = h->sp_r.data();
+  in.sp_rest = h->sp_rest.data();
+  in.sp_kk = h->sp_kk.data();
+  in.ncil = (int)h->cil.size();
+  in.cil = h->cil.data();
+  in.nbond = (long)h->newlen.size();
+  in.newlen = h->newlen.data();
+  in.oldlen = h->oldlen.data();
+  in.split = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 0) : (h->p.md_split ? 1 : 0);
+  MDPlan pl;
+  const std::string why = plan_md(in, MDForce{}, true, false, h->p.precision == MPCD_FP32 ? 1 : 0, pl);
+  if (!why.empty()) return fail(h, MPCD_EINVAL, why);
+  m.split = pl.split;
+  m.cluster = pl.cluster;
+  m.cl_lanes = pl.cl_lanes;
+  m.cl_nsp_max = pl.cl_nsp_max;
+  m.cl_nbond_max = pl.cl_nbond_max;
+  m.tile = pl.tile;
+  m.ntiles = pl.ntiles;
+  m.nslots = pl.nslots;
+  m.hmax = pl.hmax;
   const int ns = m.nslots;
-  std::vector<double> X(ns, 0.0), Y(ns, 0.0), Z(ns, 0.0), VX(ns, 0.0), VY(ns, 0.0), VZ(ns, 0.0);
-  std::vector<int> mv(ns, -1), prim(ns, 0), nhelp(ns, 0), thelp(m.ntiles, 0);
-  for (long b = 0; b < nb; ++b) {
-    const int s = slot_of[b];
-    X[s] = h->bpos[3 * b];
-    Y[s] = h->bpos[3 * b + 1];
-    Z[s] = h->bpos[3 * b + 2];
-    VX[s] = h->bvel[3 * b];
-    VY[s] = h->bvel[3 * b + 1];
-    VZ[s] = h->bvel[3 * b + 2];
-    mv[s] = h->bmoves[b] ? 1 : 0;
-    prim[s] = s;
-    nhelp[s] = width[b] - 1;
-    for (int k = 1; k < width[b]; ++k) {
-      mv[s + k] = 2;
-      prim[s + k] = s;
-      X[s + k] = X[s];
-      Y[s + k] = Y[s];
-      Z[s + k] = Z[s];
-    }
-    if (width[b] > 1) thelp[s / tile] = 1;
-  }
-  // springs: CSR by slot; a bead's list (in input order) is cut into chunks of
-  // kChunk over its primary and helper slots
-  std::vector<int> start(ns + 1, 0);
-  std::vector<int> seen(nb, 0);
-  std::vector<int> sslot(nsp);
-  for (long i = 0; i < nsp; ++i) {
-    if (dropped[i]) {
-      sslot[i] = -1;
-      continue;
-    }
-    const int b = h->sp_t[i];
-    const int chunk = width[b] > 1 ? seen[b] / cl_chunk : 0;
-    seen[b]++;
-    sslot[i] = slot_of[b] + chunk;
-    start[sslot[i] + 1]++;
-  }
-  for (int s = 0; s < ns; ++s) start[s + 1] += start[s];
-  std::vector<int> pos(start.begin(), start.end() - 1);
-  const long nspk = start[ns];  // springs kept
-  std::vector<int> so(nspk), sk(nspk), sr(nspk);
-  std::vector<double> srest(nspk), sm2k(nspk);
-  for (long i = 0; i < nsp; ++i) {
-    if (sslot[i] < 0) continue;
-    const int d = pos[sslot[i]]++;
-    so[d] = slot_of[h->sp_o[i]];
-    sk[d] = h->sp_k[i] | (react[i] ? kSpringReact : 0);
-    sr[d] = h->sp_r[i];
-    srest[d] = h->sp_rest[i];
-    sm2k[d] = -2.0 * h->sp_kk[i];
-  }
-  // halos: per tile the distinct slots of other tiles its springs reach, and
-  // every spring's other bead as an index into the tile's staged positions
-  std::vector<int> sl(nspk), halo, hstart(m.ntiles + 1, 0);
-  int hmax = 0;
-  for (int t = 0; t < m.ntiles; ++t) {
-    const int b0 = t * tile, b1 = b0 + tile;
-    std::vector<int> ext;
-    for (int s2 = start[b0]; s2 < start[b1]; ++s2)
-      if (so[s2] < b0 || so[s2] >= b1) ext.push_back(so[s2]);
-    std::sort(ext.begin(), ext.end());
-    ext.erase(std::unique(ext.begin(), ext.end()), ext.end());
-    for (int s2 = start[b0]; s2 < start[b1]; ++s2) {
-      if (so[s2] >= b0 && so[s2] < b1)
-        sl[s2] = so[s2] - b0;
-      else
-        sl[s2] = tile + (int)(std::lower_bound(ext.begin(), ext.end(), so[s2]) - ext.begin());
-    }
-    hstart[t + 1] = hstart[t] + (int)ext.size();
-    halo.insert(halo.end(), ext.begin(), ext.end());
-    hmax = std::max(hmax, (int)ext.size());
-  }
-  m.hmax = hmax;
-  if (m.cluster) {
-    // per-tile maxima for the cluster kernel's shared-memory layout
-    m.cl_nsp_max = 0;
-    m.cl_nbond_max = 0;
-    std::vector<int> tb(m.ntiles, 0);
-    for (size_t c = 0; c < h->cil.size(); ++c) tb[cil_tile[c]] += h->cil[c].rodlength;
-    for (int t = 0; t < m.ntiles; ++t) {
-      m.cl_nsp_max = std::max(m.cl_nsp_max, start[(t + 1) * tile] - start[t * tile]);
-      m.cl_nbond_max = std::max(m.cl_nbond_max, tb[t]);
-    }
-    if (!md_cluster_feasible(m)) return build_md(h, false);  // grid layout instead
-  } else {
-    const int cap = md_max_coresident_blocks(m, h->p.precision == MPCD_FP32 ? 1 : 0);
-    if (m.ntiles > cap) return fail(h, MPCD_EINVAL, "MD tiles exceed the co-resident CTA limit of the device");
-  }
-  // cilia
-  std::vector<CiliumDev> cd(h->cil.size());
-  std::vector<double> mid(h->cil.size()), ts(h->cil.size());
-  std::vector<int> tcil(m.ntiles + 1, 0);
-  for (size_t c = 0; c < h->cil.size(); ++c) {
-    const mpcd_cilium& cl = h->cil[c];
-    CiliumDev& d = cd[c];
-    d.stride = width[cl.bead0];
-    d.kind = cl.kind;
-    d.len = cl.rodlength;
-    d.num_anker = cl.num_anker;
-    d.slot0 = slot_of[cl.bead0];
-    d.bond_base = cl.bond_base;
-    d.beatstrength = cl.beatstrength;
-    d.bending = cl.bending;
-    d.max_bend = cl.max_bend;
-    d.m_speed = cl.m_speed;
-    d.power_dur = cl.power_stroke_duration;
-    d.recovery_dur = cl.recovery_stroke_duration;
-    d.start = cl.start;
-    mid[c] = cl.midpnt;
-    ts[c] = cl.tstroke;
-    tcil[cil_tile[c] + 1]++;
-  }
-  for (int t = 0; t < m.ntiles; ++t) tcil[t + 1] += tcil[t];
-  const size_t nbond = h->newlen.size();
+  const long nspk = pl.nsp_kept();
+  const size_t nbond = pl.newlen.size();
+  const size_t ncil = pl.cd.size();
   for (int b = 0; b < 2; ++b) {
     CK(dalloc(&m.x[b], ns));
     CK(dalloc(&m.y[b], ns));
@@ -643,7 +307,7 @@ int build_md(mpcd_engine* h, bool allow_cluster = true, bool no_react = false) {
   CK(dalloc(&m.sp_start, ns + 1));
   CK(dalloc(&m.sp_other, nspk));
   CK(dalloc(&m.sp_local, nspk));
-  CK(dalloc(&m.halo, halo.size()));
+  CK(dalloc(&m.halo, pl.halo.size()));
   CK(dalloc(&m.halo_start, m.ntiles + 1));
   CK(dalloc(&m.diag, nbond));
   CK(dalloc(&m.sp_kind, nspk));
@@ -651,58 +315,55 @@ int build_md(mpcd_engine* h, bool allow_cluster = true, bool no_react = false) {
   CK(dalloc(&m.sp_rest, nspk));
   CK(dalloc(&m.sp_m2k, nspk));
   CK(dalloc(&m.tile_react, m.ntiles));
-  m.ncil = (int)h->cil.size();
-  CK(dalloc(&m.cil, cd.size()));
-  CK(dalloc(&m.midpnt, cd.size()));
-  CK(dalloc(&m.tstroke, cd.size()));
+  m.ncil = (int)ncil;
+  CK(dalloc(&m.cil, ncil));
+  CK(dalloc(&m.midpnt, ncil));
+  CK(dalloc(&m.tstroke, ncil));
   CK(dalloc(&m.newlen, nbond));
   CK(dalloc(&m.oldlen, nbond));
   CK(dalloc(&m.tile_cil, m.ntiles + 1));
   auto up = [&](void* d, const void* src, size_t bytes) { return cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice); };
   for (int b = 0; b < 2; ++b) {
-    CK(up(m.x[b], X.data(), ns * 8));
-    CK(up(m.y[b], Y.data(), ns * 8));
-    CK(up(m.z[b], Z.data(), ns * 8));
+    CK(up(m.x[b], pl.X.data(), ns * 8));
+    CK(up(m.y[b], pl.Y.data(), ns * 8));
+    CK(up(m.z[b], pl.Z.data(), ns * 8));
   }
-  CK(up(m.vx, VX.data(), ns * 8));
-  CK(up(m.vy, VY.data(), ns * 8));
-  CK(up(m.vz, VZ.data(), ns * 8));
-  CK(up(m.moves, mv.data(), ns * 4));
-  CK(up(m.prim, prim.data(), ns * 4));
-  CK(up(m.nhelp, nhelp.data(), ns * 4));
-  CK(up(m.tile_help, thelp.data(), m.ntiles * 4));
-  CK(up(m.sp_start, start.data(), (ns + 1) * 4));
+  CK(up(m.vx, pl.VX.data(), ns * 8));
+  CK(up(m.vy, pl.VY.data(), ns * 8));
+  CK(up(m.vz, pl.VZ.data(), ns * 8));
+  CK(up(m.moves, pl.mv.data(), ns * 4));
+  CK(up(m.prim, pl.prim.data(), ns * 4));
+  CK(up(m.nhelp, pl.nhelp.data(), ns * 4));
+  CK(up(m.tile_help, pl.thelp.data(), m.ntiles * 4));
+  CK(up(m.sp_start, pl.start.data(), (ns + 1) * 4));
   if (nspk) {
-    CK(up(m.sp_other, so.data(), nspk * 4));
-    CK(up(m.sp_local, sl.data(), nspk * 4));
-    CK(up(m.sp_kind, sk.data(), nspk * 4));
-    CK(up(m.sp_ref, sr.data(), nspk * 4));
-    CK(up(m.sp_rest, srest.data(), nspk * 8));
-    CK(up(m.sp_m2k, sm2k.data(), nspk * 8));
+    CK(up(m.sp_other, pl.so.data(), nspk * 4));
+    CK(up(m.sp_local, pl.sl.data(), nspk * 4));
+    CK(up(m.sp_kind, pl.sk.data(), nspk * 4));
+    CK(up(m.sp_ref, pl.sr.data(), nspk * 4));
+    CK(up(m.sp_rest, pl.srest.data(), nspk * 8));
+    CK(up(m.sp_m2k, pl.sm2k.data(), nspk * 8));
   }
-  CK(up(m.tile_react, tile_react.data(), m.ntiles * 4));
-  if (!cd.empty()) {
-    CK(up(m.cil, cd.data(), cd.size() * sizeof(CiliumDev)));
-    CK(up(m.midpnt, mid.data(), cd.size() * 8));
-    CK(up(m.tstroke, ts.data(), cd.size() * 8));
+  CK(up(m.tile_react, pl.tile_react.data(), m.ntiles * 4));
+  if (ncil) {
+    CK(up(m.cil, pl.cd.data(), ncil * sizeof(CiliumDev)));
+    CK(up(m.midpnt, pl.mid.data(), ncil * 8));
+    CK(up(m.tstroke, pl.ts.data(), ncil * 8));
   }
   if (nbond) {
-    std::vector<double> dg(nbond);
-    for (size_t k = 0; k < nbond; ++k) dg[k] = std::sqrt(0.5 * 0.5 + 0.5 * h->newlen[k]);
-    CK(up(m.newlen, h->newlen.data(), nbond * 8));
-    CK(up(m.oldlen, h->oldlen.data(), nbond * 8));
-    CK(up(m.diag, dg.data(), nbond * 8));
+    CK(up(m.newlen, pl.newlen.data(), nbond * 8));
+    CK(up(m.oldlen, pl.oldlen.data(), nbond * 8));
+    CK(up(m.diag, pl.diag.data(), nbond * 8));
   }
-  if (!halo.empty()) CK(up(m.halo, halo.data(), halo.size() * 4));
-  CK(up(m.halo_start, hstart.data(), (m.ntiles + 1) * 4));
-  CK(up(m.tile_cil, tcil.data(), (m.ntiles + 1) * 4));
+  if (!pl.halo.empty()) CK(up(m.halo, pl.halo.data(), pl.halo.size() * 4));
+  CK(up(m.halo_start, pl.hstart.data(), (m.ntiles + 1) * 4));
+  CK(up(m.tile_cil, pl.tcil.data(), (m.ntiles + 1) * 4));
   m.bar.count = h->d_bar;
   m.bar.gen = h->d_bar + 1;
-  h->slot_of = slot_of;
+  h->slot_of = pl.slot_of;
   h->md_dirty = false;
   return MPCD_OK;
 }
-
 // copy device bead state back into the host arrays
 int pull_md(mpcd_engine* h) {
   MDState& m = h->md;
@@ -805,6 +466,42 @@ int sort_fluid(mpcd_engine* h) {
 }
 
 }  // namespace
+
+namespace mpcd {
+
+int engine_export(mpcd_engine* h, EngineExport& out) {
+  if (!h) return MPCD_EINVAL;
+  int rc = pull_md(h);
+  if (rc) return rc;
+  out = EngineExport{};
+  out.p = h->p;
+  std::memcpy(out.a, h->a, sizeof out.a);
+  out.globalt = h->globalt;
+  out.steps = h->steps;
+  out.nf = mpcd_fluid_count(h);
+  if (out.nf > 0) {
+    out.fpos.resize(3 * out.nf);
+    out.fvel.resize(3 * out.nf);
+    rc = mpcd_get_fluid(h, out.nf, out.fpos.data(), out.fvel.data());
+    if (rc) return rc;
+  }
+  out.nb = h->nb;
+  out.bpos = h->bpos;
+  out.bvel = h->bvel;
+  out.bmoves = h->bmoves;
+  out.sp_t = h->sp_t;
+  out.sp_o = h->sp_o;
+  out.sp_k = h->sp_k;
+  out.sp_r = h->sp_r;
+  out.sp_rest = h->sp_rest;
+  out.sp_kk = h->sp_kk;
+  out.cil = h->cil;
+  out.newlen = h->newlen;
+  out.oldlen = h->oldlen;
+  return MPCD_OK;
+}
+
+}  // namespace mpcd
 
 extern "C" {
 

@@ -14,6 +14,7 @@
 #include <cstdio>
 
 #include "engine_internal.h"
+#include "fluid_device.cuh"
 
 namespace mpcd {
 
@@ -39,38 +40,6 @@ inline int grid_for(long n, int threads = kThreads, int per_sm = 4) {
   if (g < 1) g = 1;
   const long cap = (long)sm_count() * per_sm;
   return (int)(g < cap ? g : cap);
-}
-
-// sum over the block, float lanes, one float64 result (thread 0)
-__device__ __forceinline__ double block_sum_f32(float v) {
-  __shared__ double red32[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red32[wid] = (double)v;
-  __syncthreads();
-  double r = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += red32[w];
-  return r;
-}
-
-__device__ __forceinline__ double block_sum_f64(double v) {
-  __shared__ double red[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (wid == 0) {
-    r = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-  }
-  return r;  // valid in thread 0
 }
 
 // shifted cell along one axis from the cell index and the in-cell offset:
@@ -536,110 +505,25 @@ int scan_counts(const uint32_t* count, long ncell, uint32_t* start, uint32_t* bl
 // per-cell sums and collision maps float32.  The thermostat factor and the
 // rotation are computed per cell in float64 and rounded once.
 
-__device__ __forceinline__ int shifted_f(int i, float o, float ta, int L) {
-  int s = i + (o >= ta ? 1 : 0);
-  return s == L ? 0 : s;
-}
-
-__device__ __forceinline__ void rewrap_f(float& o, int& i, int L, unsigned& bad) {
-  if (o < 0.0f || o >= 1.0f) {
-    if (!(o > -1.0e9f && o < 1.0e9f)) {
-      o = 0.5f;
-      bad |= kErrCellRange;
-      return;
-    }
-    float fl = floorf(o);
-    o -= fl;
-    i += (int)fl;
-    if (o >= 1.0f) {
-      o = 0.0f;
-      i += 1;
-    }
-    i %= L;
-    if (i < 0) i += L;
-  }
-}
-
-__device__ __forceinline__ void red_add_v4(float4* addr, float4 v) {
-  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
-               : "memory");
-}
-
 // Split-precision collision map: everything per cell in float (the sums
 // are float); the dissipated-energy bookkeeping accumulates in float64.
 __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
   float ldiss = 0.0f;
   unsigned errbits = 0;
   bool gfail = false;
-  const float mb = a.fbead_mass;
-  const float ca = (float)kCosAlpha, sa = (float)kSinAlpha, oc = 1.0f - (float)kCosAlpha;
   for (long cid = (long)blockIdx.x * blockDim.x + threadIdx.x; cid < c.ncell; cid += (long)gridDim.x * blockDim.x) {
     const uint32_t w = c.cnt[cid];
     if (w == 0) continue;
     const float4 s = c.sum[cid];
     c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
     c.cnt[cid] = 0u;
-    const int nf = cnt_fluid(w), nb = cnt_beads(w);
-    const int num = nf + nb;
-    const float M = (float)nf + (float)nb * mb;
-    const float inv = 1.0f / M;
-    const float ux = s.x * inv, uy = s.y * inv, uz = s.z * inv;
-    const float erel = s.w - (ux * s.x + uy * s.y + uz * s.z);
-    float sc = 1.0f;
-    if (erel > 0.f && num > 1) {
-      float g;
-      if (a.inj_gamma) {
-        g = (float)a.inj_gamma[cid];
-        if (g < 0.f) {
-          errbits |= kErrGammaMissing;
-          g = 0.f;
-        }
-      } else {
-        g = gamma_mt(num, a.seed, a.step, (uint32_t)cid, &gfail);
-      }
-      sc = sqrtf(2.0f * g / erel);
-    }
-    float rx, ry, rz;
-    if (a.inj_axis) {
-      rx = (float)a.inj_axis[3 * cid + 0];
-      ry = (float)a.inj_axis[3 * cid + 1];
-      rz = (float)a.inj_axis[3 * cid + 2];
-    } else {
-      const u32x4 r = draw4(a.seed, a.step, kStreamCell, (uint32_t)cid, 0u);
-      const float ct = 2.0f * u01_flt(r.y) - 1.0f;
-      const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-      float sp, cp;
-      sincospif(2.0f * u01_flt(r.x), &sp, &cp);
-      rx = st * cp;
-      ry = st * sp;
-      rz = ct;
-    }
-    const float A00 = sc * (rx * rx + (1.0f - rx * rx) * ca), A01 = sc * (rx * ry * oc - rz * sa),
-                A02 = sc * (rx * rz * oc + ry * sa);
-    const float A10 = sc * (rx * ry * oc + rz * sa), A11 = sc * (ry * ry + (1.0f - ry * ry) * ca),
-                A12 = sc * (ry * rz * oc - rx * sa);
-    const float A20 = sc * (rx * rz * oc - ry * sa), A21 = sc * (ry * rz * oc + rx * sa),
-                A22 = sc * (rz * rz + (1.0f - rz * rz) * ca);
-    float4* p = c.par + 3 * cid;
-    p[0] = make_float4(A00, A01, A02, ux - (A00 * ux + A01 * uy + A02 * uz));
-    p[1] = make_float4(A10, A11, A12, uy - (A10 * ux + A11 * uy + A12 * uz));
-    p[2] = make_float4(A20, A21, A22, uz - (A20 * ux + A21 * uy + A22 * uz));
-    ldiss += s.w;
+    cell_map_f32(s, w, (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 3 * cid, ldiss,
+                 errbits, gfail);
   }
   if (gfail) errbits |= kErrGammaLoop;
   if (errbits) atomicOr(a.err, errbits);
   const double tot = block_sum_f32(ldiss);
   if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
-}
-
-__device__ __forceinline__ void apply_map_f32(const float4* par, float& vx, float& vy, float& vz) {
-  const float4 r0 = __ldg(par + 0), r1 = __ldg(par + 1), r2 = __ldg(par + 2);
-  const float nx = fmaf(r0.x, vx, fmaf(r0.y, vy, fmaf(r0.z, vz, r0.w)));
-  const float ny = fmaf(r1.x, vx, fmaf(r1.y, vy, fmaf(r1.z, vz, r1.w)));
-  const float nz = fmaf(r2.x, vx, fmaf(r2.y, vy, fmaf(r2.z, vz, r2.w)));
-  vx = nx;
-  vy = ny;
-  vz = nz;
 }
 
 __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF32 c, StepArgs a) {
@@ -822,6 +706,10 @@ int launch_sort_f64(FluidF64& f, FluidF64& tmp, const Box& box, uint32_t* count,
   f = tmp;
   tmp = t;
   return k + 1;
+}
+
+int scan_counts_ext(const uint32_t* count, long ncell, uint32_t* start, uint32_t* blocksums, cudaStream_t s) {
+  return scan_counts(count, ncell, start, blocksums, s);
 }
 
 int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s) {

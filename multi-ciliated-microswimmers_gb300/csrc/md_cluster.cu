@@ -15,7 +15,9 @@
 // velocities) and the integration stay float64 in registers.
 #include <cooperative_groups.h>
 
+#include "batch_internal.h"
 #include "engine_internal.h"
+#include "fluid_device.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -76,13 +78,16 @@ struct ClusterLayout {
   }
 };
 
+// The MD of one swimmer on one cluster; `tile` is this CTA's tile (the
+// cluster's CTAs hold consecutive tiles).  Bin::kCollide: the beads first
+// take the SRD collision of the current step (bead_collide folded in).
 template <int kCLanes, typename Bin>
-__global__ void __launch_bounds__(1024, 1) k_md_cluster(MDState m, MDStepArgs a, Bin bin, ClusterLayout lay) {
+__device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepArgs& a, const Bin& bin,
+                                                const ClusterLayout& lay, const int tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   cg::cluster_group cluster = cg::this_cluster();
   const int T = m.tile;
   const int np = lay.np;
-  const int tile = blockIdx.x;
   const int first_tile = tile - (int)cluster.block_rank();
   const int base = tile * T;
   // carve shared memory
@@ -137,8 +142,11 @@ __global__ void __launch_bounds__(1024, 1) k_md_cluster(MDState m, MDStepArgs a,
   // position as float hi + lo (x = hi + lo to ~48 bits), velocity and force float
   float xh[3] = {0.f, 0.f, 0.f}, xl[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
   float fx = 0.f, fy = 0.f, fz = 0.f;
+  double X[3] = {0.0, 0.0, 0.0};
   if (primary) {
-    const double X[3] = {m.x[0][slot], m.y[0][slot], m.z[0][slot]};
+    X[0] = m.x[0][slot];
+    X[1] = m.y[0][slot];
+    X[2] = m.z[0][slot];
     for (int d = 0; d < 3; ++d) {
       xh[d] = (float)X[d];
       xl[d] = (float)(X[d] - (double)xh[d]);
@@ -146,8 +154,15 @@ __global__ void __launch_bounds__(1024, 1) k_md_cluster(MDState m, MDStepArgs a,
     v[0] = (float)m.vx[slot];
     v[1] = (float)m.vy[slot];
     v[2] = (float)m.vz[slot];
-    if (lane == 0) buf(0).put(q, xh, xl);
   }
+  if constexpr (Bin::kCollide) {  // MDObject beads in MPCD::next_tstep (src/libcilia/mpcd.cpp:140-247)
+    double ke = 0.0;
+    if (moves && lane == 0) ke = bin.collide(X, v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
+    if ((threadIdx.x & 31) == 0 && ke != 0.0) bin.add_diss(-ke);
+  }
+  if (primary && lane == 0) buf(0).put(q, xh, xl);
   int cur = 0;
   int eval = 0;  // index of the force evaluation within this MPC step
   cluster.sync();  // every CTA's first buffer is filled
@@ -362,7 +377,15 @@ __global__ void __launch_bounds__(1024, 1) k_md_cluster(MDState m, MDStepArgs a,
   cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
+template <int kCLanes, typename Bin>
+__global__ void __launch_bounds__(1024, 1) k_md_cluster(MDState m, MDStepArgs a, Bin bin, ClusterLayout lay) {
+  md_cluster_body<kCLanes>(m, a, bin, lay, (int)blockIdx.x);
+}
+
 struct ClBinF64 {
+  static constexpr bool kCollide = false;
+  __device__ double collide(const double*, float*) const { return 0.0; }
+  __device__ void add_diss(double) const {}
   CellsF64 c;
   Box box;
   double an[3];
@@ -384,6 +407,9 @@ struct ClBinF64 {
 };
 
 struct ClBinF32 {
+  static constexpr bool kCollide = false;
+  __device__ double collide(const double*, float*) const { return 0.0; }
+  __device__ void add_diss(double) const {}
   CellsF32 c;
   Box box;
   double an[3];
@@ -404,6 +430,71 @@ struct ClBinF32 {
     atomicAdd(c.cnt + cid, 1u << 16);
   }
 };
+
+// Binning and bead collision of one replica of a batch (cells of the arena,
+// offset by the replica's first cell).
+struct BatchBin {
+  static constexpr bool kCollide = true;
+  float4* sum;
+  uint32_t* cnt;
+  const float4* par;
+  long cell0;
+  Box box;
+  const double* a_cur;
+  const double* a_next;
+  float mb;
+  double mbd;
+  unsigned* err;
+  double* diss;
+  // MDObject beads in the collision (MPCD::next_tstep, src/libcilia/mpcd.cpp:140-247)
+  __device__ double collide(const double* X, float* v) const {
+    const long cid = unwrapped_cell(box, a_cur, X[0], X[1], X[2]);
+    if (cid < 0) {
+      atomicOr(err, kErrCellRange);
+      return 0.0;
+    }
+    apply_map_f32(par + 3 * (cell0 + cid), v[0], v[1], v[2]);
+    return mbd * ((double)v[0] * v[0] + (double)v[1] * v[1] + (double)v[2] * v[2]);
+  }
+  __device__ void add_diss(double d) const { atomicAdd(diss, d); }
+  // md_loop_stop's binning with the next shift (src/libcilia/mdobject.cpp:62-72)
+  __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
+    const long cid = unwrapped_cell(box, a_next, x, y, z);
+    if (cid < 0) {
+      atomicOr(err, kErrCellRange);
+      return;
+    }
+    const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+    red_add_v4(sum + cell0 + cid, make_float4(fvx * mb, fvy * mb, fvz * mb, mb * (fvx * fvx + fvy * fvy + fvz * fvz)));
+    atomicAdd(cnt + cell0 + cid, 1u << 16);
+  }
+};
+
+// One cluster of `ctiles` CTAs per listed replica; inactive replicas leave at
+// once (the whole cluster together).
+template <int kCLanes>
+__global__ void __launch_bounds__(1024, 1)
+    k_md_cluster_batch(MDState m, BatchTables t, BatchCells c, const int* reps, int ctiles, ClusterLayout lay) {
+  __shared__ MDStepArgs sa;
+  const int r = reps[blockIdx.x / ctiles];
+  if (!t.step[r].active) return;
+  if (threadIdx.x == 0) sa = t.step[r].md;
+  __syncthreads();
+  const BatchRep& R = t.rep[r];
+  BatchBin bin;
+  bin.sum = c.sum;
+  bin.cnt = c.cnt;
+  bin.par = c.par;
+  bin.cell0 = R.cell0;
+  bin.box = sa.box;
+  bin.a_cur = sa.a_cur;
+  bin.a_next = sa.a_next;
+  bin.mb = (float)R.bead_mass;
+  bin.mbd = R.bead_mass;
+  bin.err = &t.state[r].err;
+  bin.diss = &t.state[r].diss;
+  md_cluster_body<kCLanes>(m, sa, bin, lay, R.md_tile0 + (int)(blockIdx.x % ctiles));
+}
 
 template <int L, typename Bin>
 cudaError_t launch_cluster_l(const MDState& m, const MDStepArgs& a, const Bin& bin, cudaStream_t s) {
@@ -469,6 +560,68 @@ int cluster_feasible_l(const MDState& m) {
 
 int md_cluster_feasible(const MDState& m) {
   return m.cl_lanes == 2 ? cluster_feasible_l<2>(m) : cluster_feasible_l<1>(m);
+}
+
+size_t md_cluster_batch_smem(int tile, int hmax, int nsp_max, int nbond_max) {
+  ClusterLayout lay{tile + hmax, nsp_max, nbond_max};
+  return lay.bytes(tile);
+}
+
+namespace {
+template <int L>
+cudaLaunchConfig_t batch_cfg(int nclusters, int tile, int ctiles, size_t smem, cudaStream_t s,
+                             cudaLaunchAttribute* attr) {
+  auto kern = k_md_cluster_batch<L>;
+  cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nclusters * ctiles);
+  cfg.blockDim = dim3(L * tile);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ctiles;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+}  // namespace
+
+int md_cluster_batch_feasible(int lanes, int tile, int ctiles, size_t smem) {
+  if (ctiles < 1 || ctiles > kMaxClusterTiles || lanes * tile > 1024 || smem + sizeof(MDStepArgs) > 227 * 1024) return 0;
+  cudaLaunchAttribute attr[1];
+  int n = 0;
+  cudaError_t e;
+  if (lanes == 2) {
+    cudaLaunchConfig_t cfg = batch_cfg<2>(1, tile, ctiles, smem, nullptr, attr);
+    e = cudaOccupancyMaxActiveClusters(&n, (const void*)k_md_cluster_batch<2>, &cfg);
+  } else {
+    cudaLaunchConfig_t cfg = batch_cfg<1>(1, tile, ctiles, smem, nullptr, attr);
+    e = cudaOccupancyMaxActiveClusters(&n, (const void*)k_md_cluster_batch<1>, &cfg);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n >= 1;
+}
+
+int launch_md_cluster_batch(const MDState& m, const BatchTables& t, BatchCells c, const int* reps, int nreps,
+                            int ctiles, int hmax, int nsp_max, int nbond_max, cudaStream_t s, cudaError_t* st) {
+  if (nreps <= 0) return 0;
+  ClusterLayout lay{m.tile + hmax, nsp_max, nbond_max};
+  const size_t smem = lay.bytes(m.tile);
+  cudaLaunchAttribute attr[1];
+  if (m.cl_lanes == 2) {
+    cudaLaunchConfig_t cfg = batch_cfg<2>(nreps, m.tile, ctiles, smem, s, attr);
+    *st = cudaLaunchKernelEx(&cfg, k_md_cluster_batch<2>, m, t, c, reps, ctiles, lay);
+  } else {
+    cudaLaunchConfig_t cfg = batch_cfg<1>(nreps, m.tile, ctiles, smem, s, attr);
+    *st = cudaLaunchKernelEx(&cfg, k_md_cluster_batch<1>, m, t, c, reps, ctiles, lay);
+  }
+  return 1;
 }
 
 int launch_md_cluster_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s,

@@ -1,0 +1,426 @@
+// MD layout planner (see md_plan.h).
+//
+// Beads live in slots: the MD kernels run one thread (or two lanes) per slot,
+// a tile of slots per CTA.  A bead owns 1 + h consecutive slots (h helper
+// slots when its spring list is longer than the chunk, each helper summing
+// one chunk).  Every cilium occupies contiguous slots of one tile, so that its
+// beat bookkeeping needs no synchronisation beyond its CTA.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <utility>
+
+#include "md_plan.h"
+
+namespace mpcd {
+
+std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster, bool no_react, int grid_f32cells,
+                    MDPlan& out) {
+  // springs per helper slot: the longest serial spring chain of any thread.
+  // Odd, so that the helper slots' spring lists start in different
+  // shared-memory banks.
+  int kChunk = 31;
+  if (const char* env = std::getenv("MPCD_MD_CHUNK")) kChunk = std::max(2, std::min(256, std::atoi(env)));
+  out = MDPlan{};
+  const bool forced = force.lanes > 0;
+  out.split = in.split;
+  if (in.nb == 0) return "";
+  const long nb = in.nb;
+  const long nsp = in.nsp;
+  const int ncil = in.ncil;
+  std::vector<int> nspr(nb, 0);
+  for (long i = 0; i < nsp; ++i) {
+    if (in.sp_t[i] < 0 || in.sp_t[i] >= nb || in.sp_o[i] < 0 || in.sp_o[i] >= nb)
+      return "spring bead index out of range";
+    nspr[in.sp_t[i]]++;
+  }
+  std::vector<int> width(nb);
+  for (long b = 0; b < nb; ++b) width[b] = 1 + (nspr[b] > kChunk ? (nspr[b] + kChunk - 1) / kChunk - 1 : 0);
+  std::vector<int> owner(nb, -1);  // cilium owning the bead
+  for (int c = 0; c < ncil; ++c)
+    for (int k = 0; k < 3 * in.cil[c].rodlength; ++k) {
+      const long b = (long)in.cil[c].bead0 + k;
+      if (b < 0 || b >= nb) return "cilium bead range outside the bead array";
+      if (owner[b] >= 0) return "beads shared by two cilia";
+      owner[b] = c;
+    }
+  // Hubs (a sphere's centre: one spring to every surface bead).  When every
+  // spring of a hub has an exact reverse partner inside the same run of
+  // non-cilium beads, the one-lane cluster layout drops the hub's own list
+  // and sums the partners' forces, negated, over the tile (react[j] marks
+  // the partners).
+  std::vector<int> run_id(nb, -1);
+  for (long b = 0, r = 0; b < nb; ++b)
+    if (owner[b] < 0) run_id[b] = (b > 0 && owner[b - 1] < 0) ? run_id[b - 1] : (int)r++;
+  std::vector<int> bstart(nb + 1, 0), blist(nsp);
+  for (long i = 0; i < nsp; ++i) bstart[in.sp_t[i] + 1]++;
+  for (long b = 0; b < nb; ++b) bstart[b + 1] += bstart[b];
+  {
+    std::vector<int> fillp(bstart.begin(), bstart.end() - 1);
+    for (long i = 0; i < nsp; ++i) blist[fillp[in.sp_t[i]]++] = (int)i;
+  }
+  std::vector<char> hub(nb, 0), react(nsp, 0), dropped(nsp, 0);
+  if (!no_react) {
+    for (long b = 0; b < nb; ++b) {
+      if (owner[b] >= 0 || nspr[b] <= kChunk) continue;
+      std::vector<int> partners;
+      bool ok = true;
+      for (int q = bstart[b]; q < bstart[b + 1] && ok; ++q) {
+        const int i = blist[q];
+        const int o = in.sp_o[i];
+        if (in.sp_k[i] != MPCD_SPRING_CONST || run_id[o] != run_id[b] || o == b) {
+          ok = false;
+          break;
+        }
+        int found = -1;
+        for (int r = bstart[o]; r < bstart[o + 1]; ++r) {
+          const int j = blist[r];
+          if (in.sp_o[j] == b && in.sp_k[j] == MPCD_SPRING_CONST && in.sp_rest[j] == in.sp_rest[i] &&
+              in.sp_kk[j] == in.sp_kk[i] && !react[j]) {
+            found = j;
+            break;
+          }
+        }
+        if (found < 0) ok = false;
+        else partners.push_back(found);
+      }
+      if (!ok) continue;
+      hub[b] = 1;
+      for (int j : partners) react[j] = 1;
+      for (int q = bstart[b]; q < bstart[b + 1]; ++q) dropped[blist[q]] = 1;
+    }
+  }
+  // every bead of a cilium owns the same number of slots (the kernels address
+  // a cilium's beads as slot0 + stride * (filament * rodlength + bead))
+  auto pad_cilia = [&]() {
+    for (int c = 0; c < ncil; ++c) {
+      int wmax = 1;
+      for (int k = 0; k < 3 * in.cil[c].rodlength; ++k) wmax = std::max(wmax, width[in.cil[c].bead0 + k]);
+      for (int k = 0; k < 3 * in.cil[c].rodlength; ++k) width[in.cil[c].bead0 + k] = wmax;
+    }
+  };
+  auto widest = [&]() {
+    int w_max = 0;
+    for (int c = 0; c < ncil; ++c) {
+      int w = 0;
+      for (int k = 0; k < 3 * in.cil[c].rodlength; ++k) w += width[(long)in.cil[c].bead0 + k];
+      w_max = std::max(w_max, w);
+    }
+    for (long b = 0; b < nb; ++b)
+      if (owner[b] < 0) w_max = std::max(w_max, width[b]);
+    return w_max;
+  };
+  pad_cilia();
+  std::vector<int> width_grid = width;
+  int cl_chunk = kChunk;  // springs per slot of the chosen layout
+  int maxw = widest();
+  // Pack: cilia first (each contiguous in one tile), then the other beads in
+  // the remaining space.  Returns the number of tiles.
+  std::vector<int> fill, slot_of(nb, -1), cil_tile(ncil);
+  auto pack = [&](int tile) {
+    fill.clear();
+    std::fill(slot_of.begin(), slot_of.end(), -1);
+    for (int c = 0; c < ncil; ++c) {
+      const mpcd_cilium& cl = in.cil[c];
+      int w = 0;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[cl.bead0 + k];
+      if (fill.empty() || fill.back() + w > tile) fill.push_back(0);
+      const int t = (int)fill.size() - 1;
+      cil_tile[c] = t;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) {
+        slot_of[cl.bead0 + k] = t * tile + fill[t];
+        fill[t] += width[cl.bead0 + k];
+      }
+    }
+    size_t tcur = 0;
+    for (long b = 0; b < nb; ++b) {
+      if (owner[b] >= 0) continue;
+      while (tcur < fill.size() && fill[tcur] + width[b] > tile) ++tcur;
+      if (tcur == fill.size()) fill.push_back(0);
+      slot_of[b] = (int)tcur * tile + fill[tcur];
+      fill[tcur] += width[b];
+    }
+    return (int)fill.size();
+  };
+  // Cluster packing (split arithmetic): runs of consecutive non-cilium beads
+  // wider than 64 slots (a sphere, whose centre bead reaches every surface
+  // bead) each stay whole in one tile; cilia follow in order (next fit, so a
+  // tile's cilia have contiguous bond tables); the remaining beads fill gaps.
+  bool keep_hubs_whole = false;  // one-lane layout: hub runs stay in one tile (reactions)
+  auto pack_cluster = [&](int tile) {
+    fill.clear();
+    std::fill(slot_of.begin(), slot_of.end(), -1);
+    std::vector<std::pair<long, long>> runs;  // [begin, end) of non-cilium beads
+    for (long b = 0; b < nb;) {
+      if (owner[b] >= 0) {
+        ++b;
+        continue;
+      }
+      long e = b;
+      while (e < nb && owner[e] < 0) ++e;
+      runs.push_back({b, e});
+      b = e;
+    }
+    std::vector<char> placed(nb, 0);
+    for (auto& r : runs) {
+      long w = 0;
+      bool has_hub = false;
+      for (long b = r.first; b < r.second; ++b) {
+        w += width[b];
+        has_hub = has_hub || hub[b];
+      }
+      if (has_hub && keep_hubs_whole && w > tile) return 1 << 20;  // a hub's run must stay whole
+      if (w <= 64 || w > tile) continue;
+      fill.push_back(0);
+      const int t = (int)fill.size() - 1;
+      for (long b = r.first; b < r.second; ++b) {
+        slot_of[b] = t * tile + fill[t];
+        fill[t] += width[b];
+        placed[b] = 1;
+      }
+    }
+    const int first_cil_tile = (int)fill.size();
+    for (int c = 0; c < ncil; ++c) {
+      const mpcd_cilium& cl = in.cil[c];
+      int w = 0;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) w += width[cl.bead0 + k];
+      if ((int)fill.size() == first_cil_tile || fill.back() + w > tile) fill.push_back(0);
+      const int t = (int)fill.size() - 1;
+      cil_tile[c] = t;
+      for (int k = 0; k < 3 * cl.rodlength; ++k) {
+        slot_of[cl.bead0 + k] = t * tile + fill[t];
+        fill[t] += width[cl.bead0 + k];
+      }
+    }
+    for (long b = 0; b < nb; ++b) {
+      if (owner[b] >= 0 || placed[b]) continue;
+      size_t t = 0;
+      while (t < fill.size() && fill[t] + width[b] > tile) ++t;
+      if (t == fill.size()) fill.push_back(0);
+      slot_of[b] = (int)t * tile + fill[t];
+      fill[t] += width[b];
+    }
+    return (int)fill.size();
+  };
+  // slot widths of a cluster layout with `lanes` threads per slot
+  auto cluster_widths = [&](int lanes) {
+    // one lane per slot: short chunks (two slots per cilium bead) keep the
+    // serial spring chains short; hubs take their force from reactions
+    const int chunk = lanes == 2 ? kChunk : std::min(kChunk, 11);
+    keep_hubs_whole = lanes == 1;
+    for (long b = 0; b < nb; ++b)
+      width[b] = (hub[b] && keep_hubs_whole) ? 1 : 1 + (nspr[b] > chunk ? (nspr[b] + chunk - 1) / chunk - 1 : 0);
+    cl_chunk = chunk;
+    pad_cilia();
+    maxw = widest();
+  };
+  int tile = 0;
+  out.cluster = 0;
+  if (forced) {
+    if (!in.split) return "a fixed cluster layout needs split arithmetic";
+    if (force.lanes < 1 || force.lanes > 2 || force.tile < 32 || force.tile * force.lanes > 1024 || force.tile % 32)
+      return "invalid fixed cluster layout";
+    cluster_widths(force.lanes);
+    if (maxw > force.tile) return "a cilium does not fit into one MD tile of the fixed layout";
+    if (pack_cluster(force.tile) > 16) return "the MD bead set needs more than 16 tiles of the fixed layout";
+    tile = force.tile;
+    out.cluster = 1;
+    out.cl_lanes = force.lanes;
+  } else if (in.split && allow_cluster) {
+    int lanes_hi = 2, lanes_lo = 1;
+    if (const char* env = std::getenv("MPCD_MD_LANES")) lanes_hi = lanes_lo = std::max(1, std::min(2, std::atoi(env)));
+    for (int lanes = lanes_hi; lanes >= lanes_lo && !out.cluster; --lanes) {
+      cluster_widths(lanes);
+      const int tmax = 1024 / lanes;
+      for (int t = std::max(32, ((maxw + 31) / 32) * 32); t <= tmax; t += 32)
+        if (pack_cluster(t) <= 16) {
+          tile = t;
+          out.cluster = 1;
+          out.cl_lanes = lanes;
+          break;
+        }
+    }
+  }
+  if (out.cluster && !keep_hubs_whole) {  // two-lane layout: hubs keep their own lists and helpers
+    std::fill(hub.begin(), hub.end(), 0);
+    std::fill(react.begin(), react.end(), 0);
+    std::fill(dropped.begin(), dropped.end(), 0);
+  }
+  if (!out.cluster) {
+    width = width_grid;
+    cl_chunk = kChunk;
+    std::fill(hub.begin(), hub.end(), 0);
+    std::fill(react.begin(), react.end(), 0);
+    std::fill(dropped.begin(), dropped.end(), 0);
+    maxw = widest();
+    tile = std::max(32, ((maxw + 15) / 16) * 16);
+    if (tile > 1024) return "an MD group needs more than 1024 slots";
+    pack(tile);
+  }
+  // a hub and all its partners must share one tile, one hub per tile
+  {
+    const int nt = (int)fill.size();
+    out.tile_react.assign(nt, -1);
+    bool bad = false;
+    for (long b = 0; b < nb && !bad; ++b) {
+      if (!hub[b]) continue;
+      const int t = slot_of[b] / tile;
+      if (out.tile_react[t] >= 0) bad = true;
+      out.tile_react[t] = slot_of[b] - t * tile;
+    }
+    for (long i = 0; i < nsp && !bad; ++i)
+      if (react[i] && slot_of[in.sp_t[i]] / tile != slot_of[in.sp_o[i]] / tile) bad = true;
+    if (bad) return plan_md(in, force, allow_cluster, true, grid_f32cells, out);
+  }
+  out.tile = tile;
+  out.ntiles = (int)fill.size();
+  out.nslots = out.ntiles * tile;
+  const int ns = out.nslots;
+  out.X.assign(ns, 0.0);
+  out.Y.assign(ns, 0.0);
+  out.Z.assign(ns, 0.0);
+  out.VX.assign(ns, 0.0);
+  out.VY.assign(ns, 0.0);
+  out.VZ.assign(ns, 0.0);
+  out.mv.assign(ns, -1);
+  out.prim.assign(ns, 0);
+  out.nhelp.assign(ns, 0);
+  out.thelp.assign(out.ntiles, 0);
+  for (long b = 0; b < nb; ++b) {
+    const int s = slot_of[b];
+    out.X[s] = in.bpos[3 * b];
+    out.Y[s] = in.bpos[3 * b + 1];
+    out.Z[s] = in.bpos[3 * b + 2];
+    out.VX[s] = in.bvel[3 * b];
+    out.VY[s] = in.bvel[3 * b + 1];
+    out.VZ[s] = in.bvel[3 * b + 2];
+    out.mv[s] = in.bmoves[b] ? 1 : 0;
+    out.prim[s] = s;
+    out.nhelp[s] = width[b] - 1;
+    for (int k = 1; k < width[b]; ++k) {
+      out.mv[s + k] = 2;
+      out.prim[s + k] = s;
+      out.X[s + k] = out.X[s];
+      out.Y[s + k] = out.Y[s];
+      out.Z[s + k] = out.Z[s];
+    }
+    if (width[b] > 1) out.thelp[s / tile] = 1;
+  }
+  // springs: CSR by slot; a bead's list (in input order) is cut into chunks
+  // over its primary and helper slots
+  std::vector<int>& start = out.start;
+  start.assign(ns + 1, 0);
+  std::vector<int> seen(nb, 0);
+  std::vector<int> sslot(nsp);
+  for (long i = 0; i < nsp; ++i) {
+    if (dropped[i]) {
+      sslot[i] = -1;
+      continue;
+    }
+    const int b = in.sp_t[i];
+    const int chunk = width[b] > 1 ? seen[b] / cl_chunk : 0;
+    seen[b]++;
+    sslot[i] = slot_of[b] + chunk;
+    start[sslot[i] + 1]++;
+  }
+  for (int s = 0; s < ns; ++s) start[s + 1] += start[s];
+  std::vector<int> pos(start.begin(), start.end() - 1);
+  const long nspk = start[ns];  // springs kept
+  out.so.assign(nspk, 0);
+  out.sk.assign(nspk, 0);
+  out.sr.assign(nspk, 0);
+  out.srest.assign(nspk, 0.0);
+  out.sm2k.assign(nspk, 0.0);
+  for (long i = 0; i < nsp; ++i) {
+    if (sslot[i] < 0) continue;
+    const int d = pos[sslot[i]]++;
+    out.so[d] = slot_of[in.sp_o[i]];
+    out.sk[d] = in.sp_k[i] | (react[i] ? kSpringReact : 0);
+    out.sr[d] = in.sp_r[i];
+    out.srest[d] = in.sp_rest[i];
+    out.sm2k[d] = -2.0 * in.sp_kk[i];
+  }
+  // halos: per tile the distinct slots of other tiles its springs reach, and
+  // every spring's other bead as an index into the tile's staged positions
+  out.sl.assign(nspk, 0);
+  out.hstart.assign(out.ntiles + 1, 0);
+  int hmax = 0;
+  for (int t = 0; t < out.ntiles; ++t) {
+    const int b0 = t * tile, b1 = b0 + tile;
+    std::vector<int> ext;
+    for (int s2 = start[b0]; s2 < start[b1]; ++s2)
+      if (out.so[s2] < b0 || out.so[s2] >= b1) ext.push_back(out.so[s2]);
+    std::sort(ext.begin(), ext.end());
+    ext.erase(std::unique(ext.begin(), ext.end()), ext.end());
+    for (int s2 = start[b0]; s2 < start[b1]; ++s2) {
+      if (out.so[s2] >= b0 && out.so[s2] < b1)
+        out.sl[s2] = out.so[s2] - b0;
+      else
+        out.sl[s2] = tile + (int)(std::lower_bound(ext.begin(), ext.end(), out.so[s2]) - ext.begin());
+    }
+    out.hstart[t + 1] = out.hstart[t] + (int)ext.size();
+    out.halo.insert(out.halo.end(), ext.begin(), ext.end());
+    hmax = std::max(hmax, (int)ext.size());
+  }
+  out.hmax = hmax;
+  MDState probe;  // the fields the feasibility checks read
+  probe.tile = tile;
+  probe.ntiles = out.ntiles;
+  probe.nslots = ns;
+  probe.hmax = hmax;
+  probe.split = out.split;
+  probe.cluster = out.cluster;
+  probe.cl_lanes = out.cl_lanes;
+  if (out.cluster) {
+    // per-tile maxima for the cluster kernel's shared-memory layout
+    std::vector<int> tb(out.ntiles, 0);
+    for (int c = 0; c < ncil; ++c) tb[cil_tile[c]] += in.cil[c].rodlength;
+    for (int t = 0; t < out.ntiles; ++t) {
+      out.cl_nsp_max = std::max(out.cl_nsp_max, start[(t + 1) * tile] - start[t * tile]);
+      out.cl_nbond_max = std::max(out.cl_nbond_max, tb[t]);
+    }
+    probe.cl_nsp_max = out.cl_nsp_max;
+    probe.cl_nbond_max = out.cl_nbond_max;
+    if (!md_cluster_feasible(probe)) {
+      if (forced) return "the fixed cluster layout does not fit on the device";
+      return plan_md(in, force, false, no_react, grid_f32cells, out);  // grid layout instead
+    }
+  } else {
+    const int cap = md_max_coresident_blocks(probe, grid_f32cells);
+    if (out.ntiles > cap) return "MD tiles exceed the co-resident CTA limit of the device";
+  }
+  // cilia
+  out.cd.assign(ncil, CiliumDev{});
+  out.mid.assign(ncil, 0.0);
+  out.ts.assign(ncil, 0.0);
+  out.tcil.assign(out.ntiles + 1, 0);
+  for (int c = 0; c < ncil; ++c) {
+    const mpcd_cilium& cl = in.cil[c];
+    CiliumDev& d = out.cd[c];
+    d.stride = width[cl.bead0];
+    d.kind = cl.kind;
+    d.len = cl.rodlength;
+    d.num_anker = cl.num_anker;
+    d.slot0 = slot_of[cl.bead0];
+    d.bond_base = cl.bond_base;
+    d.beatstrength = cl.beatstrength;
+    d.bending = cl.bending;
+    d.max_bend = cl.max_bend;
+    d.m_speed = cl.m_speed;
+    d.power_dur = cl.power_stroke_duration;
+    d.recovery_dur = cl.recovery_stroke_duration;
+    d.start = cl.start;
+    out.mid[c] = cl.midpnt;
+    out.ts[c] = cl.tstroke;
+    out.tcil[cil_tile[c] + 1]++;
+  }
+  for (int t = 0; t < out.ntiles; ++t) out.tcil[t + 1] += out.tcil[t];
+  out.newlen.assign(in.newlen, in.newlen + in.nbond);
+  out.oldlen.assign(in.oldlen, in.oldlen + in.nbond);
+  out.diag.resize(in.nbond);
+  for (long k = 0; k < in.nbond; ++k) out.diag[k] = std::sqrt(0.5 * 0.5 + 0.5 * in.newlen[k]);
+  out.slot_of = slot_of;
+  return "";
+}
+
+}  // namespace mpcd

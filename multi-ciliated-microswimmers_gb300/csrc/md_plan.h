@@ -1,0 +1,58 @@
+// Host-side planning of the MD device layout: which slot every bead owns,
+// the springs in CSR by slot, tile halos, cilium records.  Shared by the
+// single-box engine (engine.cu) and the replica batch (batch.cu).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/mpcd_gpu.h"
+#include "engine_internal.h"
+
+namespace mpcd {
+
+// The bead set of one box as the setters received it (mpcd_set_beads,
+// mpcd_set_springs, mpcd_set_cilia).
+struct MDInput {
+  long nb = 0;
+  const double* bpos = nullptr;  // [nb][3]
+  const double* bvel = nullptr;  // [nb][3]
+  const int* bmoves = nullptr;   // [nb] 1 integrated, 0 fixed
+  long nsp = 0;
+  const int *sp_t = nullptr, *sp_o = nullptr, *sp_k = nullptr, *sp_r = nullptr;
+  const double *sp_rest = nullptr, *sp_kk = nullptr;
+  int ncil = 0;
+  const mpcd_cilium* cil = nullptr;
+  long nbond = 0;
+  const double *newlen = nullptr, *oldlen = nullptr;
+  int split = 0;  // 1: float spring arithmetic on hi/lo position pairs
+};
+
+// A fixed cluster layout (lanes per slot, slots per tile), or {0, 0} to let
+// the planner search (cluster first when split, else the grid layout).
+struct MDForce {
+  int lanes = 0;
+  int tile = 0;
+};
+
+// Host arrays of an MDState (engine_internal.h), indices local to the box.
+struct MDPlan {
+  int tile = 0, ntiles = 0, nslots = 0, hmax = 0;
+  int split = 0, cluster = 0, cl_nsp_max = 0, cl_nbond_max = 0, cl_lanes = 2;
+  std::vector<double> X, Y, Z, VX, VY, VZ;
+  std::vector<int> mv, prim, nhelp, thelp, tile_react;
+  std::vector<int> start, so, sl, sk, sr;
+  std::vector<double> srest, sm2k;
+  std::vector<int> halo, hstart;
+  std::vector<CiliumDev> cd;
+  std::vector<double> mid, ts, newlen, oldlen, diag;
+  std::vector<int> tcil;
+  std::vector<int> slot_of;  // bead -> primary slot
+  long nsp_kept() const { return (long)so.size(); }
+};
+
+// Plans the layout.  Returns an empty string on success, else the reason.
+// `grid_f32cells` selects the co-resident limit checked for the grid layout.
+std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster, bool no_react, int grid_f32cells,
+                    MDPlan& out);
+
+}  // namespace mpcd

@@ -255,6 +255,31 @@ def fibonacci_clami(n_cilia: int, *, radius: float, center, rodlength: int = 15,
     }
 
 
+def swimmer_config(L: int, *, radius: float, n_cilia: int, rodlength: int = 15, seed: int = 0,
+                   ststep: float = 0.002, name: str = "swimmer") -> dict:
+    """A periodic L^3 box (10 particles per cell) with a Clami of `n_cilia`
+    Fibonacci-lattice cilia at the centre (the ensemble and serving workloads)."""
+    cfg = plain_fluid(int(L), name=name)
+    cfg["ststep"] = float(ststep)
+    cfg["md_objects"] = (fibonacci_clami(int(n_cilia), radius=float(radius), center=(L / 2, L / 2, L / 2),
+                                         rodlength=int(rodlength), seed=seed),)
+    return cfg
+
+
+def ensemble_specs(n: int, seed: int = 0, edges=(16, 24, 32, 40, 48), max_cilia: int = 64,
+                   rodlengths=(10, 15)) -> list:
+    """Replica shapes of the batched ensemble: box edge uniform over `edges`,
+    sphere radius edge/8, cilia count uniform in [0, max_cilia], rodlength
+    uniform in [rodlengths[0], rodlengths[1]], independent seeds."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        L = int(rng.choice(edges))
+        out.append(dict(L=L, radius=L / 8.0, n_cilia=int(rng.integers(0, max_cilia + 1)),
+                        rodlength=int(rng.integers(rodlengths[0], rodlengths[1] + 1)), seed=int(1000 * seed + i + 1)))
+    return out
+
+
 def baseline_config(which: str, **kw) -> dict:
     """Configurations of the benchmark workloads.
 
