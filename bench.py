@@ -16,6 +16,10 @@ roofline: the fluid collide+stream kernel against the measured HBM copy
          particle state (float64: 6 x 8 B each way = 96 B; float32 split: 64 B).
 cpu_baseline: the C restatement of the reference (oracle/) with OpenMP on the
          host cores, on a bounded sample of the same workload.
+batched: the 64-replica mixed-size ensemble (box edges 16..48, 0-64 cilia)
+         advanced together by the replica batch (float32 split, CUDA graphs,
+         autotuned launch configuration), 1000 MPC steps timed, beside the
+         same replicas run one at a time through the single-box engine.
 
 --impl reference runs that CPU restatement alone (the reference's own
 sources are not available where this runs) and prints its line.
@@ -187,6 +191,77 @@ def run_e2e(args):
     return dict(value=(nf + nb) * args.steps / wall, h2d=h2d, d2h=d2h)
 
 
+# --------------------------------------------------------- batched ensemble --
+
+def run_ensemble(args, n=64, steps=1000):
+    """64 uneven replicas (box edge in {16..48}, sphere radius edge/8, 0-64
+    cilia of rodlength 10-15) advanced together by the replica batch, FP32
+    split, `steps` MPC steps timed; beside it the same replicas run one at a
+    time through the single-box engine (the plain path), FP64 and FP32."""
+    import cilia_gpu as cg
+
+    specs = simcfg.ensemble_specs(n, seed=11)
+    b = cg.Batch.for_specs(specs, device=args.device)
+    ids, parts = [], 0
+    single = {"fp64": [0.0, 0.0], "fp32": [0.0, 0.0]}  # particle-steps, ms
+    for sp in specs:
+        text = simcfg.dumps(simcfg.swimmer_config(sp["L"], radius=sp["radius"], n_cilia=sp["n_cilia"],
+                                                  rodlength=sp["rodlength"], seed=sp["seed"]))
+        for prec, key in ((cg.MPCD_FP64, "fp64"), (cg.MPCD_FP32, "fp32")):
+            s = cg.Sim(text, precision=prec, ststep=0.002, seed=sp["seed"], device=args.device)
+            npart = 10 * sp["L"] ** 3 + s.nbeads
+            s.engine.run(3)
+            ms = s.engine.timed_run(5, flush_l2=True)
+            single[key][0] += npart * 5
+            single[key][1] += float(ms.sum())
+            if key == "fp32":
+                r = b.add_engine(s.engine)
+                b.admit(r)
+                ids.append(r)
+                parts += npart
+            s.close()
+    for r in ids:
+        b.set_steps(r, 10 ** 9)
+    tuning = b.autotune(trial_steps=50)
+    stage = b.stage_times(20)
+    for r in ids:
+        b.set_steps(r, steps)
+    l0 = b.launch_count()
+    with ClockSampler(args.device) as clk:
+        ms = b.timed_run(steps)
+    launches = b.launch_count() - l0
+    value = parts * steps / (ms / 1e3)
+    kts, mom, errs = [], [], 0
+    for r in ids:
+        st = b.status(r)
+        errs += int(st["err"] != 0 or st["steps"] < steps)
+        o = b.observables(r)
+        kts.append(o["kT"])
+        mom.append(float(np.abs(o["momentum"]).max()))
+    nf_tot = sum(10 * sp["L"] ** 3 for sp in specs)
+    hbm, peak_kind = peaks()
+    achieved = nf_tot * 64 / (stage["fluid"] * 1e-3) / 1e9
+    plain64 = single["fp64"][0] / (single["fp64"][1] / 1e3)
+    plain32 = single["fp32"][0] / (single["fp32"][1] / 1e3)
+    b.close()
+    return {
+        "workload": f"ensemble{n}: {n} replicas, box edge uniform in {{16,24,32,40,48}} x 10 fluid/cell, "
+                    f"Clami radius edge/8 with 0-64 cilia of 3x(10-15) beads, 50 MD substeps, float32 split; "
+                    f"{parts} particles (fluid + beads)",
+        "metric": METRIC, "value": value, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
+        "l2": "inputs (0.9 GB of fluid state) larger than L2", "gpu_launches": launches,
+        "plain_single_run": {"fp64": plain64, "fp32": plain32,
+                             "how": "each replica alone through the single-box engine, 5 timed steps, L2 flushed"},
+        "speedup_vs_plain_fp64": value / plain64, "speedup_vs_single_fp32": value / plain32,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "kernel": "batch fluid_step (collide + stream + bin), stages serialised",
+                     "bytes_per_particle_step": 64, "avg_launch_ms": stage["fluid"]},
+        "stage_ms_per_step": stage, "tuning": tuning, "clocks": clk.summary(),
+        "kT": {"min": min(kts), "max": max(kts), "mean": float(np.mean(kts))},
+        "max_momentum_per_mass": max(mom), "replicas_with_errors": errs,
+    }
+
+
 # ------------------------------------------------------------------ CPU arm --
 
 def run_cpu(args, budget_s=None, threads=None):
@@ -229,6 +304,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--verify-counts", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--ensemble-only", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -260,6 +337,10 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.ensemble_only:
+        if rank == 0:
+            print(json.dumps(run_ensemble(args)))
+        return
     if dist is not None:
         dist.barrier()
     g = run_gpu(args, rank)
@@ -310,6 +391,8 @@ def main():
         e = run_e2e(args)
         line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                        "d2h_bytes_per_step": e["d2h"]}
+    if not args.no_ensemble and args.gpus == 1:
+        line["batched"] = run_ensemble(args)
     if not args.no_cpu:
         c = run_cpu(args)
         line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",

@@ -96,12 +96,21 @@ int mpcd_batch_observables(mpcd_batch* b, int r, mpcd_obs* out);
 int mpcd_batch_remove(mpcd_batch* b, int r);
 int mpcd_batch_resident(const mpcd_batch* b);
 
-/* times candidate launch configurations on `trial_steps` real steps each
- * (the replicas advance; results do not depend on the configuration) and
- * keeps the fastest */
+/* re-plans every swimmer's MD with another cluster layout (threads per
+ * slot, slots per CTA); nothing changes when a swimmer does not fit */
+int mpcd_batch_set_md_layout(mpcd_batch* b, int lanes, int tile);
+int mpcd_batch_get_md_layout(const mpcd_batch* b, int* lanes, int* tile);
+/* times candidate configurations (MD layout, fluid and cell launch shapes,
+ * sort interval) on `trial_steps` real steps each (the replicas advance;
+ * results do not depend on the configuration) and keeps the fastest */
 int mpcd_batch_autotune(mpcd_batch* b, int trial_steps, mpcd_batch_tuning* chosen);
 int mpcd_batch_set_tuning(mpcd_batch* b, const mpcd_batch_tuning* t);
 int mpcd_batch_get_tuning(const mpcd_batch* b, mpcd_batch_tuning* t);
+/* nsteps steps launched stage by stage without graphs, each stage bracketed
+ * by CUDA events and the MD after the fluid pass (not beside it): device ms
+ * per step of out[0] prologue + cell maps, out[1] fluid collide + stream +
+ * bin, out[2] MD of all swimmers, out[3] counting sorts (amortised) */
+int mpcd_batch_stage_times(mpcd_batch* b, int nsteps, double* out4);
 /* kernels launched so far (graph launches count their kernels) */
 long long mpcd_batch_launch_count(const mpcd_batch* b);
 

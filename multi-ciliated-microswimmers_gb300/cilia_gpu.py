@@ -145,6 +145,9 @@ def lib():
             "mpcd_batch_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(MpcdBatchTuning)]),
             "mpcd_batch_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(MpcdBatchTuning)]),
             "mpcd_batch_launch_count": (ctypes.c_longlong, [P]),
+            "mpcd_batch_stage_times": (ctypes.c_int, [P, ctypes.c_int, _DP]),
+            "mpcd_batch_set_md_layout": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+            "mpcd_batch_get_md_layout": (ctypes.c_int, [P, _IP, _IP]),
             "cilia_sim_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
                                                 ctypes.POINTER(P)]),
             "cilia_sim_destroy": (ctypes.c_int, [P]),
@@ -387,6 +390,22 @@ class Batch:
             raise MpcdError(f"mpcd_batch_create failed with code {rc}")
         self._h = h
 
+    @classmethod
+    def for_specs(cls, specs, extra_replicas=2, **kw):
+        """A batch with room for replicas of the given shapes (dicts with L,
+        n_cilia, rodlength; a Clami sphere of 643 beads each when n_cilia is
+        given, no beads when `beads` is False)."""
+        nf = sum(10 * s["L"] ** 3 for s in specs)
+        nc = sum(s["L"] ** 3 for s in specs)
+        nb = sum((643 + 3 * s["n_cilia"] * s["rodlength"]) if s.get("beads", True) else 0 for s in specs)
+        k = len(specs)
+        args = dict(max_replicas=k + extra_replicas, max_particles=nf + 8192 * k, max_cells=nc + 2048 * k,
+                    max_slots=2 * nb + 1024 * k, max_springs=14 * nb + 1, max_halo=6 * nb + 4096,
+                    max_cilia=sum(s["n_cilia"] for s in specs) + 1,
+                    max_bonds=sum(s["n_cilia"] * s["rodlength"] for s in specs) + 1)
+        args.update(kw)
+        return cls(**args)
+
     def close(self):
         if getattr(self, "_h", None):
             lib().mpcd_batch_destroy(self._h)
@@ -489,8 +508,9 @@ class Batch:
     def autotune(self, trial_steps=50):
         t = MpcdBatchTuning()
         self._ck(lib().mpcd_batch_autotune(self._h, int(trial_steps), ctypes.byref(t)), "batch_autotune")
+        lanes, tile = self.md_layout()
         return dict(fluid_threads=t.fluid_threads, fluid_blocks=t.fluid_blocks, cell_threads=t.cell_threads,
-                    cell_blocks=t.cell_blocks, sort_interval=t.sort_interval)
+                    cell_blocks=t.cell_blocks, sort_interval=t.sort_interval, md_lanes=lanes, md_tile=tile)
 
     def tuning(self):
         t = MpcdBatchTuning()
@@ -507,3 +527,17 @@ class Batch:
 
     def launch_count(self):
         return lib().mpcd_batch_launch_count(self._h)
+
+    def set_md_layout(self, lanes, tile):
+        self._ck(lib().mpcd_batch_set_md_layout(self._h, int(lanes), int(tile)), "batch_set_md_layout")
+
+    def md_layout(self):
+        a, t = ctypes.c_int(), ctypes.c_int()
+        self._ck(lib().mpcd_batch_get_md_layout(self._h, ctypes.byref(a), ctypes.byref(t)), "batch_get_md_layout")
+        return a.value, t.value
+
+    def stage_times(self, nsteps=10):
+        """Device ms per step of (cell maps, fluid pass, MD, sorts), stages serialised."""
+        out = np.zeros(4)
+        self._ck(lib().mpcd_batch_stage_times(self._h, int(nsteps), _dp(out)), "batch_stage_times")
+        return dict(cell=out[0], fluid=out[1], md=out[2], sort=out[3])

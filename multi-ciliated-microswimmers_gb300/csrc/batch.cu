@@ -144,6 +144,7 @@ struct mpcd_batch {
   cudaEvent_t ev_fork = nullptr, ev_join[kMaxClusterTiles] = {};
   int T = 512, lanes = 2;
   long part_cap = 0, cell_cap = 0, tile_cap = 0;
+  long slot_cap = 0, tile_arr_cap = 0;  // MD slots; entries of the per-tile arrays (any layout)
   long npart_pages = 0, ncell_pages = 0;
   // device tables
   BatchRep* d_rep = nullptr;
@@ -378,7 +379,7 @@ int capture(mpcd_batch* b, int par, int nsteps, bool sorts, cudaGraphExec_t* out
     return rc;
   }
   if (e != cudaSuccess) return cuda_fail(b, e, "graph capture");
-  e = cudaGraphInstantiate(out, g, 0);
+  e = cudaGraphInstantiate(out, g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_fail(b, e, "graph instantiate");
   return MPCD_OK;
@@ -485,6 +486,137 @@ std::string plan_replica(mpcd_batch* b, Replica& R) {
   return "";
 }
 
+// uploads replica r's planned MD into its ranges of the shared arrays,
+// rebasing the plan's box-local slot, spring, halo, cilium and bond indices
+int upload_md(mpcd_batch* b, int r, Replica& R) {
+  const MDPlan& pl = R.plan;
+  MDState& m = b->md;
+  if (pl.ntiles > 0) {
+    const long sb = R.tile0 * (long)b->T;
+    const long ns = pl.nslots;
+    int rc;
+    if ((rc = put_range(b, m.x[0], sb, pl.X.data(), ns))) return rc;
+    if ((rc = put_range(b, m.y[0], sb, pl.Y.data(), ns))) return rc;
+    if ((rc = put_range(b, m.z[0], sb, pl.Z.data(), ns))) return rc;
+    if ((rc = put_range(b, m.vx, sb, pl.VX.data(), ns))) return rc;
+    if ((rc = put_range(b, m.vy, sb, pl.VY.data(), ns))) return rc;
+    if ((rc = put_range(b, m.vz, sb, pl.VZ.data(), ns))) return rc;
+    if ((rc = put_range(b, m.moves, sb, pl.mv.data(), ns))) return rc;
+    std::vector<int> v(ns + 1);
+    for (long k = 0; k < ns; ++k) v[k] = pl.prim[k] + (int)sb;
+    if ((rc = put_range(b, m.prim, sb, v.data(), ns))) return rc;
+    if ((rc = put_range(b, m.nhelp, sb, pl.nhelp.data(), ns))) return rc;
+    for (long k = 0; k <= ns; ++k) v[k] = pl.start[k] + (int)R.sp0;
+    if ((rc = put_range(b, m.sp_start, sb, v.data(), ns + 1))) return rc;
+    const long nt = pl.ntiles;
+    if ((rc = put_range(b, m.tile_help, R.tile0, pl.thelp.data(), nt))) return rc;
+    if ((rc = put_range(b, m.tile_react, R.tile0, pl.tile_react.data(), nt))) return rc;
+    std::vector<int> tv(nt + 1);
+    for (long t = 0; t <= nt; ++t) tv[t] = pl.hstart[t] + (int)std::max(R.h0, 0L);
+    if ((rc = put_range(b, m.halo_start, R.tile0, tv.data(), nt + 1))) return rc;
+    for (long t = 0; t <= nt; ++t) tv[t] = pl.tcil[t] + (int)std::max(R.c0, 0L);
+    if ((rc = put_range(b, m.tile_cil, R.tile0, tv.data(), nt + 1))) return rc;
+    if (R.nsp > 0) {
+      std::vector<int> so(R.nsp), sr(R.nsp);
+      for (long k = 0; k < R.nsp; ++k) {
+        so[k] = pl.so[k] + (int)sb;
+        sr[k] = (pl.sk[k] & 3) >= 2 ? pl.sr[k] + (int)R.b0 : pl.sr[k];
+      }
+      if ((rc = put_range(b, m.sp_other, R.sp0, so.data(), R.nsp))) return rc;
+      if ((rc = put_range(b, m.sp_local, R.sp0, pl.sl.data(), R.nsp))) return rc;
+      if ((rc = put_range(b, m.sp_kind, R.sp0, pl.sk.data(), R.nsp))) return rc;
+      if ((rc = put_range(b, m.sp_ref, R.sp0, sr.data(), R.nsp))) return rc;
+      if ((rc = put_range(b, m.sp_rest, R.sp0, pl.srest.data(), R.nsp))) return rc;
+      if ((rc = put_range(b, m.sp_m2k, R.sp0, pl.sm2k.data(), R.nsp))) return rc;
+    }
+    if (R.nh > 0) {
+      std::vector<int> hv(R.nh);
+      for (long k = 0; k < R.nh; ++k) hv[k] = pl.halo[k] + (int)sb;
+      if ((rc = put_range(b, m.halo, R.h0, hv.data(), R.nh))) return rc;
+    }
+    if (R.nc > 0) {
+      std::vector<CiliumDev> cd = pl.cd;
+      for (auto& c : cd) {
+        c.slot0 += (int)sb;
+        c.bond_base += (int)R.b0;
+      }
+      if ((rc = put_range(b, m.cil, R.c0, cd.data(), R.nc))) return rc;
+      if ((rc = put_range(b, m.midpnt, R.c0, pl.mid.data(), R.nc))) return rc;
+      if ((rc = put_range(b, m.tstroke, R.c0, pl.ts.data(), R.nc))) return rc;
+    }
+    if (R.nbond > 0) {
+      if ((rc = put_range(b, m.newlen, R.b0, pl.newlen.data(), R.nbond))) return rc;
+      if ((rc = put_range(b, m.oldlen, R.b0, pl.oldlen.data(), R.nbond))) return rc;
+      if ((rc = put_range(b, m.diag, R.b0, pl.diag.data(), R.nbond))) return rc;
+    }
+    for (long t = 0; t < nt; ++t) b->tile_rep[R.tile0 + t] = r;
+    b->tile_rep[R.tile0 + nt] = -1;  // spare tile
+    if ((rc = put_range(b, b->d_tile_rep, R.tile0, b->tile_rep.data() + R.tile0, nt + 1))) return rc;
+  }
+  return MPCD_OK;
+}
+
+// copies replica r's bead state, beat state and bond tables from the device
+// into its host description (R.bpos, R.bvel, R.cil, R.newlen, R.oldlen)
+int pull_md_state(mpcd_batch* b, Replica& R) {
+  const MDPlan& pl = R.plan;
+  if (R.nb == 0 || pl.ntiles == 0) return MPCD_OK;
+  const long sb = R.tile0 * (long)b->T, ns = pl.nslots;
+  std::vector<double> X(ns), Y(ns), Z(ns), VX(ns), VY(ns), VZ(ns);
+  const MDState& m = b->md;
+  BK(cudaMemcpyAsync(X.data(), m.x[0] + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
+  BK(cudaMemcpyAsync(Y.data(), m.y[0] + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
+  BK(cudaMemcpyAsync(Z.data(), m.z[0] + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
+  BK(cudaMemcpyAsync(VX.data(), m.vx + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
+  BK(cudaMemcpyAsync(VY.data(), m.vy + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
+  BK(cudaMemcpyAsync(VZ.data(), m.vz + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
+  std::vector<double> mid(R.nc), ts(R.nc);
+  if (R.nc > 0) {
+    BK(cudaMemcpyAsync(mid.data(), m.midpnt + R.c0, R.nc * 8, cudaMemcpyDeviceToHost, b->s0));
+    BK(cudaMemcpyAsync(ts.data(), m.tstroke + R.c0, R.nc * 8, cudaMemcpyDeviceToHost, b->s0));
+  }
+  if (R.nbond > 0) {
+    BK(cudaMemcpyAsync(R.newlen.data(), m.newlen + R.b0, R.nbond * 8, cudaMemcpyDeviceToHost, b->s0));
+    BK(cudaMemcpyAsync(R.oldlen.data(), m.oldlen + R.b0, R.nbond * 8, cudaMemcpyDeviceToHost, b->s0));
+  }
+  BK(cudaStreamSynchronize(b->s0));
+  for (long k = 0; k < R.nb; ++k) {
+    const int sl = pl.slot_of[k];
+    R.bpos[3 * k] = X[sl];
+    R.bpos[3 * k + 1] = Y[sl];
+    R.bpos[3 * k + 2] = Z[sl];
+    R.bvel[3 * k] = VX[sl];
+    R.bvel[3 * k + 1] = VY[sl];
+    R.bvel[3 * k + 2] = VZ[sl];
+  }
+  for (long c = 0; c < R.nc; ++c) {
+    R.cil[c].midpnt = mid[c];
+    R.cil[c].tstroke = ts[c];
+  }
+  return MPCD_OK;
+}
+
+// takes the MD ranges of a planned replica (all or nothing)
+bool take_md_ranges(mpcd_batch* b, Replica& R) {
+  const MDPlan& pl = R.plan;
+  R.ntiles_alloc = pl.ntiles > 0 ? pl.ntiles + 1 : 0;
+  R.nsp = pl.nsp_kept();
+  R.nh = (long)pl.halo.size();
+  R.nc = (long)pl.cd.size();
+  R.nbond = (long)pl.newlen.size();
+  bool ok = true;
+  auto take = [&](RangeAlloc& a, long n, long& off) {
+    off = n > 0 ? a.alloc(n) : -1;
+    if (n > 0 && off < 0) ok = false;
+  };
+  take(b->a_tile, R.ntiles_alloc, R.tile0);
+  take(b->a_sp, R.nsp, R.sp0);
+  take(b->a_halo, R.nh, R.h0);
+  take(b->a_cil, R.nc, R.c0);
+  take(b->a_bond, R.nbond, R.b0);
+  return ok;
+}
+
 }  // namespace
 
 extern "C" {
@@ -517,8 +649,12 @@ int mpcd_batch_create(const mpcd_batch_params* params, mpcd_batch** out) {
   cudaError_t e;
   if ((e = cudaSetDevice(p.device)) != cudaSuccess) return bail(e, "cudaSetDevice");
   if ((e = cudaStreamCreateWithFlags(&b->s0, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
   for (int g = 0; g < kMaxClusterTiles; ++g) {
-    if ((e = cudaStreamCreateWithFlags(&b->smd[g], cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+    // the MD chains are latency-bound: their CTAs take SMs before the fluid pass's
+    if ((e = cudaStreamCreateWithPriority(&b->smd[g], cudaStreamNonBlocking, prio_greatest)) != cudaSuccess)
+      return bail(e, "stream");
     if ((e = cudaEventCreateWithFlags(&b->ev_join[g], cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
   }
   if ((e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
@@ -526,8 +662,11 @@ int mpcd_batch_create(const mpcd_batch_params* params, mpcd_batch** out) {
   b->ncell_pages = (p.max_cells + kCellPage - 1) / kCellPage;
   b->part_cap = b->npart_pages * kPartPage;
   b->cell_cap = b->ncell_pages * kCellPage;
-  b->tile_cap = (p.max_slots + b->T - 1) / b->T + p.max_replicas;  // one spare tile per replica
-  const long nslots = b->tile_cap * b->T;
+  // slots for the beads plus one spare tile per replica (for the smallest tile size)
+  const long nslots = ((p.max_slots + 31) / 32 + 32L * p.max_replicas) * 32L;
+  b->slot_cap = nslots;
+  b->tile_cap = nslots / b->T;
+  b->tile_arr_cap = nslots / 32 + 1;
   const int R = p.max_replicas;
   if ((e = dalloc(&b->d_rep, R)) != cudaSuccess) return bail(e, "alloc tables");
   if ((e = dalloc(&b->d_step, R)) != cudaSuccess) return bail(e, "alloc tables");
@@ -536,7 +675,7 @@ int mpcd_batch_create(const mpcd_batch_params* params, mpcd_batch** out) {
   if ((e = dalloc(&b->d_md_reps, R)) != cudaSuccess) return bail(e, "alloc tables");
   if ((e = dalloc(&b->d_part_page_rep, b->npart_pages)) != cudaSuccess) return bail(e, "alloc tables");
   if ((e = dalloc(&b->d_cell_page_rep, b->ncell_pages)) != cudaSuccess) return bail(e, "alloc tables");
-  if ((e = dalloc(&b->d_tile_rep, b->tile_cap)) != cudaSuccess) return bail(e, "alloc tables");
+  if ((e = dalloc(&b->d_tile_rep, b->tile_arr_cap)) != cudaSuccess) return bail(e, "alloc tables");
   for (int par = 0; par < 2; ++par) {
     if ((e = dalloc(&b->fl[par].id, b->part_cap)) != cudaSuccess) return bail(e, "alloc fluid");
     if ((e = dalloc(&b->fl[par].pos, b->part_cap)) != cudaSuccess) return bail(e, "alloc fluid");
@@ -569,10 +708,10 @@ int mpcd_batch_create(const mpcd_batch_params* params, mpcd_batch** out) {
   if ((e = dalloc(&m.prim, nslots)) != cudaSuccess) return bail(e, "alloc MD");
   if ((e = dalloc(&m.nhelp, nslots)) != cudaSuccess) return bail(e, "alloc MD");
   if ((e = dalloc(&m.sp_start, nslots + 1)) != cudaSuccess) return bail(e, "alloc MD");
-  if ((e = dalloc(&m.tile_help, b->tile_cap)) != cudaSuccess) return bail(e, "alloc MD");
-  if ((e = dalloc(&m.tile_react, b->tile_cap)) != cudaSuccess) return bail(e, "alloc MD");
-  if ((e = dalloc(&m.tile_cil, b->tile_cap + 1)) != cudaSuccess) return bail(e, "alloc MD");
-  if ((e = dalloc(&m.halo_start, b->tile_cap + 1)) != cudaSuccess) return bail(e, "alloc MD");
+  if ((e = dalloc(&m.tile_help, b->tile_arr_cap)) != cudaSuccess) return bail(e, "alloc MD");
+  if ((e = dalloc(&m.tile_react, b->tile_arr_cap)) != cudaSuccess) return bail(e, "alloc MD");
+  if ((e = dalloc(&m.tile_cil, b->tile_arr_cap + 1)) != cudaSuccess) return bail(e, "alloc MD");
+  if ((e = dalloc(&m.halo_start, b->tile_arr_cap + 1)) != cudaSuccess) return bail(e, "alloc MD");
   if ((e = dalloc(&m.sp_other, p.max_springs)) != cudaSuccess) return bail(e, "alloc MD");
   if ((e = dalloc(&m.sp_local, p.max_springs)) != cudaSuccess) return bail(e, "alloc MD");
   if ((e = dalloc(&m.sp_kind, p.max_springs)) != cudaSuccess) return bail(e, "alloc MD");
@@ -591,14 +730,14 @@ int mpcd_batch_create(const mpcd_batch_params* params, mpcd_batch** out) {
   b->rep.assign(R, BatchRep{});
   b->part_page_rep.assign(b->npart_pages, -1);
   b->cell_page_rep.assign(b->ncell_pages, -1);
-  b->tile_rep.assign(b->tile_cap, -1);
+  b->tile_rep.assign(b->tile_arr_cap, -1);
   b->reps.assign(R, Replica{});
   {
     std::vector<int> neg(nslots, -1);
     if ((e = cudaMemcpy(m.moves, neg.data(), nslots * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
       return bail(e, "init MD");
   }
-  if ((e = cudaMemset(m.tile_help, 0, b->tile_cap * sizeof(int))) != cudaSuccess) return bail(e, "init MD");
+  if ((e = cudaMemset(m.tile_help, 0, b->tile_arr_cap * sizeof(int))) != cudaSuccess) return bail(e, "init MD");
   if ((e = cudaMemset(b->cells.sum, 0, b->cell_cap * sizeof(float4))) != cudaSuccess) return bail(e, "init cells");
   if ((e = cudaMemset(b->cells.cnt, 0, b->cell_cap * sizeof(uint32_t))) != cudaSuccess) return bail(e, "init cells");
   if ((e = cudaMemset(b->d_state, 0, R * sizeof(BatchState))) != cudaSuccess) return bail(e, "init tables");
@@ -611,7 +750,7 @@ int mpcd_batch_create(const mpcd_batch_params* params, mpcd_batch** out) {
   if ((e = cudaMemcpy(b->d_cell_page_rep, b->cell_page_rep.data(), b->ncell_pages * sizeof(int),
                       cudaMemcpyHostToDevice)) != cudaSuccess)
     return bail(e, "init tables");
-  if ((e = cudaMemcpy(b->d_tile_rep, b->tile_rep.data(), b->tile_cap * sizeof(int), cudaMemcpyHostToDevice)) !=
+  if ((e = cudaMemcpy(b->d_tile_rep, b->tile_rep.data(), b->tile_arr_cap * sizeof(int), cudaMemcpyHostToDevice)) !=
       cudaSuccess)
     return bail(e, "init tables");
   b->a_part.reset(b->npart_pages);
@@ -809,11 +948,6 @@ int mpcd_batch_admit(mpcd_batch* b, int r) {
   // device ranges
   R.npages = (R.nf + kPartPage - 1) / kPartPage;
   R.ncpages = (R.ncell + kCellPage - 1) / kCellPage;
-  R.ntiles_alloc = pl.ntiles > 0 ? pl.ntiles + 1 : 0;
-  R.nsp = pl.nsp_kept();
-  R.nh = (long)pl.halo.size();
-  R.nc = (long)pl.cd.size();
-  R.nbond = (long)pl.newlen.size();
   bool ok = true;
   auto take = [&](RangeAlloc& a, long n, long& off) {
     off = n > 0 ? a.alloc(n) : -1;
@@ -821,11 +955,7 @@ int mpcd_batch_admit(mpcd_batch* b, int r) {
   };
   take(b->a_part, R.npages, R.page0);
   take(b->a_cell, R.ncpages, R.cpage0);
-  take(b->a_tile, R.ntiles_alloc, R.tile0);
-  take(b->a_sp, R.nsp, R.sp0);
-  take(b->a_halo, R.nh, R.h0);
-  take(b->a_cil, R.nc, R.c0);
-  take(b->a_bond, R.nbond, R.b0);
+  ok = take_md_ranges(b, R) && ok;
   if (!ok) {
     release_ranges(b, R);
     return fail(b, MPCD_EINVAL, "admit: batch capacity exhausted");
@@ -873,69 +1003,11 @@ int mpcd_batch_admit(mpcd_batch* b, int r) {
   BK(cudaMemsetAsync(b->cells.sum + cell0, 0, R.ncpages * kCellPage * sizeof(float4), b->s0));
   BK(cudaMemsetAsync(b->cells.cnt + cell0, 0, R.ncpages * kCellPage * sizeof(uint32_t), b->s0));
   // MD, rebased into the shared arrays
-  MDState& m = b->md;
-  if (pl.ntiles > 0) {
-    const long sb = R.tile0 * (long)b->T;
-    const long ns = pl.nslots;
-    int rc;
-    if ((rc = put_range(b, m.x[0], sb, pl.X.data(), ns))) return rc;
-    if ((rc = put_range(b, m.y[0], sb, pl.Y.data(), ns))) return rc;
-    if ((rc = put_range(b, m.z[0], sb, pl.Z.data(), ns))) return rc;
-    if ((rc = put_range(b, m.vx, sb, pl.VX.data(), ns))) return rc;
-    if ((rc = put_range(b, m.vy, sb, pl.VY.data(), ns))) return rc;
-    if ((rc = put_range(b, m.vz, sb, pl.VZ.data(), ns))) return rc;
-    if ((rc = put_range(b, m.moves, sb, pl.mv.data(), ns))) return rc;
-    std::vector<int> v(ns + 1);
-    for (long k = 0; k < ns; ++k) v[k] = pl.prim[k] + (int)sb;
-    if ((rc = put_range(b, m.prim, sb, v.data(), ns))) return rc;
-    if ((rc = put_range(b, m.nhelp, sb, pl.nhelp.data(), ns))) return rc;
-    for (long k = 0; k <= ns; ++k) v[k] = pl.start[k] + (int)R.sp0;
-    if ((rc = put_range(b, m.sp_start, sb, v.data(), ns + 1))) return rc;
-    const long nt = pl.ntiles;
-    if ((rc = put_range(b, m.tile_help, R.tile0, pl.thelp.data(), nt))) return rc;
-    if ((rc = put_range(b, m.tile_react, R.tile0, pl.tile_react.data(), nt))) return rc;
-    std::vector<int> tv(nt + 1);
-    for (long t = 0; t <= nt; ++t) tv[t] = pl.hstart[t] + (int)std::max(R.h0, 0L);
-    if ((rc = put_range(b, m.halo_start, R.tile0, tv.data(), nt + 1))) return rc;
-    for (long t = 0; t <= nt; ++t) tv[t] = pl.tcil[t] + (int)std::max(R.c0, 0L);
-    if ((rc = put_range(b, m.tile_cil, R.tile0, tv.data(), nt + 1))) return rc;
-    if (R.nsp > 0) {
-      std::vector<int> so(R.nsp), sr(R.nsp);
-      for (long k = 0; k < R.nsp; ++k) {
-        so[k] = pl.so[k] + (int)sb;
-        sr[k] = (pl.sk[k] & 3) >= 2 ? pl.sr[k] + (int)R.b0 : pl.sr[k];
-      }
-      if ((rc = put_range(b, m.sp_other, R.sp0, so.data(), R.nsp))) return rc;
-      if ((rc = put_range(b, m.sp_local, R.sp0, pl.sl.data(), R.nsp))) return rc;
-      if ((rc = put_range(b, m.sp_kind, R.sp0, pl.sk.data(), R.nsp))) return rc;
-      if ((rc = put_range(b, m.sp_ref, R.sp0, sr.data(), R.nsp))) return rc;
-      if ((rc = put_range(b, m.sp_rest, R.sp0, pl.srest.data(), R.nsp))) return rc;
-      if ((rc = put_range(b, m.sp_m2k, R.sp0, pl.sm2k.data(), R.nsp))) return rc;
-    }
-    if (R.nh > 0) {
-      std::vector<int> hv(R.nh);
-      for (long k = 0; k < R.nh; ++k) hv[k] = pl.halo[k] + (int)sb;
-      if ((rc = put_range(b, m.halo, R.h0, hv.data(), R.nh))) return rc;
-    }
-    if (R.nc > 0) {
-      std::vector<CiliumDev> cd = pl.cd;
-      for (auto& c : cd) {
-        c.slot0 += (int)sb;
-        c.bond_base += (int)R.b0;
-      }
-      if ((rc = put_range(b, m.cil, R.c0, cd.data(), R.nc))) return rc;
-      if ((rc = put_range(b, m.midpnt, R.c0, pl.mid.data(), R.nc))) return rc;
-      if ((rc = put_range(b, m.tstroke, R.c0, pl.ts.data(), R.nc))) return rc;
-    }
-    if (R.nbond > 0) {
-      if ((rc = put_range(b, m.newlen, R.b0, pl.newlen.data(), R.nbond))) return rc;
-      if ((rc = put_range(b, m.oldlen, R.b0, pl.oldlen.data(), R.nbond))) return rc;
-      if ((rc = put_range(b, m.diag, R.b0, pl.diag.data(), R.nbond))) return rc;
-    }
-    for (long t = 0; t < nt; ++t) b->tile_rep[R.tile0 + t] = r;
-    b->tile_rep[R.tile0 + nt] = -1;  // spare tile
-    if ((rc = put_range(b, b->d_tile_rep, R.tile0, b->tile_rep.data() + R.tile0, nt + 1))) return rc;
+  {
+    const int rc = upload_md(b, r, R);
+    if (rc) return rc;
   }
+  MDState& m = b->md;
   // tables
   BatchRep& D = b->rep[r];
   D = BatchRep{};
@@ -1084,30 +1156,10 @@ int mpcd_batch_get_beads(mpcd_batch* b, int r, long nb, double* pos, double* vel
   Replica* R = get_rep(b, r);
   if (!R || !R->admitted || nb != R->nb) return fail(b, MPCD_EINVAL, "get_beads: bad replica or size");
   if (nb == 0) return MPCD_OK;
-  const MDPlan& pl = R->plan;
-  const long sb = R->tile0 * (long)b->T, ns = pl.nslots;
-  std::vector<double> X(ns), Y(ns), Z(ns), VX(ns), VY(ns), VZ(ns);
-  const MDState& m = b->md;
-  BK(cudaMemcpyAsync(X.data(), m.x[0] + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
-  BK(cudaMemcpyAsync(Y.data(), m.y[0] + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
-  BK(cudaMemcpyAsync(Z.data(), m.z[0] + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
-  BK(cudaMemcpyAsync(VX.data(), m.vx + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
-  BK(cudaMemcpyAsync(VY.data(), m.vy + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
-  BK(cudaMemcpyAsync(VZ.data(), m.vz + sb, ns * 8, cudaMemcpyDeviceToHost, b->s0));
-  BK(cudaStreamSynchronize(b->s0));
-  for (long k = 0; k < nb; ++k) {
-    const int s = pl.slot_of[k];
-    if (pos) {
-      pos[3 * k] = X[s];
-      pos[3 * k + 1] = Y[s];
-      pos[3 * k + 2] = Z[s];
-    }
-    if (vel) {
-      vel[3 * k] = VX[s];
-      vel[3 * k + 1] = VY[s];
-      vel[3 * k + 2] = VZ[s];
-    }
-  }
+  int rc = pull_md_state(b, *R);
+  if (rc) return rc;
+  if (pos) std::memcpy(pos, R->bpos.data(), 3 * nb * sizeof(double));
+  if (vel) std::memcpy(vel, R->bvel.data(), 3 * nb * sizeof(double));
   return MPCD_OK;
 }
 
@@ -1137,6 +1189,7 @@ int mpcd_batch_observables(mpcd_batch* b, int r, mpcd_obs* out) {
     std::string msg = "device check failed for this replica:";
     if (S.err & kErrGammaLoop) msg += " Gamma sampler exceeded its iteration cap;";
     if (S.err & kErrCellRange) msg += " non-finite or out-of-range coordinate (unstable MD step?);";
+    if (S.err & kErrLayout) msg += " MD shared-memory layout mismatch;";
     return fail(b, MPCD_EDEVICE, msg);
   }
   return MPCD_OK;
@@ -1223,6 +1276,24 @@ int mpcd_batch_autotune(mpcd_batch* b, int trial_steps, mpcd_batch_tuning* chose
   };
   mpcd_batch_tuning best = b->tune;
   double best_ms = 1e30;
+  // MD layout (threads per slot, slots per CTA): every swimmer is re-planned
+  {
+    int best_lanes = b->lanes, best_tile = b->T;
+    const int layouts[][2] = {{2, 256}, {1, 512}, {2, 128}, {1, 256}, {1, 1024}, {2, 512}};
+    for (auto& lt : layouts) {
+      if (mpcd_batch_set_md_layout(b, lt[0], lt[1]) != MPCD_OK) continue;  // does not fit: skip
+      double ms;
+      int rc = trial(best, &ms);
+      if (rc) return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_lanes = lt[0];
+        best_tile = lt[1];
+      }
+    }
+    int rc = mpcd_batch_set_md_layout(b, best_lanes, best_tile);
+    if (rc) return rc;
+  }
   // fluid pass: threads per block and grid (persistent multiples of the SM count, or one block per page)
   const int threads[] = {256, 512};
   const long grids[] = {0, 4L * sms, 16L * sms, b->npart_pages};
@@ -1266,6 +1337,135 @@ int mpcd_batch_autotune(mpcd_batch* b, int trial_steps, mpcd_batch_tuning* chose
   int rc = mpcd_batch_set_tuning(b, &best);
   if (rc) return rc;
   if (chosen) *chosen = best;
+  return MPCD_OK;
+}
+
+int mpcd_batch_stage_times(mpcd_batch* b, int nsteps, double* out4) {
+  if (!b || nsteps < 1 || !out4) return fail(b, MPCD_EINVAL, "stage_times: bad arguments");
+  int rc = rebuild_graphs(b);  // MD launch plan
+  if (rc) return rc;
+  const BatchTables t = tables(b);
+  std::vector<cudaEvent_t> ev(5 * (size_t)nsteps);
+  for (auto& e : ev) BK(cudaEventCreate(&e));
+  double acc[4] = {0, 0, 0, 0};
+  for (int k = 0; k < nsteps; ++k) {
+    cudaEvent_t* E = &ev[5 * (size_t)k];
+    BK(cudaEventRecord(E[0], b->s0));
+    b->launches_total += launch_batch_prologue(t, b->s0);
+    b->launches_total += launch_batch_cell_params(t, b->cells, b->tune.cell_threads, b->tune.cell_blocks, b->s0);
+    BK(cudaEventRecord(E[1], b->s0));
+    b->launches_total +=
+        launch_batch_fluid_step(t, b->fl[b->cur], b->cells, b->tune.fluid_threads, b->tune.fluid_blocks, b->s0);
+    BK(cudaEventRecord(E[2], b->s0));
+    for (const MDLaunch& L : b->launches) {
+      cudaError_t st = cudaSuccess;
+      b->launches_total += launch_md_cluster_batch(b->md, t, b->cells, b->d_md_reps + L.offset, L.count, L.ctiles,
+                                                   L.hmax, L.nsp_max, L.nbond_max, b->s0, &st);
+      if (st != cudaSuccess) return cuda_fail(b, st, "batch MD launch");
+    }
+    BK(cudaEventRecord(E[3], b->s0));
+    if (++b->since_sort >= b->tune.sort_interval) {
+      enqueue_sort(b, b->cur);
+      b->launches_total += b->kernels_per_sort;
+      b->cur ^= 1;
+      b->since_sort = 0;
+    }
+    BK(cudaEventRecord(E[4], b->s0));
+  }
+  BK(cudaStreamSynchronize(b->s0));
+  for (int k = 0; k < nsteps; ++k) {
+    cudaEvent_t* E = &ev[5 * (size_t)k];
+    for (int j = 0; j < 4; ++j) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, E[j], E[j + 1]);
+      acc[j] += ms;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int j = 0; j < 4; ++j) out4[j] = acc[j] / nsteps;
+  BK(cudaGetLastError());
+  return MPCD_OK;
+}
+
+int mpcd_batch_set_md_layout(mpcd_batch* b, int lanes, int tile) {
+  if (!b) return MPCD_EINVAL;
+  if (lanes == 0) lanes = 2;
+  if (tile == 0) tile = 512 / lanes;
+  if ((lanes != 1 && lanes != 2) || tile < 32 || tile % 32 || tile * lanes > 1024)
+    return fail(b, MPCD_EINVAL, "set_md_layout: invalid layout");
+  if (lanes == b->lanes && tile == b->T) return MPCD_OK;
+  BK(cudaStreamSynchronize(b->s0));
+  // current bead and beat state back to the host descriptions
+  for (auto& R : b->reps)
+    if (R.admitted && R.nb > 0) {
+      int rc = pull_md_state(b, R);
+      if (rc) return rc;
+    }
+  // plan every swimmer with the new layout: nothing changes on the device on failure
+  const int oldT = b->T, oldL = b->lanes;
+  b->T = tile;
+  b->lanes = lanes;
+  std::vector<MDPlan> plans(b->reps.size());
+  long tiles_needed = 0;
+  for (size_t r = 0; r < b->reps.size(); ++r) {
+    Replica& R = b->reps[r];
+    if (!R.admitted || R.nb == 0) continue;
+    MDPlan keep;
+    keep = std::move(R.plan);
+    std::string why = plan_replica(b, R);
+    plans[r] = std::move(R.plan);
+    R.plan = std::move(keep);
+    tiles_needed += plans[r].ntiles + 1;
+    if (!why.empty()) {
+      b->T = oldT;
+      b->lanes = oldL;
+      return fail(b, MPCD_EINVAL, "set_md_layout: " + why);
+    }
+  }
+  if (tiles_needed > b->slot_cap / tile) {
+    b->T = oldT;
+    b->lanes = oldL;
+    return fail(b, MPCD_EINVAL, "set_md_layout: the MD slot capacity does not hold the new layout");
+  }
+  // clear every MD range and table
+  b->tile_cap = b->slot_cap / tile;
+  b->a_tile.reset(b->tile_cap);
+  b->a_sp.reset(b->p.max_springs);
+  b->a_halo.reset(b->p.max_halo);
+  b->a_cil.reset(b->p.max_cilia);
+  b->a_bond.reset(b->p.max_bonds);
+  MDState& m = b->md;
+  m.tile = tile;
+  m.cl_lanes = lanes;
+  m.ntiles = (int)b->tile_cap;
+  {
+    std::vector<int> neg(b->slot_cap, -1);
+    BK(cudaMemcpy(m.moves, neg.data(), b->slot_cap * sizeof(int), cudaMemcpyHostToDevice));
+    std::fill(b->tile_rep.begin(), b->tile_rep.end(), -1);
+    BK(cudaMemcpy(b->d_tile_rep, b->tile_rep.data(), b->tile_arr_cap * sizeof(int), cudaMemcpyHostToDevice));
+    BK(cudaMemset(m.tile_help, 0, b->tile_arr_cap * sizeof(int)));
+  }
+  for (size_t r = 0; r < b->reps.size(); ++r) {
+    Replica& R = b->reps[r];
+    if (!R.admitted || R.nb == 0) continue;
+    R.tile0 = R.sp0 = R.h0 = R.c0 = R.b0 = -1;
+    R.plan = std::move(plans[r]);
+    if (!take_md_ranges(b, R)) return fail(b, MPCD_EINVAL, "set_md_layout: MD capacity exhausted (batch unusable)");
+    int rc = upload_md(b, (int)r, R);
+    if (rc) return rc;
+    b->rep[r].md_tile0 = (int)R.tile0;
+    b->rep[r].md_ntiles = R.plan.ntiles;
+    if ((rc = put_range(b, b->d_rep, (long)r, &b->rep[r], 1))) return rc;
+  }
+  BK(cudaStreamSynchronize(b->s0));
+  b->graphs_dirty = true;
+  return MPCD_OK;
+}
+
+int mpcd_batch_get_md_layout(const mpcd_batch* b, int* lanes, int* tile) {
+  if (!b) return MPCD_EINVAL;
+  if (lanes) *lanes = b->lanes;
+  if (tile) *tile = b->T;
   return MPCD_OK;
 }
 

@@ -411,6 +411,7 @@ int device_error(mpcd_engine* h) {
   if (e & kErrBarrier) msg += " MD grid barrier timed out;";
   if (e & kErrCellRange) msg += " non-finite or out-of-range coordinate (unstable MD step?);";
   if (e & kErrCellOverflow) msg += " cell occupancy overflow;";
+  if (e & kErrLayout) msg += " MD shared-memory layout mismatch;";
   cudaMemset(h->d_err, 0, sizeof(unsigned));
   return fail(h, MPCD_EDEVICE, msg);
 }

@@ -26,12 +26,13 @@ namespace mpcd {
 namespace {
 
 
-// Cilia::length(i) (src/cilia.cpp:79-121) in float arithmetic
-__device__ float cl_cilium_length(const CiliumDev& cl, int i, float midpnt, float oldlen, float tl) {
-  const float bondlength = 0.5f, beat = (float)cl.beatstrength, bend = (float)cl.bending;
+// Cilia::length(i) (src/cilia.cpp:79-121) in float arithmetic; cp = (num_anker,
+// rodlength, beatstrength, bending) of the cilium
+__device__ float cl_cilium_length(const float4 cp, int i, float midpnt, float oldlen, float tl) {
+  const float bondlength = 0.5f, beat = cp.z, bend = cp.w;
   float l;
   if ((float)i < midpnt - 2.0f) {
-    const float base = 1.0f - ((float)i - cl.num_anker - 1.0f) / (float)(cl.len - cl.num_anker - 1);
+    const float base = 1.0f - ((float)i - cp.x - 1.0f) / (cp.y - cp.x - 1.0f);
     l = bondlength + beat * (base * base * sqrtf(base)) * 0.5f * (1.0f - 1.0f / (midpnt - (float)i - 1.0f));
   } else {
     const float di = (float)i - midpnt;
@@ -66,12 +67,20 @@ struct PBuf {
   }
 };
 
+// Shared memory of one CTA.  nsp_max counts spring entries in the warp-sliced
+// layout (entry k of thread t of warp w at wbase[w] + 32 k + t, every warp
+// padded to its longest list), so that a warp's loads of its k-th springs
+// are consecutive words (no bank conflicts).
 struct ClusterLayout {
   int np, nsp_max, nbond_max;
+  __host__ __device__ int max_cilia() const { return nbond_max / 2 + 1; }
   __host__ __device__ size_t bytes(int T) const {
     size_t b = 2 * 6 * sizeof(float) * (size_t)np;           // two position buffers
     b += (size_t)nsp_max * (sizeof(uint32_t) + 2 * sizeof(float));  // springs
     b += (size_t)nbond_max * 3 * sizeof(float);                      // bond tables
+    b = (b + 15) & ~(size_t)15;
+    b += (size_t)nbond_max * sizeof(int4);                      // refresh entries
+    b += (size_t)max_cilia() * (sizeof(float4) + sizeof(float));  // cilium parameters, midpoints
     b = (b + 15) & ~(size_t)15;
     b += 3 * sizeof(float) * (size_t)T;                         // helper partial forces
     return b;
@@ -102,40 +111,82 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
   float* bnew = reinterpret_cast<float*>(ptr);
   float* bold = bnew + lay.nbond_max;
   float* bdiag = bold + lay.nbond_max;
-  ptr = reinterpret_cast<unsigned char*>(bdiag + lay.nbond_max);
+  ptr = reinterpret_cast<unsigned char*>(((uintptr_t)(bdiag + lay.nbond_max) + 15) & ~(uintptr_t)15);
+  int4* rf = reinterpret_cast<int4*>(ptr);  // per bond: (slot i, slot i+1, position i, cilium), x < 0 unused
+  float4* cpar = reinterpret_cast<float4*>(rf + lay.nbond_max);
+  float* cmid = reinterpret_cast<float*>(cpar + lay.max_cilia());
+  ptr = reinterpret_cast<unsigned char*>(cmid + lay.max_cilia());
   float* part = reinterpret_cast<float*>(((uintptr_t)ptr + 15) & ~(uintptr_t)15);
 
   // per-tile constants
-  const int sp0 = m.sp_start[base], sp1 = m.sp_start[base + T];
   const int c0 = m.tile_cil[tile], c1 = m.tile_cil[tile + 1];
   const int bond0 = c1 > c0 ? m.cil[c0].bond_base : 0;
   const int nbond = c1 > c0 ? m.cil[c1 - 1].bond_base + m.cil[c1 - 1].len - bond0 : 0;
   const int h0 = m.halo_start[tile], hn = m.halo_start[tile + 1] - h0;
-  // stage springs and bond tables
-  for (int s = sp0 + (int)threadIdx.x; s < sp1; s += blockDim.x) {
-    const int k = s - sp0;
-    const int kraw = m.sp_kind[s];
-    const int kind = kraw & 3;
-    // bond-table index for BOND/DIAG springs; bit 13 marks a reaction owed to a hub
-    const int bl = kind >= 2 ? m.sp_ref[s] - bond0 : ((kraw & kSpringReact) ? 0x2000 : 0);
-    sw[k] = (uint32_t)m.sp_local[s] | ((uint32_t)bl << 16) | ((uint32_t)kind << 30);
-    srest[k] = (float)m.sp_rest[s];
-    sm2k[k] = (float)m.sp_m2k[s];
+  const int q = threadIdx.x / kCLanes, lane = threadIdx.x % kCLanes;  // kCLanes lanes per slot
+  const int slot = base + q;
+  const bool valid = q < T;
+  // stage this thread's springs (CSR entries s0 + lane + kCLanes k of its
+  // slot) into the warp-sliced layout
+  int nmine = 0, ebase = 0;
+  {
+    __shared__ int wbase[33];
+    const int gs0 = valid ? m.sp_start[slot] : 0, gs1 = valid ? m.sp_start[slot + 1] : 0;
+    nmine = max(0, (gs1 - gs0 - lane + kCLanes - 1) / kCLanes);
+    const int wid = (int)(threadIdx.x >> 5), lid = (int)(threadIdx.x & 31);
+    const int W = __reduce_max_sync(0xffffffffu, nmine);
+    if (lid == 0) wbase[wid] = 32 * W;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      const int nw = (int)(blockDim.x >> 5);
+      for (int w = 0; w < nw; ++w) {
+        const int t = wbase[w];
+        wbase[w] = acc;
+        acc += t;
+      }
+      wbase[nw] = acc;
+    }
+    __syncthreads();
+    if (wbase[blockDim.x >> 5] > lay.nsp_max) {  // layout mismatch: no springs, and say so
+      if (threadIdx.x == 0) atomicOr(a.err, kErrLayout);
+      nmine = 0;
+    }
+    ebase = wbase[wid] + lid;
+    for (int k = 0; k < nmine; ++k) {
+      const int s = gs0 + lane + kCLanes * k;
+      const int e = ebase + 32 * k;
+      const int kraw = m.sp_kind[s];
+      const int kind = kraw & 3;
+      // bond-table index for BOND/DIAG springs; bit 13 marks a reaction owed to a hub
+      const int bl = kind >= 2 ? m.sp_ref[s] - bond0 : ((kraw & kSpringReact) ? 0x2000 : 0);
+      sw[e] = (uint32_t)m.sp_local[s] | ((uint32_t)bl << 16) | ((uint32_t)kind << 30);
+      srest[e] = (float)m.sp_rest[s];
+      sm2k[e] = (float)m.sp_m2k[s];
+    }
   }
   for (int k = threadIdx.x; k < nbond; k += blockDim.x) {
     bnew[k] = (float)m.newlen[bond0 + k];
     bold[k] = (float)m.oldlen[bond0 + k];
     bdiag[k] = (float)m.diag[bond0 + k];
+    rf[k] = make_int4(-1, 0, 0, 0);
   }
-  const int q = threadIdx.x / kCLanes, lane = threadIdx.x % kCLanes;  // kCLanes lanes per slot
-  const int slot = base + q;
-  const bool valid = q < T;
+  __syncthreads();
+  // refresh entries: the driven bonds num_anker-1 .. rodlength-2 of every cilium
+  for (int c = c0 + (int)threadIdx.x; c < c1; c += (int)blockDim.x) {
+    const CiliumDev cl = m.cil[c];
+    const int cc = c - c0;
+    cpar[cc] = make_float4((float)cl.num_anker, (float)cl.len, (float)cl.beatstrength, (float)cl.bending);
+    cmid[cc] = (float)m.midpnt[c];
+    const int l0 = cl.slot0 - base, sd = cl.stride;
+    for (int i = cl.num_anker - 1; i <= cl.len - 2; ++i)
+      rf[cl.bond_base - bond0 + i] = make_int4(l0 + sd * i, l0 + sd * (i + 1), i, cc);
+  }
   const int mv = valid ? m.moves[slot] : -1;
   const bool moves = mv == 1;
   const bool primary = mv == 0 || mv == 1;
   const int me = valid && mv >= 0 ? m.prim[slot] - base : 0;
   const int nh = primary ? m.nhelp[slot] : 0;
-  const int s0 = valid ? m.sp_start[slot] - sp0 : 0, s1 = valid ? m.sp_start[slot + 1] - sp0 : 0;
   const bool helpers = m.tile_help[tile] != 0;
   const int hub_local = m.tile_react[tile];
   const float fdt = (float)a.dt;
@@ -186,22 +237,13 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
     const bool due = (a.refresh[eval >> 6] >> (eval & 63)) & 1ull;  // refresh (src/cilia.cpp:206-215)
     ++eval;
     if (c1 > c0 && due) {
-      int off = 0;
-      for (int c = c0; c < c1; ++c) {
-        const CiliumDev cl = m.cil[c];
-        const int nb = cl.len - cl.num_anker;
-        const int w = (int)threadIdx.x - off;
-        if (w >= 0 && w < nb) {
-          const int i = cl.num_anker - 1 + w;
-          const int k = cl.bond_base - bond0 + i;
-          const int l0 = cl.slot0 - base;
-          const int sd = cl.stride;
-          const float l = cl_cilium_length(cl, i, (float)m.midpnt[c], bold[k], B.dist(l0 + sd * i, l0 + sd * (i + 1)));
-          bnew[k] = l;
-          bold[k] = l;
-          bdiag[k] = sqrtf(0.25f + 0.5f * l);
-        }
-        off += nb;
+      for (int k = threadIdx.x; k < nbond; k += blockDim.x) {
+        const int4 e = rf[k];
+        if (e.x < 0) continue;
+        const float l = cl_cilium_length(cpar[e.w], e.z, cmid[e.w], bold[k], B.dist(e.x, e.y));
+        bnew[k] = l;
+        bold[k] = l;
+        bdiag[k] = sqrtf(0.25f + 0.5f * l);
       }
       __syncthreads();
     }
@@ -237,12 +279,12 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
           rz = fmaf(-dz, fac, rz);
         }
       };
-      int s = s0 + lane;
-      for (; s + kCLanes < s1; s += 2 * kCLanes) {
-        one(s, ax, ay, az);
-        one(s + kCLanes, bx, by, bz);
+      int k = 0;
+      for (; k + 1 < nmine; k += 2) {
+        one(ebase + 32 * k, ax, ay, az);
+        one(ebase + 32 * (k + 1), bx, by, bz);
       }
-      if (s < s1) one(s, ax, ay, az);
+      if (k < nmine) one(ebase + 32 * k, ax, ay, az);
       ax += bx;
       ay += by;
       az += bz;

@@ -375,8 +375,24 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     // per-tile maxima for the cluster kernel's shared-memory layout
     std::vector<int> tb(out.ntiles, 0);
     for (int c = 0; c < ncil; ++c) tb[cil_tile[c]] += in.cil[c].rodlength;
+    // springs per tile in the kernel's warp-sliced layout: thread th = q *
+    // lanes + lane takes entries lane, lane + lanes, ... of slot q's list;
+    // every warp is padded to its longest thread list
+    const int lanes = out.cl_lanes;
+    const int nthreads = tile * lanes;
     for (int t = 0; t < out.ntiles; ++t) {
-      out.cl_nsp_max = std::max(out.cl_nsp_max, start[(t + 1) * tile] - start[t * tile]);
+      int entries = 0;
+      for (int w = 0; w < nthreads / 32; ++w) {
+        int W = 0;
+        for (int th = 32 * w; th < 32 * w + 32; ++th) {
+          const int q = th / lanes, lane = th % lanes;
+          const int slot = t * tile + q;
+          const int len = start[slot + 1] - start[slot];
+          W = std::max(W, std::max(0, (len - lane + lanes - 1) / lanes));
+        }
+        entries += 32 * W;
+      }
+      out.cl_nsp_max = std::max(out.cl_nsp_max, entries);
       out.cl_nbond_max = std::max(out.cl_nbond_max, tb[t]);
     }
     probe.cl_nsp_max = out.cl_nsp_max;

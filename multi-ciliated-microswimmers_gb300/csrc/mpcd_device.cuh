@@ -18,6 +18,7 @@ enum : unsigned {
   kErrBarrier = 4u,        // grid barrier wait exceeded its iteration cap
   kErrCellRange = 8u,      // a non-finite or out-of-range coordinate (e.g. an unstable MD step)
   kErrCellOverflow = 16u,  // more than 65535 particles of one kind in a cell
+  kErrLayout = 32u,        // MD shared-memory layout smaller than the tile needs (planner mismatch)
 };
 
 // ----------------------------------------------------------- constants ---

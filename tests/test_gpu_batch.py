@@ -195,3 +195,24 @@ def test_autotune_picks_a_valid_configuration():
         assert st["err"] == 0 and st["steps"] > 100
         o = b.observables(k)
         assert 0.8 < o["kT"] < 1.3
+
+
+def test_md_relayout_continues_the_trajectory():
+    spec = dict(L=16, radius=2.0, n_cilia=8, rodlength=10, seed=17)
+    s = swimmer_sim(spec)
+    b1, b2 = make_batch([spec]), make_batch([spec])
+    r1, r2 = b1.add_engine(s.engine), b2.add_engine(s.engine)
+    b1.admit(r1)
+    b2.admit(r2)
+    for b, r in ((b1, r1), (b2, r2)):
+        b.set_steps(r, 6)
+        b.run(3)
+    b2.set_md_layout(1, 512)
+    assert b2.md_layout() == (1, 512)
+    b1.run(3)
+    b2.run(3)
+    nb = s.nbeads
+    p1, v1 = b1.beads(r1, nb)
+    p2, v2 = b2.beads(r2, nb)
+    assert np.abs(p1 - p2).max() < 1e-3
+    assert b2.status(r2)["steps"] == 6 and b2.status(r2)["err"] == 0
