@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -262,6 +263,79 @@ def run_ensemble(args, n=64, steps=1000):
     }
 
 
+# ----------------------------------------------------------------- serving --
+
+def run_serving(args, n=60, steps_range=(100, 2000), load=0.8, seed=21):
+    """Continuous batching of swimmer runs: Poisson arrivals of requests with
+    box edge uniform in 16..64 (10 fluid per cell), 0-200 cilia of rodlength
+    15 on a sphere of radius min(8, edge/4) (a radius-edge/8 sphere carrying
+    more than about 70 cilia goes numerically unstable within a few hundred
+    steps in the reference's own arithmetic), step counts log-uniform in
+    steps_range, float32 split; the arrival rate offers `load` x an estimated
+    throughput.  Reports completion latency (submit -> done) percentiles and
+    throughput."""
+    import cilia_gpu as cg
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(n):
+        L = int(rng.integers(16, 65))
+        nc = int(rng.integers(0, 201))
+        st = int(round(math.exp(rng.uniform(math.log(steps_range[0]), math.log(steps_range[1])))))
+        reqs.append((L, nc, st, 1000 + k))
+    e_l3 = float(np.mean([x ** 3 for x in range(16, 65)]))
+    mean_particles = 10 * e_l3 + 643 + 45 * 100
+    mean_steps = (steps_range[1] - steps_range[0]) / math.log(steps_range[1] / steps_range[0])
+    est_throughput = 1.5e10  # particle-steps/s of a full batch (ensemble measurement)
+    rate = load * est_throughput / (mean_particles * mean_steps)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    # capacity for about 64 average requests resident, budget 60 % of it (admission by footprint)
+    cap_req = 64
+    caps = dict(max_replicas=cap_req + 16, max_particles=int(cap_req * 10 * e_l3 * 1.1) + 64 * 8192,
+                max_cells=int(cap_req * e_l3 * 1.1) + 64 * 2048, max_slots=cap_req * 2 * 5200 + 40 * 2048,
+                max_springs=cap_req * 14 * 5200, max_halo=cap_req * 6 * 5200 + 4096, max_cilia=cap_req * 200,
+                max_bonds=cap_req * 200 * 15, md_lanes=1, md_tile=1024)
+    # the device bytes of the whole capacity; requests are admitted while the
+    # sum of their footprints stays within 60 % of it
+    cap_bytes = cg.lib().mpcd_batch_estimate(None, caps["max_particles"], caps["max_cells"], cap_req * 5200,
+                                             caps["max_springs"], caps["max_cilia"], caps["max_bonds"])
+    budget = int(0.6 * cap_bytes)
+    srv = cg.Server(budget_bytes=budget, chunk_steps=25, prep_threads=4, device=args.device, **caps)
+    texts = {}
+    t0 = time.perf_counter()
+    ids = []
+    for (L, nc, st, sd), ta in zip(reqs, arrivals):
+        key = (L, nc)
+        if key not in texts:
+            texts[key] = simcfg.dumps(simcfg.swimmer_config(L, radius=min(8.0, L / 4.0), n_cilia=nc, rodlength=15,
+                                                            seed=sd))
+        dt = t0 + ta - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(srv.submit(texts[key], st, seed=sd))
+    srv.drain(3600)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    infos = [srv.info(i) for i in ids]
+    errors = sorted({f"{srv.error(i)} (bits {inf['err']}, L {r[0]}, cilia {r[1]})"
+                     for i, inf, r in zip(ids, infos, reqs) if inf["state"] != cg.REQ_DONE})
+    srv.close()
+    done = [i for i in infos if i["state"] == cg.REQ_DONE]
+    return {
+        "workload": f"serving: {n} swimmer runs, Poisson arrivals at {rate:.1f}/s, box edge uniform 16..64 x 10 "
+                    f"fluid/cell, sphere radius min(8, edge/4) with 0-200 cilia of 3x15 beads, steps log-uniform {steps_range[0]}..{steps_range[1]}, "
+                    f"float32 split",
+        "metric": METRIC, "value": st["throughput"], "unit": UNIT, "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+        "mean_s": st["mean_s"], "max_s": st["max_s"], "completed": st["completed"], "failed": st["failed"],
+        "wall_s": wall, "busy_s": st["busy_s"], "particle_steps": st["particle_steps"],
+        "peak_resident": st["peak_resident"], "peak_resident_gb": st["peak_resident_bytes"] / 1e9,
+        "budget_gb": budget / 1e9, "gpu_launches": st["gpu_launches"],
+        "queue_wait_p50_s": float(np.median([i["t_admit"] - i["t_submit"] for i in done])) if done else None,
+        "kT_range": [min(i["obs"]["kT"] for i in done), max(i["obs"]["kT"] for i in done)] if done else None,
+        "errors": errors[:12],
+    }
+
+
 # ------------------------------------------------------------------ CPU arm --
 
 def run_cpu(args, budget_s=None, threads=None):
@@ -306,6 +380,9 @@ def main():
     ap.add_argument("--verify-counts", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-only", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-only", action="store_true")
+    ap.add_argument("--serving-full", action="store_true", help="500 requests, steps 500..20000")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -340,6 +417,11 @@ def main():
     if args.ensemble_only:
         if rank == 0:
             print(json.dumps(run_ensemble(args)))
+        return
+    if args.serving_only or args.serving_full:
+        if rank == 0:
+            kw = dict(n=500, steps_range=(500, 20000)) if args.serving_full else {}
+            print(json.dumps(run_serving(args, **kw)))
         return
     if dist is not None:
         dist.barrier()
@@ -393,6 +475,8 @@ def main():
                        "d2h_bytes_per_step": e["d2h"]}
     if not args.no_ensemble and args.gpus == 1:
         line["batched"] = run_ensemble(args)
+    if not args.no_serving and args.gpus == 1:
+        line["serving"] = run_serving(args)
     if not args.no_cpu:
         c = run_cpu(args)
         line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",

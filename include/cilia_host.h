@@ -18,6 +18,7 @@
 #ifndef CILIA_HOST_H
 #define CILIA_HOST_H
 
+#include "mpcd_batch.h"
 #include "mpcd_gpu.h"
 
 #ifdef __cplusplus
@@ -53,6 +54,13 @@ long cilia_sim_bead_count(const cilia_sim* s);
 int cilia_sim_next_tstep(cilia_sim* s, const mpcd_inject* inj);
 int cilia_sim_run(cilia_sim* s);
 int cilia_sim_save(cilia_sim* s);
+/* Builds the system a sim.cfg describes on the host only (objects, springs,
+ * cilia, the fluid of Fluid::create or fluid_n.dat, the grid shift) and adds
+ * it to a replica batch as a new replica, not yet admitted (mpcd_batch_admit).
+ * opt->precision is ignored: a batch runs MPCD_FP32.  Errors from the cfg
+ * come back through cilia_sim_last_error(NULL), from the batch through
+ * mpcd_batch_last_error. */
+int cilia_batch_add_cfg(mpcd_batch* b, const char* cfg, int is_text, const cilia_options* opt, int* replica);
 /* writes the cfg back with the current globalt (src/main.cpp:95-96) */
 int cilia_sim_write_cfg(cilia_sim* s, const char* path);
 

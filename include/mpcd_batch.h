@@ -75,6 +75,10 @@ int mpcd_batch_set_cilia(mpcd_batch* b, int r, int nc, const mpcd_cilium* cilia,
                          const double* oldlength);
 /* device bytes the replica will hold once admitted (fluid, cells, MD) */
 int mpcd_batch_footprint(mpcd_batch* b, int r, long long* bytes);
+/* the same estimate from the sizes alone: fluid particles, cells, beads,
+ * springs, cilia, bond-table entries */
+long long mpcd_batch_estimate(const mpcd_batch* b, long nf, long ncell, long nb, long nsprings, int ncilia,
+                              long nbonds);
 /* plans the replica's MD, takes its device ranges, uploads and bins it;
  * MPCD_EINVAL (nothing changed) when a capacity is exhausted */
 int mpcd_batch_admit(mpcd_batch* b, int r);

@@ -1,6 +1,6 @@
 """Build the native libraries in-tree.
 
-  libmpcd_gpu.so  CUDA kernels + C ABI (include/mpcd_gpu.h), sm_103a only
+  libmpcd_gpu.so  CUDA kernels + C ABI (include/*.h), sm_103a only
   cilia           drop-in executable `cilia sim.cfg` (host C++ over the C ABI)
 
 Translation units compile in parallel; outputs land next to this file
@@ -23,9 +23,9 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-rela
            "-I", CSRC, "-I", os.path.join(REPO, "include")] + ARCH
 CU_SOURCES = ["fluid_kernels.cu", "md_kernels.cu", "md_cluster.cu", "md_plan.cu", "engine.cu", "static_step.cu",
               "batch_kernels.cu", "batch.cu"]
-HOST_SOURCES = ["host/libconfig_lite.cpp", "host/objects.cpp", "host/cilia_capi.cpp"]
+HOST_SOURCES = ["host/libconfig_lite.cpp", "host/objects.cpp", "host/cilia_capi.cpp", "host/server.cpp"]
 CXX = os.environ.get("CXX", "g++")
-CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", os.path.join(CSRC, "host"), "-I", os.path.join(REPO, "include")]
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-pthread", "-I", os.path.join(CSRC, "host"), "-I", os.path.join(REPO, "include")]
 
 LIB = os.path.join(OUT, "libmpcd_gpu.so")
 
@@ -41,7 +41,8 @@ def _headers():
     hs = []
     for root, _, files in os.walk(CSRC):
         hs += [os.path.join(root, f) for f in files if f.endswith((".h", ".cuh", ".hpp"))]
-    hs.append(os.path.join(REPO, "include", "mpcd_gpu.h"))
+    inc = os.path.join(REPO, "include")
+    hs += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     return hs
 
 
@@ -78,12 +79,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs = [f.result() for f in fut_cu] + [f.result() for f in fut_host[:-1]]
         main_obj = fut_host[-1].result()
     if force or _newer(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
     if force or _newer(EXE, [LIB, main_obj]):
-        cmd = [CXX, "-o", EXE, main_obj, "-L", OUT, "-lmpcd_gpu", "-Wl,-rpath,$ORIGIN"]
+        cmd = [CXX, "-pthread", "-o", EXE, main_obj, "-L", OUT, "-lmpcd_gpu", "-Wl,-rpath,$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of cilia failed:\n{r.stderr}")

@@ -70,6 +70,29 @@ class MpcdBatchTuning(ctypes.Structure):
                 ("cell_blocks", ctypes.c_int), ("sort_interval", ctypes.c_int)]
 
 
+class MpcdServerParams(ctypes.Structure):
+    _fields_ = [("batch", MpcdBatchParams), ("budget_bytes", ctypes.c_longlong), ("chunk_steps", ctypes.c_int),
+                ("keep_fluid", ctypes.c_int), ("lookahead", ctypes.c_int), ("prep_threads", ctypes.c_int)]
+
+
+class MpcdRequestInfo(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_longlong), ("state", ctypes.c_int), ("steps", ctypes.c_longlong),
+                ("t_submit", _D), ("t_admit", _D), ("t_done", _D), ("nfluid", ctypes.c_longlong),
+                ("nbeads", ctypes.c_longlong), ("footprint", ctypes.c_longlong), ("obs", MpcdObs),
+                ("err_bits", ctypes.c_uint)]
+
+
+class MpcdServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong), ("failed", ctypes.c_longlong),
+                ("resident", ctypes.c_longlong), ("queued", ctypes.c_longlong), ("p50_s", _D), ("p99_s", _D),
+                ("mean_s", _D), ("max_s", _D), ("particle_steps", _D), ("busy_s", _D), ("throughput", _D),
+                ("peak_resident_bytes", ctypes.c_longlong), ("peak_resident", ctypes.c_int),
+                ("gpu_launches", ctypes.c_longlong)]
+
+
+REQ_QUEUED, REQ_RESIDENT, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
 class MpcdError(RuntimeError):
     pass
 
@@ -127,6 +150,10 @@ def lib():
             "mpcd_batch_set_cilia": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(MpcdCilium), _DP,
                                                     _DP]),
             "mpcd_batch_footprint": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
+            "mpcd_batch_estimate": (ctypes.c_longlong, [P, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long,
+                                                        ctypes.c_int, ctypes.c_long]),
+            "cilia_batch_add_cfg": (ctypes.c_int, [P, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
+                                                   _IP]),
             "mpcd_batch_admit": (ctypes.c_int, [P, ctypes.c_int]),
             "mpcd_batch_set_steps": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_longlong]),
             "mpcd_batch_run": (ctypes.c_int, [P, ctypes.c_int]),
@@ -148,6 +175,18 @@ def lib():
             "mpcd_batch_stage_times": (ctypes.c_int, [P, ctypes.c_int, _DP]),
             "mpcd_batch_set_md_layout": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
             "mpcd_batch_get_md_layout": (ctypes.c_int, [P, _IP, _IP]),
+            "mpcd_server_create": (ctypes.c_int, [ctypes.POINTER(MpcdServerParams), ctypes.POINTER(P)]),
+            "mpcd_server_destroy": (ctypes.c_int, [P]),
+            "mpcd_server_last_error": (ctypes.c_char_p, [P]),
+            "mpcd_server_submit": (ctypes.c_int, [P, ctypes.c_char_p, ctypes.c_longlong, ctypes.c_ulonglong,
+                                                  ctypes.POINTER(ctypes.c_longlong)]),
+            "mpcd_server_info": (ctypes.c_int, [P, ctypes.c_longlong, ctypes.POINTER(MpcdRequestInfo)]),
+            "mpcd_server_wait": (ctypes.c_int, [P, ctypes.c_longlong, _D, ctypes.POINTER(MpcdRequestInfo)]),
+            "mpcd_server_drain": (ctypes.c_int, [P, _D]),
+            "mpcd_server_result_beads": (ctypes.c_int, [P, ctypes.c_longlong, ctypes.c_long, _DP, _DP]),
+            "mpcd_server_result_fluid": (ctypes.c_int, [P, ctypes.c_longlong, ctypes.c_long, _DP, _DP]),
+            "mpcd_server_get_stats": (ctypes.c_int, [P, ctypes.POINTER(MpcdServerStats)]),
+            "mpcd_server_request_error": (ctypes.c_char_p, [P, ctypes.c_longlong]),
             "cilia_sim_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
                                                 ctypes.POINTER(P)]),
             "cilia_sim_destroy": (ctypes.c_int, [P]),
@@ -435,6 +474,18 @@ class Batch:
         self._ck(lib().mpcd_batch_add_engine(self._h, engine.handle, ctypes.byref(r)), "batch_add_engine")
         return r.value
 
+    def add_cfg(self, cfg, *, is_text=True, seed=1, ststep=0.0, bead_mass=5.0, create_fluid=True):
+        """A replica built on the host from a sim.cfg (not yet admitted)."""
+        o = CiliaOptions(MPCD_FP32, 0, seed, ststep, int(create_fluid), 0, WALLS_NONE, 0.0, bead_mass, 0)
+        r = ctypes.c_int()
+        rc = lib().cilia_batch_add_cfg(self._h, cfg.encode() if isinstance(cfg, str) else cfg, int(is_text),
+                                       ctypes.byref(o), ctypes.byref(r))
+        if rc:
+            m1 = lib().cilia_sim_last_error(None)
+            m2 = lib().mpcd_batch_last_error(self._h)
+            raise MpcdError(f"cilia_batch_add_cfg failed ({rc}): {(m1 or b'').decode()} {(m2 or b'').decode()}")
+        return r.value
+
     def set_fluid(self, r, pos, vel):
         pos, vel = _f64(pos), _f64(vel)
         self._ck(lib().mpcd_batch_set_fluid(self._h, r, pos.shape[0], _dp(pos), _dp(vel)), "batch_set_fluid")
@@ -541,3 +592,87 @@ class Batch:
         out = np.zeros(4)
         self._ck(lib().mpcd_batch_stage_times(self._h, int(nsteps), _dp(out)), "batch_stage_times")
         return dict(cell=out[0], fluid=out[1], md=out[2], sort=out[3])
+
+
+def _info_dict(i):
+    o = i.obs
+    return dict(id=i.id, state=i.state, steps=i.steps, t_submit=i.t_submit, t_admit=i.t_admit, t_done=i.t_done,
+                nfluid=i.nfluid, nbeads=i.nbeads, footprint=i.footprint, err=i.err_bits,
+                obs=dict(momentum=np.array(o.momentum[:]), n=o.n, mass=o.mass, kT=o.kT, fluid_T=o.fluid_T,
+                         diss_energy=o.diss_energy, globalt=o.globalt, energy_fluid=o.energy_fluid))
+
+
+class Server:
+    """Continuous batching of swimmer runs (mpcd_server)."""
+
+    def __init__(self, *, budget_bytes=0, chunk_steps=0, keep_fluid=False, lookahead=0, prep_threads=0, **batch):
+        b = dict(device=0, max_replicas=16, max_particles=0, max_cells=0, max_slots=0, max_springs=0, max_halo=0,
+                 max_cilia=0, max_bonds=0, md_lanes=0, md_tile=0, sort_interval=0, sorts_per_graph=0)
+        b.update(batch)
+        p = MpcdServerParams(MpcdBatchParams(b["device"], b["max_replicas"], b["max_particles"], b["max_cells"],
+                                             b["max_slots"], b["max_springs"], b["max_halo"], b["max_cilia"],
+                                             b["max_bonds"], b["md_lanes"], b["md_tile"], b["sort_interval"],
+                                             b["sorts_per_graph"]),
+                             int(budget_bytes), int(chunk_steps), int(bool(keep_fluid)), int(lookahead),
+                             int(prep_threads))
+        h = ctypes.c_void_p()
+        rc = lib().mpcd_server_create(ctypes.byref(p), ctypes.byref(h))
+        if rc:
+            raise MpcdError(f"mpcd_server_create failed with code {rc}")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mpcd_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, cfg, nsteps, seed=1):
+        i = ctypes.c_longlong()
+        rc = lib().mpcd_server_submit(self._h, cfg.encode() if isinstance(cfg, str) else cfg, int(nsteps), int(seed),
+                                      ctypes.byref(i))
+        if rc:
+            raise MpcdError(f"submit failed ({rc})")
+        return i.value
+
+    def info(self, rid):
+        i = MpcdRequestInfo()
+        if lib().mpcd_server_info(self._h, int(rid), ctypes.byref(i)):
+            raise MpcdError("unknown request")
+        return _info_dict(i)
+
+    def wait(self, rid, timeout=600.0):
+        """Info of the finished request; raises if it failed or timed out."""
+        i = MpcdRequestInfo()
+        rc = lib().mpcd_server_wait(self._h, int(rid), float(timeout), ctypes.byref(i))
+        if rc:
+            msg = lib().mpcd_server_last_error(self._h)
+            raise MpcdError(f"request {rid}: wait failed ({rc}): {self.error(rid) or (msg.decode() if msg else '')}")
+        return _info_dict(i)
+
+    def drain(self, timeout=600.0):
+        if lib().mpcd_server_drain(self._h, float(timeout)):
+            raise MpcdError("drain timed out")
+
+    def result_beads(self, rid, nb):
+        pos, vel = np.zeros((nb, 3)), np.zeros((nb, 3))
+        if lib().mpcd_server_result_beads(self._h, int(rid), int(nb), _dp(pos), _dp(vel)):
+            raise MpcdError("no bead result")
+        return pos, vel
+
+    def result_fluid(self, rid, n):
+        pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
+        if lib().mpcd_server_result_fluid(self._h, int(rid), int(n), _dp(pos), _dp(vel)):
+            raise MpcdError("no fluid result")
+        return pos, vel
+
+    def error(self, rid):
+        m = lib().mpcd_server_request_error(self._h, int(rid))
+        return m.decode() if m else ""
+
+    def stats(self):
+        st = MpcdServerStats()
+        lib().mpcd_server_get_stats(self._h, ctypes.byref(st))
+        return {k: getattr(st, k) for k, _ in MpcdServerStats._fields_}

@@ -130,7 +130,7 @@ struct Replica {
 };
 
 struct MDLaunch {
-  int ctiles = 0, hmax = 0, nsp_max = 0, nbond_max = 0;
+  int ctiles = 0, hmax = 0, nsp_max = 0, nbond_max = 0, nbuf = 2;
   int offset = 0, count = 0;  // into the device list of replica indices
 };
 
@@ -212,6 +212,7 @@ BatchTables tables(mpcd_batch* b) {
 
 Replica* get_rep(mpcd_batch* b, int r) {
   if (!b || r < 0 || r >= (int)b->reps.size() || !b->reps[r].used) return nullptr;
+  cudaSetDevice(b->p.device);  // the calling thread may not have the batch's device current
   return &b->reps[r];
 }
 
@@ -288,6 +289,14 @@ void free_all(mpcd_batch* b) {
 int plan_launches(mpcd_batch* b) {
   std::vector<int> list;
   b->launches.clear();
+  // position buffers for a launch layout: 2 if that fits, else 1; 0 if neither
+  auto buffers = [&](const MDLaunch& L) {
+    for (int nbuf = 2; nbuf >= 1; --nbuf)
+      if (md_cluster_batch_feasible(b->lanes, b->T, L.ctiles,
+                                    md_cluster_batch_smem(b->T, L.hmax, L.nsp_max, L.nbond_max, nbuf)))
+        return nbuf;
+    return 0;
+  };
   for (int c = 1; c <= kMaxClusterTiles; ++c) {
     MDLaunch cur;
     for (int r = 0; r < (int)b->reps.size(); ++r) {
@@ -298,19 +307,21 @@ int plan_launches(mpcd_batch* b) {
       nxt.hmax = std::max(cur.hmax, R.plan.hmax);
       nxt.nsp_max = std::max(cur.nsp_max, R.plan.cl_nsp_max);
       nxt.nbond_max = std::max(cur.nbond_max, R.plan.cl_nbond_max);
-      const size_t smem = md_cluster_batch_smem(b->T, nxt.hmax, nxt.nsp_max, nxt.nbond_max);
-      if (cur.count > 0 && !md_cluster_batch_feasible(b->lanes, b->T, c, smem)) {
+      nxt.nbuf = buffers(nxt);
+      if (cur.count > 0 && nxt.nbuf < cur.nbuf) {  // would shrink or break the layout: new launch
         b->launches.push_back(cur);
         nxt = MDLaunch{};
         nxt.ctiles = c;
         nxt.hmax = R.plan.hmax;
         nxt.nsp_max = R.plan.cl_nsp_max;
         nxt.nbond_max = R.plan.cl_nbond_max;
+        nxt.nbuf = buffers(nxt);
         nxt.offset = (int)list.size();
         nxt.count = 0;
       } else if (cur.count == 0) {
         nxt.offset = (int)list.size();
       }
+      if (nxt.nbuf == 0) return fail(b, MPCD_EINVAL, "an admitted swimmer's MD layout does not fit on the device");
       list.push_back(r);
       nxt.count += 1;
       cur = nxt;
@@ -337,7 +348,7 @@ int enqueue_step(mpcd_batch* b, int par) {
       const MDLaunch& L = b->launches[k];
       cudaError_t st = cudaSuccess;
       n += launch_md_cluster_batch(b->md, t, b->cells, b->d_md_reps + L.offset, L.count, L.ctiles, L.hmax, L.nsp_max,
-                                   L.nbond_max, s, &st);
+                                   L.nbond_max, L.nbuf, s, &st);
       if (st != cudaSuccess) return cuda_fail(b, st, "batch MD launch");
     }
   }
@@ -480,9 +491,12 @@ std::string plan_replica(mpcd_batch* b, Replica& R) {
   f.tile = b->T;
   std::string why = plan_md(in, f, true, false, 1, R.plan);
   if (!why.empty()) return why;
-  const size_t smem = md_cluster_batch_smem(b->T, R.plan.hmax, R.plan.cl_nsp_max, R.plan.cl_nbond_max);
-  if (!md_cluster_batch_feasible(b->lanes, b->T, R.plan.ntiles, smem))
-    return "the replica's MD cluster does not fit on the device with this layout";
+  bool fits = false;
+  for (int nbuf = 2; nbuf >= 1 && !fits; --nbuf)
+    fits = md_cluster_batch_feasible(b->lanes, b->T, R.plan.ntiles,
+                                     md_cluster_batch_smem(b->T, R.plan.hmax, R.plan.cl_nsp_max,
+                                                           R.plan.cl_nbond_max, nbuf));
+  if (!fits) return "the replica's MD cluster does not fit on the device with this layout";
   return "";
 }
 
@@ -921,18 +935,26 @@ int mpcd_batch_set_cilia(mpcd_batch* b, int r, int nc, const mpcd_cilium* cilia,
   return MPCD_OK;
 }
 
+long long mpcd_batch_estimate(const mpcd_batch* b, long nf, long ncell, long nb, long nsprings, int ncilia,
+                              long nbonds) {
+  const long T = b ? b->T : 512;
+  const long pages = (nf + kPartPage - 1) / kPartPage, cpages = (ncell + kCellPage - 1) / kCellPage;
+  long long f = pages * (long long)kPartPage * (2 * (sizeof(float4) * 2 + 4) + 4);  // two buffers + rank
+  f += cpages * (long long)kCellPage * (sizeof(float4) * 4 + 3 * 4);               // sum, par, cnt, count, start
+  if (nb > 0) {
+    const long slots = nb + nb / 8 + 2 * T;                                         // helpers, padding, spare tile
+    f += (long long)slots * (6 * 8 + 4 * 4);
+    f += (long long)nsprings * 36 + (long long)nb * 4;                              // springs, halo
+    f += (long long)ncilia * (sizeof(CiliumDev) + 16) + (long long)nbonds * 24;
+  }
+  return f;
+}
+
 int mpcd_batch_footprint(mpcd_batch* b, int r, long long* bytes) {
   Replica* R = get_rep(b, r);
   if (!R || !bytes) return fail(b, MPCD_EINVAL, "footprint: bad arguments");
-  const long pages = (R->nf + kPartPage - 1) / kPartPage, cpages = (R->ncell + kCellPage - 1) / kCellPage;
-  long long f = pages * (long long)kPartPage * (2 * (sizeof(float4) * 2 + 4) + 4);  // two buffers + rank
-  f += cpages * (long long)kCellPage * (sizeof(float4) * 4 + 3 * 4);               // sum, par, cnt, count, start
-  // MD: slots, springs, halo from the spring count (planned at admission)
-  const long slots = R->nb + R->nb / 8 + b->T;
-  f += (long long)slots * (6 * 8 + 4 * 4);
-  f += (long long)R->sp_t.size() * 32 + (long long)R->sp_t.size() * 4;
-  f += (long long)R->cil.size() * (sizeof(CiliumDev) + 16) + (long long)R->newlen.size() * 24;
-  *bytes = f;
+  *bytes = mpcd_batch_estimate(b, R->nf, R->ncell, R->nb, (long)R->sp_t.size(), (int)R->cil.size(),
+                               (long)R->newlen.size());
   return MPCD_OK;
 }
 
@@ -1067,11 +1089,13 @@ int mpcd_batch_set_steps(mpcd_batch* b, int r, long long nsteps) {
 
 int mpcd_batch_run(mpcd_batch* b, int nsteps) {
   if (!b || nsteps < 0) return fail(b, MPCD_EINVAL, "run: bad arguments");
+  cudaSetDevice(b->p.device);
   return run_steps(b, nsteps);
 }
 
 int mpcd_batch_timed_run(mpcd_batch* b, int nsteps, double* total_ms) {
   if (!b || nsteps < 0) return fail(b, MPCD_EINVAL, "timed_run: bad arguments");
+  cudaSetDevice(b->p.device);
   int rc = rebuild_graphs(b);
   if (rc) return rc;
   cudaEvent_t e0, e1;
@@ -1091,6 +1115,7 @@ int mpcd_batch_timed_run(mpcd_batch* b, int nsteps, double* total_ms) {
 
 int mpcd_batch_sync(mpcd_batch* b) {
   if (!b) return MPCD_EINVAL;
+  cudaSetDevice(b->p.device);
   BK(cudaStreamSynchronize(b->s0));
   return MPCD_OK;
 }
@@ -1235,6 +1260,7 @@ int mpcd_batch_resident(const mpcd_batch* b) {
 
 int mpcd_batch_set_tuning(mpcd_batch* b, const mpcd_batch_tuning* t) {
   if (!b || !t) return fail(b, MPCD_EINVAL, "set_tuning: bad arguments");
+  cudaSetDevice(b->p.device);
   if (t->fluid_threads < 32 || t->fluid_threads > 1024 || t->fluid_threads % 32 || t->cell_threads < 32 ||
       t->cell_threads > 1024 || t->cell_threads % 32 || t->fluid_blocks < 0 || t->cell_blocks < 0 ||
       t->sort_interval < 1)
@@ -1258,6 +1284,7 @@ int mpcd_batch_get_tuning(const mpcd_batch* b, mpcd_batch_tuning* t) {
 
 int mpcd_batch_autotune(mpcd_batch* b, int trial_steps, mpcd_batch_tuning* chosen) {
   if (!b || trial_steps < 1) return fail(b, MPCD_EINVAL, "autotune: bad arguments");
+  cudaSetDevice(b->p.device);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1342,6 +1369,7 @@ int mpcd_batch_autotune(mpcd_batch* b, int trial_steps, mpcd_batch_tuning* chose
 
 int mpcd_batch_stage_times(mpcd_batch* b, int nsteps, double* out4) {
   if (!b || nsteps < 1 || !out4) return fail(b, MPCD_EINVAL, "stage_times: bad arguments");
+  cudaSetDevice(b->p.device);
   int rc = rebuild_graphs(b);  // MD launch plan
   if (rc) return rc;
   const BatchTables t = tables(b);
@@ -1360,7 +1388,7 @@ int mpcd_batch_stage_times(mpcd_batch* b, int nsteps, double* out4) {
     for (const MDLaunch& L : b->launches) {
       cudaError_t st = cudaSuccess;
       b->launches_total += launch_md_cluster_batch(b->md, t, b->cells, b->d_md_reps + L.offset, L.count, L.ctiles,
-                                                   L.hmax, L.nsp_max, L.nbond_max, b->s0, &st);
+                                                   L.hmax, L.nsp_max, L.nbond_max, L.nbuf, b->s0, &st);
       if (st != cudaSuccess) return cuda_fail(b, st, "batch MD launch");
     }
     BK(cudaEventRecord(E[3], b->s0));
@@ -1389,6 +1417,7 @@ int mpcd_batch_stage_times(mpcd_batch* b, int nsteps, double* out4) {
 
 int mpcd_batch_set_md_layout(mpcd_batch* b, int lanes, int tile) {
   if (!b) return MPCD_EINVAL;
+  cudaSetDevice(b->p.device);
   if (lanes == 0) lanes = 2;
   if (tile == 0) tile = 512 / lanes;
   if ((lanes != 1 && lanes != 2) || tile < 32 || tile % 32 || tile * lanes > 1024)

@@ -95,8 +95,10 @@ int launch_batch_observables(const BatchTables& t, BatchFluid f, const MDState& 
                              double* out, cudaStream_t s);
 // MD of the replicas listed in `reps` (all with `ctiles` tiles), one cluster each
 int launch_md_cluster_batch(const MDState& m, const BatchTables& t, BatchCells c, const int* reps, int nreps,
-                            int ctiles, int hmax, int nsp_max, int nbond_max, cudaStream_t s, cudaError_t* st);
-size_t md_cluster_batch_smem(int tile, int hmax, int nsp_max, int nbond_max);
+                            int ctiles, int hmax, int nsp_max, int nbond_max, int nbuf, cudaStream_t s,
+                            cudaError_t* st);
+// shared memory of one CTA; nbuf position buffers (2, or 1 with a second cluster barrier per substep)
+size_t md_cluster_batch_smem(int tile, int hmax, int nsp_max, int nbond_max, int nbuf);
 int md_cluster_batch_feasible(int lanes, int tile, int ctiles, size_t smem);
 
 // shared with fluid_kernels.cu: exclusive scan of `count` into `start`

@@ -284,6 +284,7 @@ int build_md(mpcd_engine* h) {
   m.cl_lanes = pl.cl_lanes;
   m.cl_nsp_max = pl.cl_nsp_max;
   m.cl_nbond_max = pl.cl_nbond_max;
+  m.cl_nbuf = pl.cl_nbuf;
   m.tile = pl.tile;
   m.ntiles = pl.ntiles;
   m.nslots = pl.nslots;

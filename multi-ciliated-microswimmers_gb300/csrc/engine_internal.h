@@ -107,6 +107,7 @@ struct MDState {
   int cl_nsp_max = 0;        // cluster layout: most springs of one tile
   int cl_nbond_max = 0;      // cluster layout: most bond-table entries of one tile
   int cl_lanes = 2;          // cluster layout: threads per slot (1 or 2)
+  int cl_nbuf = 2;           // cluster layout: position buffers (1 when two do not fit)
   int* sp_kind = nullptr;
   int* sp_ref = nullptr;
   double* sp_rest = nullptr;

@@ -57,6 +57,23 @@ cilia::SimOptions to_options(const cilia_options* o) {
 
 extern "C" {
 
+int cilia_batch_add_cfg(mpcd_batch* b, const char* cfg, int is_text, const cilia_options* opt, int* replica) {
+  if (!b || !cfg || !replica) return MPCD_EINVAL;
+  return guarded(g_create_error, [&]() {
+    libconfig::Config c;
+    if (is_text)
+      c.readString(cfg);
+    else
+      c.readFile(cfg);
+    cilia::SimOptions so = to_options(opt);
+    so.host_only = 1;
+    so.precision = MPCD_FP32;
+    cilia::Simulation sim(c.getRoot(), so);
+    cilia::add_to_batch(b, sim.host, sim.nbeads, replica);
+    return MPCD_OK;
+  });
+}
+
 int cilia_sim_create(const char* cfg, int is_text, const cilia_options* opt, cilia_sim** out) {
   if (!cfg || !out) return MPCD_EINVAL;
   *out = nullptr;

@@ -109,7 +109,7 @@ bool MDObject::load(std::istream& in) {
   return (bool)in;
 }
 
-bool MDObject::read_files = true;
+thread_local bool MDObject::read_files = true;
 
 bool MDObject::open_datfile() {
   if (!read_files) return false;
@@ -617,6 +617,32 @@ void World::saveparameter(libconfig::Setting& root) const {
   root["sizez"] = sizez;
 }
 
+void add_to_batch(mpcd_batch* b, const HostSystem& h, long nbeads, int* replica) {
+  mpcd_params p = h.p;
+  p.precision = MPCD_FP32;
+  int r = -1;
+  if (mpcd_batch_add(b, &p, &r) != MPCD_OK) throw std::runtime_error(std::string("batch: ") + mpcd_batch_last_error(b));
+  auto ck = [&](int rc) {
+    if (rc != MPCD_OK) {
+      const std::string m = std::string("batch: ") + mpcd_batch_last_error(b);
+      mpcd_batch_remove(b, r);
+      throw std::runtime_error(m);
+    }
+  };
+  ck(mpcd_batch_set_shift(b, r, h.a));
+  ck(mpcd_batch_set_time(b, r, h.globalt));
+  const long nf = (long)h.fpos.size() / 3;
+  if (nf > 0) ck(mpcd_batch_set_fluid(b, r, nf, h.fpos.data(), h.fvel.data()));
+  if (nbeads > 0) {
+    const SpringList& sp = h.springs;
+    ck(mpcd_batch_set_beads(b, r, nbeads, h.bpos.data(), h.bvel.data(), h.moves.data()));
+    ck(mpcd_batch_set_springs(b, r, (long)sp.size(), sp.target.data(), sp.other.data(), sp.kind.data(),
+                              sp.ref.data(), sp.rest.data(), sp.k.data()));
+    ck(mpcd_batch_set_cilia(b, r, (int)h.cilia.size(), h.cilia.data(), h.newlen.data(), h.oldlen.data()));
+  }
+  *replica = r;
+}
+
 // ----------------------------------------------------------- Simulation ---
 
 Simulation::Simulation(const libconfig::Setting& root, const SimOptions& o) : opt(o) {
@@ -652,8 +678,13 @@ Simulation::Simulation(const libconfig::Setting& root, const SimOptions& o) : op
   p.device = opt.device;
   p.sort_interval = opt.sort_interval;
   p.md_split = opt.md_split;
-  check(mpcd_create(&p, &eng), eng, "mpcd_create");
-  mpcd_set_time(eng, wc.globalt);
+  if (opt.host_only) {
+    host.p = p;
+    host.globalt = wc.globalt;
+  } else {
+    check(mpcd_create(&p, &eng), eng, "mpcd_create");
+    mpcd_set_time(eng, wc.globalt);
+  }
   // MPCD::MPCD: grid shift from mpcd.dat or three draws (src/libcilia/mpcd.cpp:86-97)
   double a[3];
   bool have = false;
@@ -663,7 +694,10 @@ Simulation::Simulation(const libconfig::Setting& root, const SimOptions& o) : op
   }
   if (!have)
     for (double& q : a) q = rng->rnd();
-  check(mpcd_set_shift(eng, a), eng, "mpcd_set_shift");
+  if (opt.host_only)
+    std::memcpy(host.a, a, sizeof host.a);
+  else
+    check(mpcd_set_shift(eng, a), eng, "mpcd_set_shift");
   // Simulation::load_config (src/simulation.cpp:614-648)
   const libconfig::Setting& objs = root["md_objects"];
   for (int i = 0; i < objs.getLength(); ++i) {
@@ -728,6 +762,16 @@ void Simulation::upload_md() {
   std::vector<mpcd_cilium> cil;
   std::vector<double> nl, ol;
   for (auto& o : md_objects) o->emit_cilia(cil, nl, ol);
+  if (opt.host_only) {
+    host.bpos = P;
+    host.bvel = V;
+    host.moves = moves;
+    host.springs = s;
+    host.cilia = cil;
+    host.newlen = nl;
+    host.oldlen = ol;
+    return;
+  }
   check(mpcd_set_beads(eng, nbeads, P.data(), V.data(), moves.data()), eng, "mpcd_set_beads");
   check(mpcd_set_springs(eng, (long)s.size(), s.target.data(), s.other.data(), s.kind.data(), s.ref.data(),
                          s.rest.data(), s.k.data()),
@@ -785,6 +829,11 @@ void Simulation::create_fluid() {
   for (int q = 0; q < 3; ++q) cm[q] /= n;
   for (long i = 0; i < n; ++i)
     for (int q = 0; q < 3; ++q) V[3 * i + q] -= cm[q];
+  if (opt.host_only) {
+    host.fpos.swap(P);
+    host.fvel.swap(V);
+    return;
+  }
   check(mpcd_set_fluid(eng, n, P.data(), V.data()), eng, "mpcd_set_fluid");
 }
 
@@ -807,6 +856,11 @@ bool Simulation::load_fluid(const char* path) {
     in >> V[3 * i] >> V[3 * i + 1] >> V[3 * i + 2] >> m;
   }
   if (!in) throw std::runtime_error("cannot read fluid file");
+  if (opt.host_only) {
+    host.fpos.swap(P);
+    host.fvel.swap(V);
+    return true;
+  }
   check(mpcd_set_fluid(eng, n, P.data(), V.data()), eng, "mpcd_set_fluid");
   return true;
 }

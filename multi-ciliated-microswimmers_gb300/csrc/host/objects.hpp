@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "libconfig_lite.hpp"
+#include "mpcd_batch.h"
 #include "mpcd_gpu.h"
 
 namespace cilia {
@@ -83,7 +84,7 @@ class MDObject {
   virtual bool load(std::istream& in);
   bool open_datfile();
   // whether constructors read <name>.dat checkpoints (set by the Simulation)
-  static bool read_files;
+  static thread_local bool read_files;
 };
 
 class Sphere : public MDObject {
@@ -189,7 +190,26 @@ struct SimOptions {
   double bead_mass = 5.0;
   int sort_interval = 0;
   int md_split = -1;       // -1 auto, 0 float64 springs, 1 split springs
+  int host_only = 0;       // 1: no engine; the system is only described on the host (HostSystem)
 };
+
+// Everything the engine would receive, kept on the host (host_only runs):
+// the input of a replica batch (mpcd_batch.h).
+struct HostSystem {
+  mpcd_params p{};
+  double a[3] = {0.5, 0.5, 0.5};
+  double globalt = 0.0;
+  std::vector<double> fpos, fvel;  // fluid, n x 3
+  std::vector<double> bpos, bvel;  // beads, nb x 3
+  std::vector<int> moves;
+  SpringList springs;
+  std::vector<mpcd_cilium> cilia;
+  std::vector<double> newlen, oldlen;
+};
+
+// Adds a host-described system to a replica batch as a new replica (not yet
+// admitted); throws std::runtime_error with the batch's message on failure.
+void add_to_batch(mpcd_batch* b, const HostSystem& h, long nbeads, int* replica);
 
 class Simulation {
  public:
@@ -204,6 +224,7 @@ class Simulation {
   std::unique_ptr<HostRng> rng;
   std::vector<std::unique_ptr<MDObject>> md_objects;
   mpcd_engine* eng = nullptr;
+  HostSystem host;  // host_only: what the engine would have received
   long nbeads = 0;
 
   MDObject* add_md_object(const libconfig::Setting& cfg);

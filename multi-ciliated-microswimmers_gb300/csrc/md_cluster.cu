@@ -67,15 +67,14 @@ struct PBuf {
   }
 };
 
-// Shared memory of one CTA.  nsp_max counts spring entries in the warp-sliced
-// layout (entry k of thread t of warp w at wbase[w] + 32 k + t, every warp
-// padded to its longest list), so that a warp's loads of its k-th springs
-// are consecutive words (no bank conflicts).
+// Shared memory of one CTA: nsp_max springs (CSR by slot), nbond_max entries
+// of the bond tables.
 struct ClusterLayout {
   int np, nsp_max, nbond_max;
+  int nbuf;  // position buffers: 2 (one cluster barrier per substep) or 1 (two, less shared memory)
   __host__ __device__ int max_cilia() const { return nbond_max / 2 + 1; }
   __host__ __device__ size_t bytes(int T) const {
-    size_t b = 2 * 6 * sizeof(float) * (size_t)np;           // two position buffers
+    size_t b = (size_t)nbuf * 6 * sizeof(float) * (size_t)np;  // position buffers
     b += (size_t)nsp_max * (sizeof(uint32_t) + 2 * sizeof(float));  // springs
     b += (size_t)nbond_max * 3 * sizeof(float);                      // bond tables
     b = (b + 15) & ~(size_t)15;
@@ -102,8 +101,9 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
   // carve shared memory
   unsigned char* ptr = smem;
   float* const pbase = reinterpret_cast<float*>(ptr);  // buffer b at pbase + b * 6 * np
-  auto buf = [&](int b) { return PBuf{pbase + b * 6 * np, np}; };
-  ptr += 2 * 6 * sizeof(float) * (size_t)np;
+  const int nbuf = lay.nbuf;
+  auto buf = [&](int b) { return PBuf{pbase + (nbuf == 2 ? b : 0) * 6 * np, np}; };
+  ptr += (size_t)nbuf * 6 * sizeof(float) * (size_t)np;
   uint32_t* sw = reinterpret_cast<uint32_t*>(ptr);
   float* srest = reinterpret_cast<float*>(sw + lay.nsp_max);
   float* sm2k = srest + lay.nsp_max;
@@ -126,45 +126,24 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
   const int q = threadIdx.x / kCLanes, lane = threadIdx.x % kCLanes;  // kCLanes lanes per slot
   const int slot = base + q;
   const bool valid = q < T;
-  // stage this thread's springs (CSR entries s0 + lane + kCLanes k of its
-  // slot) into the warp-sliced layout
-  int nmine = 0, ebase = 0;
-  {
-    __shared__ int wbase[33];
-    const int gs0 = valid ? m.sp_start[slot] : 0, gs1 = valid ? m.sp_start[slot + 1] : 0;
-    nmine = max(0, (gs1 - gs0 - lane + kCLanes - 1) / kCLanes);
-    const int wid = (int)(threadIdx.x >> 5), lid = (int)(threadIdx.x & 31);
-    const int W = __reduce_max_sync(0xffffffffu, nmine);
-    if (lid == 0) wbase[wid] = 32 * W;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int acc = 0;
-      const int nw = (int)(blockDim.x >> 5);
-      for (int w = 0; w < nw; ++w) {
-        const int t = wbase[w];
-        wbase[w] = acc;
-        acc += t;
-      }
-      wbase[nw] = acc;
-    }
-    __syncthreads();
-    if (wbase[blockDim.x >> 5] > lay.nsp_max) {  // layout mismatch: no springs, and say so
-      if (threadIdx.x == 0) atomicOr(a.err, kErrLayout);
-      nmine = 0;
-    }
-    ebase = wbase[wid] + lid;
-    for (int k = 0; k < nmine; ++k) {
-      const int s = gs0 + lane + kCLanes * k;
-      const int e = ebase + 32 * k;
+  // stage the tile's springs (CSR by slot)
+  const int sp0 = m.sp_start[base], sp1 = m.sp_start[base + T];
+  if (sp1 - sp0 > lay.nsp_max) {  // layout smaller than the tile needs: no springs, and say so
+    if (threadIdx.x == 0) atomicOr(a.err, kErrLayout);
+  } else {
+    for (int s = sp0 + (int)threadIdx.x; s < sp1; s += blockDim.x) {
+      const int k = s - sp0;
       const int kraw = m.sp_kind[s];
       const int kind = kraw & 3;
       // bond-table index for BOND/DIAG springs; bit 13 marks a reaction owed to a hub
       const int bl = kind >= 2 ? m.sp_ref[s] - bond0 : ((kraw & kSpringReact) ? 0x2000 : 0);
-      sw[e] = (uint32_t)m.sp_local[s] | ((uint32_t)bl << 16) | ((uint32_t)kind << 30);
-      srest[e] = (float)m.sp_rest[s];
-      sm2k[e] = (float)m.sp_m2k[s];
+      sw[k] = (uint32_t)m.sp_local[s] | ((uint32_t)bl << 16) | ((uint32_t)kind << 30);
+      srest[k] = (float)m.sp_rest[s];
+      sm2k[k] = (float)m.sp_m2k[s];
     }
   }
+  const int s0 = valid && sp1 - sp0 <= lay.nsp_max ? m.sp_start[slot] - sp0 : 0;
+  const int s1 = valid && sp1 - sp0 <= lay.nsp_max ? m.sp_start[slot + 1] - sp0 : 0;
   for (int k = threadIdx.x; k < nbond; k += blockDim.x) {
     bnew[k] = (float)m.newlen[bond0 + k];
     bold[k] = (float)m.oldlen[bond0 + k];
@@ -279,12 +258,12 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
           rz = fmaf(-dz, fac, rz);
         }
       };
-      int k = 0;
-      for (; k + 1 < nmine; k += 2) {
-        one(ebase + 32 * k, ax, ay, az);
-        one(ebase + 32 * (k + 1), bx, by, bz);
+      int s = s0 + lane;
+      for (; s + kCLanes < s1; s += 2 * kCLanes) {
+        one(s, ax, ay, az);
+        one(s + kCLanes, bx, by, bz);
       }
-      if (k < nmine) one(ebase + 32 * k, ax, ay, az);
+      if (s < s1) one(s, ax, ay, az);
       ax += bx;
       ay += by;
       az += bz;
@@ -353,6 +332,7 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
         xl[d] = __fsub_rn(lo, __fsub_rn(xh[d], sum));
       }
     }
+    if (nbuf == 1) cluster.sync();  // one buffer: every read of this substep is done
     if (primary && lane == 0) buf(cur ^ 1).put(q, xh, xl);
     cluster.sync();
     cur ^= 1;
@@ -540,7 +520,7 @@ __global__ void __launch_bounds__(1024, 1)
 
 template <int L, typename Bin>
 cudaError_t launch_cluster_l(const MDState& m, const MDStepArgs& a, const Bin& bin, cudaStream_t s) {
-  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max};
+  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max, m.cl_nbuf};
   const size_t smem = lay.bytes(m.tile);
   auto kern = k_md_cluster<L, Bin>;
   cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -568,7 +548,7 @@ cudaError_t launch_cluster(const MDState& m, const MDStepArgs& a, const Bin& bin
 }  // namespace
 
 size_t md_cluster_smem(const MDState& m) {
-  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max};
+  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max, m.cl_nbuf};
   return lay.bytes(m.tile);
 }
 
@@ -604,8 +584,8 @@ int md_cluster_feasible(const MDState& m) {
   return m.cl_lanes == 2 ? cluster_feasible_l<2>(m) : cluster_feasible_l<1>(m);
 }
 
-size_t md_cluster_batch_smem(int tile, int hmax, int nsp_max, int nbond_max) {
-  ClusterLayout lay{tile + hmax, nsp_max, nbond_max};
+size_t md_cluster_batch_smem(int tile, int hmax, int nsp_max, int nbond_max, int nbuf) {
+  ClusterLayout lay{tile + hmax, nsp_max, nbond_max, nbuf};
   return lay.bytes(tile);
 }
 
@@ -651,9 +631,10 @@ int md_cluster_batch_feasible(int lanes, int tile, int ctiles, size_t smem) {
 }
 
 int launch_md_cluster_batch(const MDState& m, const BatchTables& t, BatchCells c, const int* reps, int nreps,
-                            int ctiles, int hmax, int nsp_max, int nbond_max, cudaStream_t s, cudaError_t* st) {
+                            int ctiles, int hmax, int nsp_max, int nbond_max, int nbuf, cudaStream_t s,
+                            cudaError_t* st) {
   if (nreps <= 0) return 0;
-  ClusterLayout lay{m.tile + hmax, nsp_max, nbond_max};
+  ClusterLayout lay{m.tile + hmax, nsp_max, nbond_max, nbuf};
   const size_t smem = lay.bytes(m.tile);
   cudaLaunchAttribute attr[1];
   if (m.cl_lanes == 2) {

@@ -204,9 +204,10 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
   };
   // slot widths of a cluster layout with `lanes` threads per slot
   auto cluster_widths = [&](int lanes) {
-    // one lane per slot: short chunks (two slots per cilium bead) keep the
-    // serial spring chains short; hubs take their force from reactions
-    const int chunk = lanes == 2 ? kChunk : std::min(kChunk, 11);
+    // one lane per slot: chunks of 15 springs keep every cilium bead (up to
+    // 8 filament springs plus 6 attachment springs) on one slot, so that a
+    // cilium needs one slot per bead; hubs take their force from reactions
+    const int chunk = lanes == 2 ? kChunk : std::min(kChunk, 15);
     keep_hubs_whole = lanes == 1;
     for (long b = 0; b < nb; ++b)
       width[b] = (hub[b] && keep_hubs_whole) ? 1 : 1 + (nspr[b] > chunk ? (nspr[b] + chunk - 1) / chunk - 1 : 0);
@@ -222,7 +223,14 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
       return "invalid fixed cluster layout";
     cluster_widths(force.lanes);
     if (maxw > force.tile) return "a cilium does not fit into one MD tile of the fixed layout";
-    if (pack_cluster(force.tile) > 16) return "the MD bead set needs more than 16 tiles of the fixed layout";
+    if (pack_cluster(force.tile) > 16) {
+      // a hub whose run of beads cannot stay in one tile keeps its own spring
+      // list (helper slots) instead of reactions
+      bool any_hub = false;
+      for (long b = 0; b < nb && !any_hub; ++b) any_hub = hub[b] != 0;
+      if (any_hub && !no_react) return plan_md(in, force, allow_cluster, true, grid_f32cells, out);
+      return "the MD bead set needs more than 16 tiles of the fixed layout";
+    }
     tile = force.tile;
     out.cluster = 1;
     out.cl_lanes = force.lanes;
@@ -375,28 +383,17 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     // per-tile maxima for the cluster kernel's shared-memory layout
     std::vector<int> tb(out.ntiles, 0);
     for (int c = 0; c < ncil; ++c) tb[cil_tile[c]] += in.cil[c].rodlength;
-    // springs per tile in the kernel's warp-sliced layout: thread th = q *
-    // lanes + lane takes entries lane, lane + lanes, ... of slot q's list;
-    // every warp is padded to its longest thread list
-    const int lanes = out.cl_lanes;
-    const int nthreads = tile * lanes;
     for (int t = 0; t < out.ntiles; ++t) {
-      int entries = 0;
-      for (int w = 0; w < nthreads / 32; ++w) {
-        int W = 0;
-        for (int th = 32 * w; th < 32 * w + 32; ++th) {
-          const int q = th / lanes, lane = th % lanes;
-          const int slot = t * tile + q;
-          const int len = start[slot + 1] - start[slot];
-          W = std::max(W, std::max(0, (len - lane + lanes - 1) / lanes));
-        }
-        entries += 32 * W;
-      }
-      out.cl_nsp_max = std::max(out.cl_nsp_max, entries);
+      out.cl_nsp_max = std::max(out.cl_nsp_max, start[(t + 1) * tile] - start[t * tile]);
       out.cl_nbond_max = std::max(out.cl_nbond_max, tb[t]);
     }
     probe.cl_nsp_max = out.cl_nsp_max;
     probe.cl_nbond_max = out.cl_nbond_max;
+    probe.cl_nbuf = 2;
+    if (!md_cluster_feasible(probe)) {
+      probe.cl_nbuf = 1;  // one position buffer and a second cluster barrier per substep
+      out.cl_nbuf = 1;
+    }
     if (!md_cluster_feasible(probe)) {
       if (forced) return "the fixed cluster layout does not fit on the device";
       return plan_md(in, force, false, no_react, grid_f32cells, out);  // grid layout instead

@@ -37,7 +37,7 @@ struct MDForce {
 // Host arrays of an MDState (engine_internal.h), indices local to the box.
 struct MDPlan {
   int tile = 0, ntiles = 0, nslots = 0, hmax = 0;
-  int split = 0, cluster = 0, cl_nsp_max = 0, cl_nbond_max = 0, cl_lanes = 2;
+  int split = 0, cluster = 0, cl_nsp_max = 0, cl_nbond_max = 0, cl_lanes = 2, cl_nbuf = 2;
   std::vector<double> X, Y, Z, VX, VY, VZ;
   std::vector<int> mv, prim, nhelp, thelp, tile_react;
   std::vector<int> start, so, sl, sk, sr;

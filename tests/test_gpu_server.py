@@ -1,0 +1,139 @@
+"""Continuous batching server (include/mpcd_server.h).
+
+Requests are sim.cfg texts with a step count and a seed.  A request's
+random numbers are keyed by its own seed and step counter, so its result is
+the same whether it ran alone or while other requests were admitted,
+running and retired around it, up to the order of float additions into its
+cell sums.  That order is not reproducible even between two runs alone, and
+the dynamics amplify it (a particle within rounding of a cell face changes
+collision partners), so:
+  - over a short run (8 steps) the alone and mixed results agree: beads
+    within 1e-3, 99.9 % of the fluid positions within 1e-4, kT within 1e-4,
+    and the share of fluid velocities off by more than 1e-4 (particles in the
+    swimmer's cells, which feel its float-rounded bead velocities) is at most
+    2x (+0.5 %) that share between two runs alone;
+  - over a longer run (40 steps) the difference between the alone and the
+    mixed result is no larger than 5x (+1e-3) the difference between two runs
+    of the request alone, and kT agrees within 1e-3.
+"""
+import numpy as np
+import pytest
+
+import cilia_gpu as cg
+import simcfg
+
+pytestmark = pytest.mark.gpu
+
+
+def request_cfg(L, n_cilia, rodlength=10, seed=0):
+    return simcfg.dumps(simcfg.swimmer_config(L, radius=L / 8.0, n_cilia=n_cilia, rodlength=rodlength, seed=seed))
+
+
+def capacity(n, L=24, n_cilia=8, rodlength=10, **kw):
+    nb = 643 + 3 * n_cilia * rodlength
+    c = dict(max_replicas=n + 2, max_particles=n * (10 * L ** 3 + 8192), max_cells=n * (L ** 3 + 2048),
+             max_slots=n * (2 * nb + 1024), max_springs=n * 14 * nb, max_halo=n * (6 * nb + 4096),
+             max_cilia=n * n_cilia + 1, max_bonds=n * n_cilia * rodlength + 1)
+    c.update(kw)
+    return c
+
+
+def periodic_diff(a, b, L):
+    d = a - b
+    return d - np.round(d / float(L)) * float(L)
+
+
+def test_requests_complete_with_latency_stats():
+    srv = cg.Server(chunk_steps=10, **capacity(6))
+    ids = []
+    for k, (L, nc, steps) in enumerate([(16, 0, 30), (24, 6, 20), (16, 4, 50), (24, 0, 10), (16, 8, 40)]):
+        ids.append((srv.submit(request_cfg(L, nc, seed=k), steps, seed=100 + k), steps))
+    srv.drain(300)
+    for rid, steps in ids:
+        info = srv.wait(rid, 10)
+        assert info["state"] == cg.REQ_DONE and info["steps"] == steps and info["err"] == 0
+        assert info["t_submit"] <= info["t_admit"] <= info["t_done"]
+        assert 0.8 < info["obs"]["kT"] < 1.3
+    st = srv.stats()
+    assert st["completed"] == 5 and st["failed"] == 0
+    assert 0 < st["p50_s"] <= st["p99_s"] <= st["max_s"]
+    assert st["throughput"] > 0 and st["gpu_launches"] > 0
+    srv.close()
+
+
+def run_alone(target, steps, seed):
+    srv = cg.Server(chunk_steps=10, keep_fluid=True, **capacity(2))
+    rid = srv.submit(target, steps, seed=seed)
+    info = srv.wait(rid, 300)
+    beads = srv.result_beads(rid, info["nbeads"])
+    fluid = srv.result_fluid(rid, info["nfluid"])
+    srv.close()
+    return info, beads, fluid
+
+
+def run_in_mix(target, steps, seed):
+    mix = cg.Server(chunk_steps=7, keep_fluid=True, **capacity(6))
+    for k, (L, nc, st) in enumerate([(24, 6, 60), (16, 0, 15), (16, 8, 90)]):
+        mix.submit(request_cfg(L, nc, seed=10 + k), st, seed=500 + k)
+    rid = mix.submit(target, steps, seed=seed)  # joins a batch already running
+    mix.submit(request_cfg(24, 2, seed=20), 30, seed=600)
+    info = mix.wait(rid, 300)
+    beads = mix.result_beads(rid, info["nbeads"])
+    fluid = mix.result_fluid(rid, info["nfluid"])
+    mix.drain(300)
+    peak = mix.stats()["peak_resident"]
+    mix.close()
+    return info, beads, fluid, peak
+
+
+def test_result_same_alone_and_in_the_mix():
+    target = request_cfg(16, 5, seed=3)
+    ia, (pa, _), fa = run_alone(target, 8, 77)
+    _, _, fb = run_alone(target, 8, 77)
+    im, (pm, _), fm, peak = run_in_mix(target, 8, 77)
+    assert im["steps"] == ia["steps"] == 8 and peak >= 2
+    assert np.abs(pa - pm).max() < 1e-3
+    dp = np.abs(periodic_diff(fa[0], fm[0], 16)).max(axis=1)
+    assert np.mean(dp < 1e-4) > 0.999
+    off_mix = np.mean(np.abs(fa[1] - fm[1]).max(axis=1) > 1e-4)
+    off_rep = np.mean(np.abs(fa[1] - fb[1]).max(axis=1) > 1e-4)
+    assert off_mix <= 2 * off_rep + 0.005, (off_mix, off_rep)
+    assert abs(ia["obs"]["kT"] - im["obs"]["kT"]) < 1e-4
+
+
+def test_long_run_mix_within_the_run_to_run_spread():
+    target = request_cfg(16, 5, seed=3)
+    ia, (pa, _), _ = run_alone(target, 40, 77)
+    ib, (pb, _), _ = run_alone(target, 40, 77)
+    im, (pm, _), _, _ = run_in_mix(target, 40, 77)
+    spread = np.abs(pa - pb).max()
+    diff = np.abs(pa - pm).max()
+    assert diff < 5 * spread + 1e-3, (diff, spread)
+    assert abs(ia["obs"]["kT"] - im["obs"]["kT"]) < 1e-3
+
+
+def test_admission_respects_the_budget():
+    probe = cg.Batch.for_specs([dict(L=16, n_cilia=4, rodlength=10)])
+    r = probe.add_cfg(request_cfg(16, 4), seed=1)
+    fp = probe.footprint(r)
+    probe.close()
+    srv = cg.Server(chunk_steps=10, budget_bytes=int(2.5 * fp), **capacity(6, L=16, n_cilia=4))
+    ids = [srv.submit(request_cfg(16, 4, seed=k), 20, seed=k + 1) for k in range(5)]
+    srv.drain(300)
+    st = srv.stats()
+    assert st["completed"] == 5
+    assert st["peak_resident"] <= 2 and st["peak_resident_bytes"] <= 2.5 * fp
+    for rid in ids:
+        assert srv.info(rid)["state"] == cg.REQ_DONE
+    srv.close()
+
+
+def test_bad_request_fails_alone():
+    srv = cg.Server(chunk_steps=10, **capacity(3, L=16))
+    bad = srv.submit("sizex = ;", 10, seed=1)
+    good = srv.submit(request_cfg(16, 2), 10, seed=2)
+    with pytest.raises(cg.MpcdError):
+        srv.wait(bad, 60)
+    assert srv.info(bad)["state"] == cg.REQ_FAILED
+    assert srv.wait(good, 300)["state"] == cg.REQ_DONE
+    srv.close()
