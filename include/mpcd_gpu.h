@@ -81,6 +81,8 @@ typedef struct {
   const double* shift_next; /* [3], in (0,1): MPCD::a after shift_boxes */
   const double* gamma;      /* [ncells]; < 0 where the reference drew none */
   const double* axis;       /* [ncells][3] */
+  const double* virt;       /* [ncells][3] virtual-particle momentum of the wall-layer cells
+                               (src/libcilia/mpcd.cpp:175-198); NULL: from the generator */
 } mpcd_inject;
 
 typedef struct {

@@ -36,7 +36,7 @@ class MpcdParams(ctypes.Structure):
 
 
 class MpcdInject(ctypes.Structure):
-    _fields_ = [("shift_next", _DP), ("gamma", _DP), ("axis", _DP)]
+    _fields_ = [("shift_next", _DP), ("gamma", _DP), ("axis", _DP), ("virt", _DP)]
 
 
 class MpcdObs(ctypes.Structure):
@@ -309,12 +309,12 @@ class Engine:
     def prepare(self):
         self._ck(lib().mpcd_prepare(self._h), "prepare")
 
-    def step(self, shift_next=None, gamma=None, axis=None):
-        if shift_next is None and gamma is None and axis is None:
+    def step(self, shift_next=None, gamma=None, axis=None, virt=None):
+        if shift_next is None and gamma is None and axis is None and virt is None:
             self._ck(lib().mpcd_step(self._h, None), "step")
             return
-        keep = [_f64(shift_next), _f64(gamma), _f64(axis)]
-        inj = MpcdInject(_dp(keep[0]), _dp(keep[1]), _dp(keep[2]))
+        keep = [_f64(shift_next), _f64(gamma), _f64(axis), _f64(virt)]
+        inj = MpcdInject(_dp(keep[0]), _dp(keep[1]), _dp(keep[2]), _dp(keep[3]))
         self._ck(lib().mpcd_step(self._h, ctypes.byref(inj)), "step")
 
     def run(self, nsteps):
@@ -398,12 +398,12 @@ class Sim:
     def beads(self):
         return self.engine.beads(self.nbeads)
 
-    def next_tstep(self, shift_next=None, gamma=None, axis=None):
-        if shift_next is None and gamma is None and axis is None:
+    def next_tstep(self, shift_next=None, gamma=None, axis=None, virt=None):
+        if shift_next is None and gamma is None and axis is None and virt is None:
             self._ck(lib().cilia_sim_next_tstep(self._h, None), "next_tstep")
             return
-        keep = [_f64(shift_next), _f64(gamma), _f64(axis)]
-        inj = MpcdInject(_dp(keep[0]), _dp(keep[1]), _dp(keep[2]))
+        keep = [_f64(shift_next), _f64(gamma), _f64(axis), _f64(virt)]
+        inj = MpcdInject(_dp(keep[0]), _dp(keep[1]), _dp(keep[2]), _dp(keep[3]))
         self._ck(lib().cilia_sim_next_tstep(self._h, ctypes.byref(inj)), "next_tstep")
 
     def run(self):

@@ -47,6 +47,7 @@ struct mpcd_engine {
   uint32_t *d_count = nullptr, *d_start = nullptr, *d_rank = nullptr, *d_blocksums = nullptr;
   double* d_inj_gamma = nullptr;
   double* d_inj_axis = nullptr;
+  double* d_inj_virt = nullptr;
 
   // MD (host copies; device layout built by prepare)
   long nb = 0;
@@ -588,6 +589,7 @@ int mpcd_destroy(mpcd_engine* h) {
   cudaFree(h->d_blocksums);
   cudaFree(h->d_inj_gamma);
   cudaFree(h->d_inj_axis);
+  cudaFree(h->d_inj_virt);
   free_md(h->md);
   cudaFree(h->d_err);
   cudaFree(h->d_diss);
@@ -891,6 +893,11 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
   for (int k = 1; k < h->nsub; ++k) t_move += h->p.ststep;
   t_move += h->p.ststep;
   StepArgs s = step_args(h, h->a, a_next, t_move);
+  if (inj && inj->virt) {
+    if (!h->d_inj_virt) CK(dalloc(&h->d_inj_virt, 3 * h->ncell));
+    CK(cudaMemcpyAsync(h->d_inj_virt, inj->virt, 3 * h->ncell * 8, cudaMemcpyHostToDevice, h->stream));
+    s.inj_virt = h->d_inj_virt;
+  }
   if (inj && (inj->gamma || inj->axis)) {
     if (!h->d_inj_gamma) {
       CK(dalloc(&h->d_inj_gamma, h->ncell));

@@ -59,6 +59,7 @@ struct StepArgs {
   uint64_t step;      // index of this collision step (generator counter)
   const double* inj_gamma;  // device, or nullptr
   const double* inj_axis;   // device, or nullptr
+  const double* inj_virt;   // device [ncell][3] virtual-particle momenta (walls), or nullptr
   unsigned* err;
   double* diss;       // accumulated dissipated energy (float64)
   // float copies for the split-precision kernels (no conversions per thread)

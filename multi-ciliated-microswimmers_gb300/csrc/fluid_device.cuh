@@ -72,14 +72,33 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float4 v) {
 // random axis, written as three float4 rows (A row, b) of v' = A v + b.  The
 // cell's sum m v^2 before the collision goes into ldiss.  `cid` keys the
 // generator (the cell's index within its own box).
-__device__ __forceinline__ void cell_map_f32(const float4 s, const uint32_t w, const uint32_t cid, const uint64_t seed,
+__device__ __forceinline__ void cell_map_f32(const float4 s0, const uint32_t w, const uint32_t cid, const uint64_t seed,
                                              const uint64_t step, const float mb, const double* inj_gamma,
                                              const double* inj_axis, float4* par_out, float& ldiss, unsigned& errbits,
-                                             bool& gfail) {
+                                             bool& gfail, const bool wall_cell = false,
+                                             const double* inj_virt = nullptr) {
   const float ca = (float)kCosAlpha, sa = (float)kSinAlpha, oc = 1.0f - (float)kCosAlpha;
   const int nf = cnt_fluid(w), nb = cnt_beads(w);
-  const int num = nf + nb;
-  const float M = (float)nf + (float)nb * mb;
+  int num = nf + nb;
+  float M = (float)nf + (float)nb * mb;
+  float4 s = s0;
+  if (wall_cell && num < 10) {  // virtual particles up to rho = 10 (src/libcilia/mpcd.cpp:175-198)
+    const int dm = 10 - num;
+    double pv[3];
+    if (inj_virt) {
+      pv[0] = inj_virt[3 * cid];
+      pv[1] = inj_virt[3 * cid + 1];
+      pv[2] = inj_virt[3 * cid + 2];
+    } else {
+      virtual_momentum(seed, step, cid, dm, pv);
+    }
+    s.x += (float)pv[0];
+    s.y += (float)pv[1];
+    s.z += (float)pv[2];
+    s.w += (float)((pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2]) / dm);
+    M += (float)dm;
+    num += dm;
+  }
   const float inv = 1.0f / M;
   const float ux = s.x * inv, uy = s.y * inv, uz = s.z * inv;
   const float erel = s.w - (ux * s.x + uy * s.y + uz * s.z);

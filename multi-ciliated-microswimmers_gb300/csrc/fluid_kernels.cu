@@ -74,8 +74,25 @@ __device__ __forceinline__ void rewrap(double& o, int& i, int L, unsigned& bad) 
 __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, const StepArgs& a, double* A,
                                               double* b, double& ldiss, unsigned& errbits, bool& gfail) {
   const int nf = cnt_fluid(w), nb = cnt_beads(w);
-  const int num = nf + nb;
-  const double M = (double)nf + (double)nb * a.bead_mass;
+  int num = nf + nb;
+  double M = (double)nf + (double)nb * a.bead_mass;
+  if (a.walls && num < 10 && wall_layer_cell(a.box, cid)) {  // virtual particles up to rho = 10
+    const int dm = 10 - num;
+    double pv[3];
+    if (a.inj_virt) {
+      pv[0] = a.inj_virt[3 * cid];
+      pv[1] = a.inj_virt[3 * cid + 1];
+      pv[2] = a.inj_virt[3 * cid + 2];
+    } else {
+      virtual_momentum(a.seed, a.step, (uint32_t)cid, dm, pv);
+    }
+    s.x += pv[0];
+    s.y += pv[1];
+    s.z += pv[2];
+    s.w += (pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2]) / dm;
+    M += dm;
+    num += dm;
+  }
   const double inv = 1.0 / M;
   const double ux = s.x * inv, uy = s.y * inv, uz = s.z * inv;
   const double erel = s.w - (ux * s.x + uy * s.y + uz * s.z);  // K - M u^2
@@ -518,7 +535,7 @@ __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
     c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
     c.cnt[cid] = 0u;
     cell_map_f32(s, w, (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 3 * cid, ldiss,
-                 errbits, gfail);
+                 errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt);
   }
   if (gfail) errbits |= kErrGammaLoop;
   if (errbits) atomicOr(a.err, errbits);

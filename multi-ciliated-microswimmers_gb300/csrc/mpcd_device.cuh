@@ -93,6 +93,22 @@ __device__ __forceinline__ float gamma_mt(int nc, uint64_t seed, uint64_t step, 
   return d;
 }
 
+// Virtual particles of a wall-layer cell (src/libcilia/mpcd.cpp:175-198): dm
+// particles of mass 1 at kT = 1 enter the cell's sums as one momentum vector
+// with components sqrt(dm) N(0,1); the normals come from one counter block of
+// the wall stream by Box-Muller (both branches of the first pair).
+__device__ __forceinline__ void virtual_momentum(uint64_t seed, uint64_t step, uint32_t cell, int dm, double* p) {
+  const u32x4 r = draw4(seed, step, kStreamWall, cell, 0u);
+  const double r1 = sqrt(-2.0 * log(u01_dbl(r.x))), r3 = sqrt(-2.0 * log(u01_dbl(r.z)));
+  double s2, c2;
+  sincospi(2.0 * u01_dbl(r.y), &s2, &c2);
+  const double c4 = cospi(2.0 * u01_dbl(r.w));
+  const double sd = sqrt((double)dm);
+  p[0] = sd * r1 * c2;
+  p[1] = sd * r1 * s2;
+  p[2] = sd * r3 * c4;
+}
+
 // ---------------------------------------------------------------- cells ---
 // A particle's cell is packed as ix | iy << 10 | iz << 20 (edges up to 1024).
 MPCD_HD uint32_t pack_cell(int ix, int iy, int iz) { return (uint32_t)ix | ((uint32_t)iy << 10) | ((uint32_t)iz << 20); }
@@ -125,6 +141,14 @@ MPCD_HD long unwrapped_cell(const Box& b, const double* a, double x, double y, d
   const int cz = unwrapped_cell_axis(z, a[2], b.L[2]);
   if (cx < 0 || cy < 0 || cz < 0) return -1;
   return cx + (long)b.L[0] * (cy + (long)b.L[1] * cz);
+}
+
+// A cell of the bottom or top layer in the reference's wall test
+// (src/libcilia/mpcd.cpp:177-178; strict `>` at the top, so the first cell of
+// the top layer is not one).
+MPCD_HD bool wall_layer_cell(const Box& b, long cid) {
+  const long layer = (long)b.L[0] * b.L[1];
+  return cid < layer || cid > layer * (b.L[2] - 1);
 }
 
 // Count word of a cell: fluid particles in the low 16 bits, beads in the high.

@@ -132,6 +132,9 @@ struct orc_sim {
   long* cstart;
   long* members;
   double* l_energy;
+  /* boundaries and body force (-DNOSLIP / -DSLIP, -DFLUID_FLOW_G in the reference) */
+  int walls;            /* 0 periodic, 1 no-slip, 2 slip walls at z = 0 and z = Lz - 1 */
+  double gravity, omega;
 };
 
 /* ---------------------------------------------------------------- setup -- */
@@ -612,7 +615,7 @@ static inline double* vel_of(orc_sim* s, long m, double* mass) {
 /* MPCD::next_tstep for one cell (src/libcilia/mpcd.cpp:149-246) with the
  * rotation matrix of generate_collision_matrix (mpcd.cpp:269-295). */
 static int collide_cell(orc_sim* s, long cid, mt_t* g, const double* inj_gamma, const double* inj_axis,
-                        double* rec_gamma, double* rec_axis) {
+                        const double* inj_virt, double* rec_gamma, double* rec_axis, double* rec_virt) {
   const double calpha = -0.6427876, salpha = 0.76604444; /* mpcd.h:74-75 */
   double ux = 0.0, uy = 0.0, uz = 0.0, le = 0.0;
   int num = 0, masse = 0;
@@ -629,6 +632,24 @@ static int collide_cell(orc_sim* s, long cid, mt_t* g, const double* inj_gamma, 
   num = (int)(b1 - b0);
   int err = 0;
   if (num > 0) {
+    /* wall layers: virtual particles fill a cell up to rho = 10 with momentum
+       N(0, sqrt(dm kT)) per component, drawn before the cell's Gamma variate
+       (src/libcilia/mpcd.cpp:175-198; the top-layer test is a strict `>`, so
+       the first top-layer cell takes none) */
+    const long layer = (long)s->L[0] * s->L[1];
+    if (s->walls && (cid < layer || cid > layer * (s->L[2] - 1)) && num < 10) {
+      const int dm = 10 - num;
+      double pv[3];
+      for (int q = 0; q < 3; ++q) pv[q] = inj_virt ? inj_virt[3 * cid + q] : sqrt((double)dm * 1.0) * mt_normal(g);
+      if (rec_virt)
+        for (int q = 0; q < 3; ++q) rec_virt[3 * cid + q] = pv[q];
+      ux += pv[0];
+      uy += pv[1];
+      uz += pv[2];
+      masse += dm;
+      num += dm;
+      le += (pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2]) / dm;
+    }
     ux /= masse;
     uy /= masse;
     uz /= masse;
@@ -689,12 +710,12 @@ static int collide_cell(orc_sim* s, long cid, mt_t* g, const double* inj_gamma, 
   return err;
 }
 
-static int collide(orc_sim* s, const double* inj_gamma, const double* inj_axis, double* rec_gamma,
-                   double* rec_axis) {
+static int collide(orc_sim* s, const double* inj_gamma, const double* inj_axis, const double* inj_virt,
+                   double* rec_gamma, double* rec_axis, double* rec_virt) {
   int err = 0;
   if (s->threads <= 1) {
     for (long c = 0; c < s->ncell; ++c)
-      err |= collide_cell(s, c, &s->rng, inj_gamma, inj_axis, rec_gamma, rec_axis);
+      err |= collide_cell(s, c, &s->rng, inj_gamma, inj_axis, inj_virt, rec_gamma, rec_axis, rec_virt);
   } else {
 #pragma omp parallel num_threads(s->threads) reduction(| : err)
     {
@@ -704,7 +725,7 @@ static int collide(orc_sim* s, const double* inj_gamma, const double* inj_axis, 
 #endif
 #pragma omp for schedule(static)
       for (long c = 0; c < s->ncell; ++c)
-        err |= collide_cell(s, c, &s->trng[tid], inj_gamma, inj_axis, rec_gamma, rec_axis);
+        err |= collide_cell(s, c, &s->trng[tid], inj_gamma, inj_axis, inj_virt, rec_gamma, rec_axis, rec_virt);
     }
   }
   long double tot = 0.0L;
@@ -912,17 +933,62 @@ static void switch_logic(orc_sim* s) {
 }
 
 /* ----------------------------------------------------------------- step -- */
+/* MPCD::move (src/libcilia/mpcd.cpp:340-376): streaming, then bounce-back at
+ * the walls (vwx = vwy = 0); Fluid::move's body force (fluid.cpp:156-158) */
 static void stream_fluid(orc_sim* s) {
+  const double ztop = (double)(s->L[2] - 1);
+  const double kick = s->gravity != 0.0 ? s->gravity * cos(s->globalt * s->omega) * s->tstep : 0.0;
 #pragma omp parallel for schedule(static) num_threads(s->threads) if (s->threads > 1)
-  for (long i = 0; i < s->n; ++i)
-    for (int q = 0; q < 3; ++q) s->pos[3 * i + q] += s->vel[3 * i + q] * s->tstep;
+  for (long i = 0; i < s->n; ++i) {
+    double* x = s->pos + 3 * i;
+    double* v = s->vel + 3 * i;
+    for (int q = 0; q < 3; ++q) x[q] += v[q] * s->tstep;
+    if (s->walls) {
+      if (x[2] > ztop) {
+        if (s->walls == 1) {
+          const double t2 = (x[2] - ztop) / v[2];
+          v[0] = -v[0];
+          v[1] = -v[1];
+          v[2] = -v[2];
+          x[0] += 2.0 * t2 * v[0];
+          x[1] += 2.0 * t2 * v[1];
+          x[2] += 2.0 * t2 * v[2];
+        } else {
+          v[2] = -v[2];
+          x[2] = -x[2] + ztop * 2.0;
+        }
+      }
+      if (x[2] < 0) {
+        const double t2 = x[2] / v[2];
+        v[0] = -v[0];
+        v[1] = -v[1];
+        v[2] = -v[2];
+        x[0] += v[0] * 2.0 * t2;
+        x[1] += v[1] * 2.0 * t2;
+        x[2] += v[2] * 2.0 * t2;
+      }
+    }
+    if (kick != 0.0) v[0] += kick;
+  }
+}
+
+void orc_set_walls(orc_sim* s, int walls) { s->walls = walls; }
+void orc_set_gravity(orc_sim* s, double g, double omega) {
+  s->gravity = g;
+  s->omega = omega;
 }
 
 /* Simulation::next_tstep (src/simulation.cpp:217-265) */
 int orc_step(orc_sim* s, const double* inj_shift_next, const double* inj_gamma, const double* inj_axis,
              double* rec_shift_next, double* rec_gamma, double* rec_axis) {
+  return orc_step_walls(s, inj_shift_next, inj_gamma, inj_axis, NULL, rec_shift_next, rec_gamma, rec_axis, NULL);
+}
+
+int orc_step_walls(orc_sim* s, const double* inj_shift_next, const double* inj_gamma, const double* inj_axis,
+                   const double* inj_virt, double* rec_shift_next, double* rec_gamma, double* rec_axis,
+                   double* rec_virt) {
   const int n = (int)((s->tstep + 0.00000001) / s->ststep);
-  int err = collide(s, inj_gamma, inj_axis, rec_gamma, rec_axis);
+  int err = collide(s, inj_gamma, inj_axis, inj_virt, rec_gamma, rec_axis, rec_virt);
   if (s->nb > 0) {
     recalc_forces(s);
     md_kick_drift(s, s->ststep / 2.0);

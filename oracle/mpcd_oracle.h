@@ -78,6 +78,15 @@ void orc_init_bins(orc_sim* s);
  * for a cell that needs one. */
 int orc_step(orc_sim* s, const double* inj_shift_next, const double* inj_gamma,
              const double* inj_axis, double* rec_shift_next, double* rec_gamma, double* rec_axis);
+/* the same with walls: inj_virt / rec_virt hold the virtual-particle momentum
+ * of every wall-layer cell that took virtual particles ([ncell][3]) */
+int orc_step_walls(orc_sim* s, const double* inj_shift_next, const double* inj_gamma, const double* inj_axis,
+                   const double* inj_virt, double* rec_shift_next, double* rec_gamma, double* rec_axis,
+                   double* rec_virt);
+/* boundaries (0 periodic, 1 no-slip, 2 slip walls along z; src/libcilia/mpcd.cpp:175-198,
+ * 346-376) and the body force g cos(omega t) along x (src/libcilia/fluid.cpp:156-158) */
+void orc_set_walls(orc_sim* s, int walls);
+void orc_set_gravity(orc_sim* s, double g, double omega);
 double orc_diss_energy(const orc_sim* s);
 void orc_reset_diss(orc_sim* s);
 

@@ -76,6 +76,10 @@ def lib():
         L.orc_clami_springs.argtypes = [_P, _I, _DP, _I]
         L.orc_step.restype = _I
         L.orc_step.argtypes = [_P, _DP, _DP, _DP, _DP, _DP, _DP]
+        L.orc_step_walls.restype = _I
+        L.orc_step_walls.argtypes = [_P, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP]
+        L.orc_set_walls.argtypes = [_P, _I]
+        L.orc_set_gravity.argtypes = [_P, _D, _D]
         L.orc_diss_energy.restype = _D
         L.orc_diss_energy.argtypes = [_P]
         L.orc_set_threads.argtypes = [_P, _I]
@@ -225,20 +229,31 @@ class OracleSim:
         lib().orc_init_bins(self._h)
 
     # --- stepping
-    def step(self, shift_next=None, gamma=None, axis=None, record=False):
-        rs = rg = ra = None
+    def set_walls(self, walls):
+        """0 periodic, 1 no-slip, 2 slip walls at z = 0 and z = Lz - 1."""
+        lib().orc_set_walls(self._h, int(walls))
+
+    def set_gravity(self, g, omega=0.0):
+        lib().orc_set_gravity(self._h, float(g), float(omega))
+
+    def step(self, shift_next=None, gamma=None, axis=None, record=False, virt=None):
+        """One MPC step; with record=True returns (shift, gamma, axis, virt) as drawn."""
+        rs = rg = ra = rv = None
         if record:
             rs = np.zeros(3)
             rg = np.full(self.ncell, -2.0)
             ra = np.zeros((self.ncell, 3))
+            rv = np.zeros((self.ncell, 3))
         sn = None if shift_next is None else _f64(shift_next)
         g = None if gamma is None else _f64(gamma)
         ax = None if axis is None else _f64(axis)
-        err = lib().orc_step(self._h, _ptr(sn), _ptr(g), _ptr(ax), _ptr(rs), _ptr(rg), _ptr(ra))
+        vv = None if virt is None else _f64(virt)
+        err = lib().orc_step_walls(self._h, _ptr(sn), _ptr(g), _ptr(ax), _ptr(vv), _ptr(rs), _ptr(rg), _ptr(ra),
+                                   _ptr(rv))
         if err:
             raise RuntimeError("oracle step: injected gamma missing for a thermostatted cell")
         if record:
-            return rs, rg, ra
+            return rs, rg, ra, rv
         return None
 
     def diss_energy(self):

@@ -17,7 +17,8 @@
 //       through Simulation::next_tstep (src/simulation.cpp:217-265).  Before
 //       each step it replays the collision's random draws on a clone of the
 //       generator, in the consumption order of src/libcilia/mpcd.cpp:148-212, to
-//       record the per-cell Gamma variate and rotation axis, and checks
+//       record the per-cell Gamma variate and rotation axis (and, in the walls
+//       build, the virtual-particle momentum of wall-layer cells), and checks
 //       afterwards that the real step consumed exactly those draws.  It writes
 //       raw little-endian float64 arrays plus index.txt into <outdir>.
 #include <omp.h>
@@ -90,7 +91,7 @@ bool same_state(MTRand& a, MTRand& b) {
 // randi[0].  gamma[c] = Gamma variate, -1 if the cell was not thermostatted
 // (E_rel <= 0 or N_c <= 1), -2 if the cell was empty.  axis[c] = rotation axis.
 void replay_collision(Simulation& sim, MTRand& clone, std::vector<double>& gamma,
-                      std::vector<double>& axis) {
+                      std::vector<double>& axis, std::vector<double>& virt) {
   MPCD& m = sim.mpcd;
   MTRand* orig = randi[0];
   MTRand::uint32 st[MTRand::SAVE];
@@ -100,6 +101,7 @@ void replay_collision(Simulation& sim, MTRand& clone, std::vector<double>& gamma
   const int ncell = m.numberofboxes;
   gamma.assign(ncell, -2.0);
   axis.assign(3 * (size_t)ncell, 0.0);
+  virt.assign(3 * (size_t)ncell, 0.0);
   for (int cid = 0; cid < ncell; ++cid) {
     double ux = 0, uy = 0, uz = 0, le = 0;
     int num = 0, masse = 0;
@@ -114,6 +116,23 @@ void replay_collision(Simulation& sim, MTRand& clone, std::vector<double>& gamma
     }
     num += m.boxes[0][cid].size();
     if (num > 0) {
+#if defined(SLIP) || defined(NOSLIP)
+      // wall layers: virtual particles, drawn before the Gamma variate (mpcd.cpp:175-198)
+      if ((cid < m.size[0] * m.size[1]) or (cid > m.size[0] * m.size[1] * (m.size[2] - 1))) {
+        if (num < MPCD::rho) {
+          const int dm = MPCD::rho - num;
+          for (int q = 0; q < 3; ++q) virt[3 * cid + q] = sqrt(dm * MPCD::temp) * normalrand();
+          ux += virt[3 * cid + 0];
+          uy += virt[3 * cid + 1];
+          uz += virt[3 * cid + 2];
+          masse += dm;
+          num += dm;
+          le += (virt[3 * cid] * virt[3 * cid] + virt[3 * cid + 1] * virt[3 * cid + 1] +
+                 virt[3 * cid + 2] * virt[3 * cid + 2]) /
+                dm;
+        }
+      }
+#endif
       ux /= masse;
       uy /= masse;
       uz /= masse;
@@ -226,8 +245,8 @@ int run_mode(int argc, char** argv) {
   int ok = 1;
   MTRand clone(1u);
   for (int s = 1; s <= nsteps; ++s) {
-    std::vector<double> gamma, axis;
-    replay_collision(*sim, clone, gamma, axis);
+    std::vector<double> gamma, axis, virt;
+    replay_collision(*sim, clone, gamma, axis, virt);
     sim->next_tstep();
     // shift_boxes draws three more values after the collision (mpcd.cpp:249-253)
     clone.randDblExc();
@@ -237,6 +256,9 @@ int run_mode(int argc, char** argv) {
     const long nc = (long)gamma.size();
     out.put("gamma_" + std::to_string(s), gamma, {nc});
     out.put("axis_" + std::to_string(s), axis, {nc, 3});
+#if defined(SLIP) || defined(NOSLIP)
+    out.put("virt_" + std::to_string(s), virt, {nc, 3});
+#endif
     double a[3] = {sim->mpcd.a[0], sim->mpcd.a[1], sim->mpcd.a[2]};
     out.put("shift_" + std::to_string(s), a, {3});
     if (std::find(dumps.begin(), dumps.end(), s) != dumps.end())

@@ -6,7 +6,8 @@ tests/golden/cases/ and packs its outputs into compressed .npz files:
 
   <case>.npz   step0_* initial state, gamma_k / axis_k (per-cell Gamma variate
                and rotation axis the reference drew in step k), shift_k (grid
-               shift after step k), stepK_* dumped states, replay_ok.
+               shift after step k), stepK_* dumped states, replay_ok; the
+               walls case also virt_k (virtual-particle momentum per cell).
   mt.npz       MT19937 outputs of the reference's MTRand for a few seeds and
                rgamma(Nc) samples (src/libcilia/mpcd.cpp:13-43).
 
@@ -24,21 +25,24 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
+# the same harness built with -DNOSLIP -DFLUID_FLOW_G=0.02 (walls along z, body force along x)
+HARNESS_WALLS = os.path.join(REPO, "oracle", "_ref", "ref_harness_walls")
 
-# case name: (seed, steps, ststep, dump list)
+# case name: (seed, steps, ststep, dump list, harness)
 CASES = {
-    "fluid4": (11, 5, 0.002, "1,5"),
-    "fluid8": (7, 3, 0.002, "3"),
-    "clami10": (3, 4, 0.002, "4"),
-    "objects8": (3, 4, 0.002, "4"),
+    "fluid4": (11, 5, 0.002, "1,5", HARNESS),
+    "fluid8": (7, 3, 0.002, "3", HARNESS),
+    "clami10": (3, 4, 0.002, "4", HARNESS),
+    "objects8": (3, 4, 0.002, "4", HARNESS),
+    "walls8": (9, 5, 0.002, "1,5", HARNESS_WALLS),
 }
 
 
-def run_case(name, seed, steps, ststep, dumps):
+def run_case(name, seed, steps, ststep, dumps, harness=HARNESS):
     cfg = os.path.join(HERE, "cases", name + ".cfg")
     with tempfile.TemporaryDirectory() as tmp:
         out = os.path.join(tmp, "out")
-        subprocess.run([HARNESS, "run", cfg, out, str(seed), str(steps), repr(ststep), dumps],
+        subprocess.run([harness, "run", cfg, out, str(seed), str(steps), repr(ststep), dumps],
                        check=True, stdout=subprocess.DEVNULL)
         arrays = {}
         with open(os.path.join(out, "index.txt")) as f:
@@ -63,13 +67,18 @@ def run_mt():
 
 
 def main():
+    """python make_golden.py [case ...]: every case (and mt.npz), or the named ones."""
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: make -C oracle ref")
-    for name, (seed, steps, ststep, dumps) in CASES.items():
-        a = run_case(name, seed, steps, ststep, dumps)
+    names = sys.argv[1:] or list(CASES) + ["mt"]
+    for name in names:
+        if name == "mt":
+            run_mt()
+            print("mt.npz written")
+            continue
+        seed, steps, ststep, dumps, harness = CASES[name]
+        a = run_case(name, seed, steps, ststep, dumps, harness)
         print(name, "arrays:", len(a), "replay_ok:", a["replay_ok"][0])
-    run_mt()
-    print("mt.npz written")
 
 
 if __name__ == "__main__":

@@ -102,7 +102,7 @@ def test_fluid_matches_oracle_larger_and_ragged(L):
     e.set_fluid(p0, v0)
     e.shift = o.shift
     for _ in range(6):
-        rs, rg, ra = o.step(record=True)
+        rs, rg, ra, _ = o.step(record=True)
         e.step(rs, rg, ra)
     p, v = e.fluid()
     po, vo = o.fluid()
@@ -140,7 +140,7 @@ def test_empty_and_sparse_cells():
     e.set_fluid(pos, vel)
     e.shift = o.shift
     for _ in range(4):
-        rs, rg, ra = o.step(record=True)
+        rs, rg, ra, _ = o.step(record=True)
         e.step(rs, rg, ra)
     p, v = e.fluid()
     po, vo = o.fluid()

@@ -1,0 +1,135 @@
+"""No-slip walls along z with virtual particles and a body force along x
+(the reference's -DNOSLIP -DFLUID_FLOW_G build: src/libcilia/mpcd.cpp:175-198,
+346-376, src/libcilia/fluid.cpp:156-158), against the fixture the reference
+itself produced (tests/golden/walls8.npz, body force 0.02) and, for the shear
+viscosity of a Poiseuille flow, against the C oracle.
+
+Tolerances: float64 path as the other parity tests (positions 1e-10,
+velocities 1e-9 after 5 injected steps); float32 split path 99.5 % of the
+particles within 2e-4 (a bounce-back turns the rounding of the wall-crossing
+time into a position change, so a few more particles than in the periodic
+case stray); the kinetic temperature of a free run with walls sits above 1
+in the reference's own arithmetic (about 1.05 - 1.07 for an 8 x 8 x 12
+channel), so it is compared with the oracle's within 0.03; Poiseuille
+viscosity (fit of the time-averaged velocity profile) within 8 % of the
+oracle's, the statistical error of runs of this length being about 3 %.
+"""
+import numpy as np
+import pytest
+
+import cilia_gpu as cg
+from conftest import golden
+from oracle import OracleSim
+
+pytestmark = pytest.mark.gpu
+
+
+def periodic_diff(a, b, L):
+    d = a - b
+    L = np.asarray(L, dtype=float)
+    return d - np.round(d / L) * L
+
+
+def run_walls_golden(precision):
+    g = golden("walls8")
+    L = (8, 8, 8)
+    e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=precision, walls=cg.WALLS_NOSLIP, gravity=0.02, omega=0.0)
+    e.set_fluid(g["step0_fluid_pos"], g["step0_fluid_vel"])
+    e.shift = g["shift_0"]
+    out = {}
+    for k in range(1, 6):
+        e.step(g[f"shift_{k}"], g[f"gamma_{k}"], g[f"axis_{k}"], g[f"virt_{k}"])
+        if f"step{k}_fluid_pos" in g:
+            out[k] = e.fluid()
+    return g, L, e, out
+
+
+def test_walls_match_reference_golden():
+    g, L, e, out = run_walls_golden(cg.MPCD_FP64)
+    for k, (p, v) in out.items():
+        assert np.abs(periodic_diff(p, g[f"step{k}_fluid_pos"], L)).max() < 1e-10
+        assert np.abs(v - g[f"step{k}_fluid_vel"]).max() < 1e-9
+    obs = e.observables()
+    ref = g["step5_meta"][1]
+    assert abs(obs["diss_energy"] - ref) < 1e-8 * max(1.0, abs(ref))
+
+
+def test_walls_fp32_tracks_reference_golden():
+    g, L, e, out = run_walls_golden(cg.MPCD_FP32)
+    p, v = out[5]
+    dp = np.abs(periodic_diff(p, g["step5_fluid_pos"], L)).max(axis=1)
+    dv = np.abs(v - g["step5_fluid_vel"]).max(axis=1)
+    assert np.mean(dp < 2e-4) > 0.995
+    assert np.mean(dv < 2e-4) > 0.995
+
+
+@pytest.mark.parametrize("precision", [cg.MPCD_FP64, cg.MPCD_FP32])
+def test_walls_free_run_keeps_the_channel(precision):
+    L = (8, 8, 12)
+    o = OracleSim(L, tstep=0.1, ststep=0.002, seed=12)
+    o.init_shift()
+    o.fluid_create()
+    p0, v0 = o.fluid()
+    e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=precision, walls=cg.WALLS_NOSLIP, seed=5)
+    e.set_fluid(p0, v0)
+    e.run(80)
+    p, v = e.fluid()
+    assert p[:, 2].min() >= 0.0 and p[:, 2].max() <= L[2] - 1 + 1e-6
+    o.set_walls(1)
+    o.set_threads(4)
+    o.init_bins()
+    for _ in range(80):
+        o.step()
+    kt_gpu, kt_orc = e.observables()["kT"], o.observables()["kT"]
+    assert 1.0 < kt_orc < 1.12 and abs(kt_gpu - kt_orc) < 0.03, (kt_gpu, kt_orc)
+
+
+def poiseuille_viscosity(profile, g, rho=10.0, zmin=1.5, zmax=None):
+    """eta from the curvature of a fitted parabola: rho g + eta v'' = 0."""
+    z = np.arange(len(profile)) + 0.5
+    zmax = zmax if zmax is not None else len(profile) - 1.5
+    sel = (z > zmin) & (z < zmax)
+    c2 = np.polyfit(z[sel], profile[sel], 2)[0]
+    return -rho * g / (2.0 * c2)
+
+
+def test_poiseuille_viscosity_matches_oracle():
+    L = (8, 8, 14)
+    grav, warm, samples, every = 0.01, 600, 300, 5
+    nbin = L[2] - 1
+    # GPU (float32 split: the production path for long runs)
+    o = OracleSim(L, tstep=0.1, ststep=0.002, seed=21)
+    o.init_shift()
+    o.fluid_create()
+    p0, v0 = o.fluid()
+    e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=cg.MPCD_FP32, walls=cg.WALLS_NOSLIP, gravity=grav, seed=9)
+    e.set_fluid(p0, v0)
+    e.run(warm)
+    prof = np.zeros(nbin)
+    cnt = np.zeros(nbin)
+    for _ in range(samples):
+        e.run(every)
+        p, v = e.fluid()
+        b = np.clip(p[:, 2].astype(int), 0, nbin - 1)
+        prof += np.bincount(b, weights=v[:, 0], minlength=nbin)
+        cnt += np.bincount(b, minlength=nbin)
+    eta_gpu = poiseuille_viscosity(prof / cnt, grav)
+    # oracle, same set-up and length
+    o.set_walls(1)
+    o.set_gravity(grav, 0.0)
+    o.set_threads(8)
+    o.init_bins()
+    for _ in range(warm):
+        o.step()
+    prof[:] = 0
+    cnt[:] = 0
+    for _ in range(samples):
+        for _ in range(every):
+            o.step()
+        p, v = o.fluid()
+        b = np.clip(p[:, 2].astype(int), 0, nbin - 1)
+        prof += np.bincount(b, weights=v[:, 0], minlength=nbin)
+        cnt += np.bincount(b, minlength=nbin)
+    eta_orc = poiseuille_viscosity(prof / cnt, grav)
+    assert 2.0 < eta_orc < 20.0
+    assert abs(eta_gpu - eta_orc) < 0.08 * eta_orc, (eta_gpu, eta_orc)

@@ -7,7 +7,9 @@ import simcfg
 from conftest import GOLDEN, golden
 from oracle import OracleSim, build_from_cfg
 
-CASES = ["fluid4", "fluid8", "clami10", "objects8"]
+CASES = ["fluid4", "fluid8", "clami10", "objects8", "walls8"]
+# cases built with -DNOSLIP -DFLUID_FLOW_G=0.02 in the reference harness: (walls, gravity)
+WALLS = {"walls8": (1, 0.02)}
 
 
 def test_mt19937_matches_reference():
@@ -46,7 +48,11 @@ def _build(case):
     g = golden(case)
     seed, steps, ststep = g["params"]
     cfg = simcfg.load(f"{GOLDEN}/cases/{case}.cfg")
-    return g, cfg, build_from_cfg(cfg, int(seed), float(ststep)), int(steps)
+    s = build_from_cfg(cfg, int(seed), float(ststep))
+    if case in WALLS:
+        s.set_walls(WALLS[case][0])
+        s.set_gravity(WALLS[case][1], float(cfg["omega"]))
+    return g, cfg, s, int(steps)
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -62,7 +68,9 @@ def test_oracle_free_run_matches_reference(case):
     assert np.array_equal(bp, rp), "MD geometry must be bitwise identical"
     np.testing.assert_array_equal(s.shift, g["shift_0"])
     for k in range(1, steps + 1):
-        rs, rg, ra = s.step(record=True)
+        rs, rg, ra, rv = s.step(record=True)
+        if f"virt_{k}" in g:
+            np.testing.assert_allclose(rv, g[f"virt_{k}"], rtol=0, atol=1e-14)
         np.testing.assert_array_equal(rg, g[f"gamma_{k}"])
         np.testing.assert_array_equal(rs, g[f"shift_{k}"])
         np.testing.assert_allclose(ra, g[f"axis_{k}"], rtol=0, atol=1e-15)
@@ -81,12 +89,12 @@ def test_oracle_free_run_matches_reference(case):
     assert abs(s.diss_energy() - g[f"step{steps}_meta"][1]) <= 1e-9 * max(1.0, abs(g[f"step{steps}_meta"][1]))
 
 
-@pytest.mark.parametrize("case", ["fluid8", "clami10"])
+@pytest.mark.parametrize("case", ["fluid8", "clami10", "walls8"])
 def test_oracle_injected_run_matches_reference(case):
-    """Inject mode: the recorded shift / Gamma / axis reproduce the states."""
+    """Inject mode: the recorded shift / Gamma / axis (/ virtual momenta) reproduce the states."""
     g, cfg, s, steps = _build(case)
     for k in range(1, steps + 1):
-        s.step(shift_next=g[f"shift_{k}"], gamma=g[f"gamma_{k}"], axis=g[f"axis_{k}"])
+        s.step(shift_next=g[f"shift_{k}"], gamma=g[f"gamma_{k}"], axis=g[f"axis_{k}"], virt=g.get(f"virt_{k}"))
     p, v = s.fluid()
     np.testing.assert_allclose(p, g[f"step{steps}_fluid_pos"], rtol=0, atol=1e-11)
     np.testing.assert_allclose(v, g[f"step{steps}_fluid_vel"], rtol=0, atol=1e-10)
