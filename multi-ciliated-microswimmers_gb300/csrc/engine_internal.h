@@ -70,6 +70,12 @@ struct StepArgs {
 // spring kind flag: the spring's force, negated, is also owed to its other
 // bead (a hub whose own list was dropped); only in the cluster layout
 constexpr int kSpringReact = 8;
+// Spring groups of the cluster layout, the order in which the planner sorts
+// every slot's list: CONST, CONST owed to a hub, GUARDED, BOND, DIAG.
+__host__ __device__ inline int spring_group(int kraw) {
+  const int kind = kraw & 3;
+  return kind == 0 ? ((kraw & kSpringReact) ? 1 : 0) : kind + 1;
+}
 int md_max_coresident_blocks(const struct MDState& m, int f32cells);
 int md_cluster_feasible(const struct MDState& m);
 

@@ -46,36 +46,45 @@ __device__ float cl_cilium_length(const float4 cp, int i, float midpnt, float ol
 }
 
 // one position buffer: six float arrays of length np (hi x,y,z then lo x,y,z)
+// One position buffer of np beads: (hi x, hi y, hi z, lo x) as float4 and
+// (lo y, lo z) as float2, so that a neighbour costs two shared loads.
 struct PBuf {
-  float* p;
-  int np;
-  __device__ float* hx() const { return p; }
+  float4* p4;
+  float2* p2;
   __device__ void put(int i, const float* h, const float* l) const {
-    p[i] = h[0];
-    p[np + i] = h[1];
-    p[2 * np + i] = h[2];
-    p[3 * np + i] = l[0];
-    p[4 * np + i] = l[1];
-    p[5 * np + i] = l[2];
+    p4[i] = make_float4(h[0], h[1], h[2], l[0]);
+    p2[i] = make_float2(l[1], l[2]);
   }
-  // |x_i - x_j| from the hi/lo pairs, in float
+  // x_i - x_j from the hi/lo pairs, in float
+  __device__ void diff(int i, int j, float& dx, float& dy, float& dz) const {
+    const float4 a = p4[i], b = p4[j];
+    const float2 c = p2[i], d = p2[j];
+    dx = (a.x - b.x) + (a.w - b.w);
+    dy = (a.y - b.y) + (c.x - d.x);
+    dz = (a.z - b.z) + (c.y - d.y);
+  }
   __device__ float dist(int i, int j) const {
-    const float dx = (p[i] - p[j]) + (p[3 * np + i] - p[3 * np + j]);
-    const float dy = (p[np + i] - p[np + j]) + (p[4 * np + i] - p[4 * np + j]);
-    const float dz = (p[2 * np + i] - p[2 * np + j]) + (p[5 * np + i] - p[5 * np + j]);
+    float dx, dy, dz;
+    diff(i, j, dx, dy, dz);
     return sqrtf(dx * dx + dy * dy + dz * dz);
   }
 };
 
+// positions staged per CTA: the tile's slots and its halo, rounded up to an
+// even count so that every buffer's float4 part stays 16-byte aligned
+__host__ __device__ inline int cl_np(int tile, int hmax) { return (tile + hmax + 1) & ~1; }
+
+
 // Shared memory of one CTA: nsp_max springs (CSR by slot), nbond_max entries
 // of the bond tables.
 struct ClusterLayout {
-  int np, nsp_max, nbond_max;
+  int np, nsp_max, nbond_max;  // np even (cl_np)
   int nbuf;  // position buffers: 2 (one cluster barrier per substep) or 1 (two, less shared memory)
   __host__ __device__ int max_cilia() const { return nbond_max / 2 + 1; }
+  __host__ __device__ int nsp2() const { return (nsp_max + 1) & ~1; }
   __host__ __device__ size_t bytes(int T) const {
     size_t b = (size_t)nbuf * 6 * sizeof(float) * (size_t)np;  // position buffers
-    b += (size_t)nsp_max * (sizeof(uint32_t) + 2 * sizeof(float));  // springs
+    b += (size_t)nsp2() * (sizeof(uint32_t) + 2 * sizeof(float));  // springs: word, (rest, -2k)
     b += (size_t)nbond_max * 3 * sizeof(float);                      // bond tables
     b = (b + 15) & ~(size_t)15;
     b += (size_t)nbond_max * sizeof(int4);                      // refresh entries
@@ -100,14 +109,16 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
   const int base = tile * T;
   // carve shared memory
   unsigned char* ptr = smem;
-  float* const pbase = reinterpret_cast<float*>(ptr);  // buffer b at pbase + b * 6 * np
+  unsigned char* const pbase = ptr;  // buffer b at pbase + b * 24 * np bytes
   const int nbuf = lay.nbuf;
-  auto buf = [&](int b) { return PBuf{pbase + (nbuf == 2 ? b : 0) * 6 * np, np}; };
-  ptr += (size_t)nbuf * 6 * sizeof(float) * (size_t)np;
-  uint32_t* sw = reinterpret_cast<uint32_t*>(ptr);
-  float* srest = reinterpret_cast<float*>(sw + lay.nsp_max);
-  float* sm2k = srest + lay.nsp_max;
-  ptr = reinterpret_cast<unsigned char*>(sm2k + lay.nsp_max);
+  auto buf = [&](int b) {
+    unsigned char* q = pbase + (size_t)(nbuf == 2 ? b : 0) * 24 * np;
+    return PBuf{reinterpret_cast<float4*>(q), reinterpret_cast<float2*>(q + 16 * (size_t)np)};
+  };
+  ptr += (size_t)nbuf * 24 * (size_t)np;
+  float2* srk = reinterpret_cast<float2*>(ptr);                  // (rest, -2k) per spring
+  uint32_t* sw = reinterpret_cast<uint32_t*>(srk + lay.nsp2());  // other | bond entry << 16
+  ptr = reinterpret_cast<unsigned char*>(sw + lay.nsp2());
   float* bnew = reinterpret_cast<float*>(ptr);
   float* bold = bnew + lay.nbond_max;
   float* bdiag = bold + lay.nbond_max;
@@ -133,17 +144,25 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
   } else {
     for (int s = sp0 + (int)threadIdx.x; s < sp1; s += blockDim.x) {
       const int k = s - sp0;
-      const int kraw = m.sp_kind[s];
-      const int kind = kraw & 3;
-      // bond-table index for BOND/DIAG springs; bit 13 marks a reaction owed to a hub
-      const int bl = kind >= 2 ? m.sp_ref[s] - bond0 : ((kraw & kSpringReact) ? 0x2000 : 0);
-      sw[k] = (uint32_t)m.sp_local[s] | ((uint32_t)bl << 16) | ((uint32_t)kind << 30);
-      srest[k] = (float)m.sp_rest[s];
-      sm2k[k] = (float)m.sp_m2k[s];
+      const int kind = m.sp_kind[s] & 3;
+      // BOND/DIAG springs carry their bond-table entry in the high half
+      const uint32_t bl = kind >= 2 ? (uint32_t)(m.sp_ref[s] - bond0) : 0u;
+      sw[k] = (uint32_t)m.sp_local[s] | (bl << 16);
+      srk[k] = make_float2((float)m.sp_rest[s], (float)m.sp_m2k[s]);
     }
   }
   const int s0 = valid && sp1 - sp0 <= lay.nsp_max ? m.sp_start[slot] - sp0 : 0;
   const int s1 = valid && sp1 - sp0 <= lay.nsp_max ? m.sp_start[slot + 1] - sp0 : 0;
+  // group boundaries of this slot's list (the planner sorts it by spring_group):
+  // CONST [s0, g1), CONST owed to a hub [g1, g2), GUARDED [g2, g3), BOND [g3, g4), DIAG [g4, s1)
+  int g1 = s0, g2 = s0, g3 = s0, g4 = s0;  // ends of groups 0..3; group 4 ends at s1
+  for (int s = s0; s < s1; ++s) {
+    const int grp = spring_group(m.sp_kind[sp0 + s]);
+    g1 += grp < 1;
+    g2 += grp < 2;
+    g3 += grp < 3;
+    g4 += grp < 4;
+  }
   for (int k = threadIdx.x; k < nbond; k += blockDim.x) {
     bnew[k] = (float)m.newlen[bond0 + k];
     bold[k] = (float)m.oldlen[bond0 + k];
@@ -201,16 +220,12 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
     const PBuf B = buf(cur);
     // halo: beads of other CTAs, from their current buffer
     for (int i = threadIdx.x; i < hn; i += blockDim.x) {
-      const int g = m.halo[h0 + i];
-      const int r = g / T - first_tile, j = g % T;
-      const float* rp = cluster.map_shared_rank(B.p, r);
-      float* dst = B.p + T + i;
-      dst[0] = rp[j];
-      dst[np] = rp[np + j];
-      dst[2 * np] = rp[2 * np + j];
-      dst[3 * np] = rp[3 * np + j];
-      dst[4 * np] = rp[4 * np + j];
-      dst[5 * np] = rp[5 * np + j];
+      const int gs = m.halo[h0 + i];
+      const int r = gs / T - first_tile, j = gs % T;
+      const float4* rp4 = cluster.map_shared_rank(B.p4, r);
+      const float2* rp2 = cluster.map_shared_rank(B.p2, r);
+      B.p4[T + i] = rp4[j];
+      B.p2[T + i] = rp2[j];
     }
     __syncthreads();
     const bool due = (a.refresh[eval >> 6] >> (eval & 63)) & 1ull;  // refresh (src/cilia.cpp:206-215)
@@ -229,44 +244,70 @@ __device__ __forceinline__ void md_cluster_body(const MDState& m, const MDStepAr
     float ax = 0.f, ay = 0.f, az = 0.f;
     float rx = 0.f, ry = 0.f, rz = 0.f;  // reactions owed to the tile's hub
     if (mv >= 0) {
-      const float* hx = B.p;
-      const float* hy = hx + np;
-      const float* hz = hy + np;
-      const float* lx = hz + np;
-      const float* ly = lx + np;
-      const float* lz = ly + np;
-      const float mhx = hx[me], mhy = hy[me], mhz = hz[me], mlx = lx[me], mly = ly[me], mlz = lz[me];
-      // two springs per iteration into independent accumulators (more ILP)
-      float bx = 0.f, by = 0.f, bz = 0.f;
-      auto one = [&](int s, float& cx, float& cy, float& cz) {
-        const uint32_t w = sw[s];
-        const int o = (int)(w & 0xffffu);
-        const int kind = (int)(w >> 30);
-        const int bl = (int)((w >> 16) & 0x3fffu);
-        const float b = kind <= 1 ? srest[s] : (kind == 2 ? bnew[bl] : bdiag[bl]);
-        const float dx = (mhx - hx[o]) + (mlx - lx[o]);
-        const float dy = (mhy - hy[o]) + (mly - ly[o]);
-        const float dz = (mhz - hz[o]) + (mlz - lz[o]);
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const float fac = (kind == 1 && d2 == 0.0f) ? 0.0f : sm2k[s] * (1.0f - b * rsqrtf(d2));
-        cx = fmaf(dx, fac, cx);
-        cy = fmaf(dy, fac, cy);
-        cz = fmaf(dz, fac, cz);
-        if (kind == 0 && (bl & 0x2000)) {
-          rx = fmaf(-dx, fac, rx);
-          ry = fmaf(-dy, fac, ry);
-          rz = fmaf(-dz, fac, rz);
-        }
+      // one loop per spring group: no per-spring dispatch on the kind
+      const float4 m4 = B.p4[me];
+      const float2 m2 = B.p2[me];
+      auto geo = [&](int o, float& dx, float& dy, float& dz) {
+        const float4 b4 = B.p4[o];
+        const float2 b2 = B.p2[o];
+        dx = (m4.x - b4.x) + (m4.w - b4.w);
+        dy = (m4.y - b4.y) + (m2.x - b2.x);
+        dz = (m4.z - b4.z) + (m2.y - b2.y);
       };
-      int s = s0 + lane;
-      for (; s + kCLanes < s1; s += 2 * kCLanes) {
-        one(s, ax, ay, az);
-        one(s + kCLanes, bx, by, bz);
+#pragma unroll 2
+      for (int s = s0 + lane; s < g1; s += kCLanes) {  // CONST
+        const float2 rk = srk[s];
+        float dx, dy, dz;
+        geo((int)sw[s], dx, dy, dz);
+        const float fac = rk.y * (1.0f - rk.x * rsqrtf(dx * dx + dy * dy + dz * dz));
+        ax = fmaf(dx, fac, ax);
+        ay = fmaf(dy, fac, ay);
+        az = fmaf(dz, fac, az);
       }
-      if (s < s1) one(s, ax, ay, az);
-      ax += bx;
-      ay += by;
-      az += bz;
+      for (int s = g1 + lane; s < g2; s += kCLanes) {  // CONST, reaction owed to the hub
+        const float2 rk = srk[s];
+        float dx, dy, dz;
+        geo((int)sw[s], dx, dy, dz);
+        const float fac = rk.y * (1.0f - rk.x * rsqrtf(dx * dx + dy * dy + dz * dz));
+        ax = fmaf(dx, fac, ax);
+        ay = fmaf(dy, fac, ay);
+        az = fmaf(dz, fac, az);
+        rx = fmaf(-dx, fac, rx);
+        ry = fmaf(-dy, fac, ry);
+        rz = fmaf(-dz, fac, rz);
+      }
+      for (int s = g2 + lane; s < g3; s += kCLanes) {  // GUARDED: no force at zero distance
+        const float2 rk = srk[s];
+        float dx, dy, dz;
+        geo((int)sw[s], dx, dy, dz);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float fac = d2 == 0.0f ? 0.0f : rk.y * (1.0f - rk.x * rsqrtf(d2));
+        ax = fmaf(dx, fac, ax);
+        ay = fmaf(dy, fac, ay);
+        az = fmaf(dz, fac, az);
+      }
+#pragma unroll 2
+      for (int s = g3 + lane; s < g4; s += kCLanes) {  // BOND: active rest length
+        const uint32_t w = sw[s];
+        const float b = bnew[w >> 16];
+        float dx, dy, dz;
+        geo((int)(w & 0xffffu), dx, dy, dz);
+        const float fac = srk[s].y * (1.0f - b * rsqrtf(dx * dx + dy * dy + dz * dz));
+        ax = fmaf(dx, fac, ax);
+        ay = fmaf(dy, fac, ay);
+        az = fmaf(dz, fac, az);
+      }
+#pragma unroll 2
+      for (int s = g4 + lane; s < s1; s += kCLanes) {  // DIAG
+        const uint32_t w = sw[s];
+        const float b = bdiag[w >> 16];
+        float dx, dy, dz;
+        geo((int)(w & 0xffffu), dx, dy, dz);
+        const float fac = srk[s].y * (1.0f - b * rsqrtf(dx * dx + dy * dy + dz * dz));
+        ax = fmaf(dx, fac, ax);
+        ay = fmaf(dy, fac, ay);
+        az = fmaf(dz, fac, az);
+      }
     }
     if (kCLanes == 2) {
       ax += __shfl_xor_sync(0xffffffffu, ax, 1);
@@ -454,41 +495,48 @@ struct ClBinF32 {
 };
 
 // Binning and bead collision of one replica of a batch (cells of the arena,
-// offset by the replica's first cell).
-struct BatchBin {
-  static constexpr bool kCollide = true;
+// offset by the replica's first cell).  The fields live in shared memory and
+// are read only at the start and end of the launch, so they hold no
+// registers through the substeps.
+struct BatchBinData {
   float4* sum;
   uint32_t* cnt;
   const float4* par;
   long cell0;
   Box box;
-  const double* a_cur;
-  const double* a_next;
+  double a_cur[3], a_next[3];
   float mb;
   double mbd;
   unsigned* err;
   double* diss;
+};
+
+struct BatchBin {
+  static constexpr bool kCollide = true;
+  const BatchBinData* d;
   // MDObject beads in the collision (MPCD::next_tstep, src/libcilia/mpcd.cpp:140-247)
   __device__ double collide(const double* X, float* v) const {
-    const long cid = unwrapped_cell(box, a_cur, X[0], X[1], X[2]);
+    const long cid = unwrapped_cell(d->box, d->a_cur, X[0], X[1], X[2]);
     if (cid < 0) {
-      atomicOr(err, kErrCellRange);
+      atomicOr(d->err, kErrCellRange);
       return 0.0;
     }
-    apply_map_f32(par + 3 * (cell0 + cid), v[0], v[1], v[2]);
-    return mbd * ((double)v[0] * v[0] + (double)v[1] * v[1] + (double)v[2] * v[2]);
+    apply_map_f32(d->par + 3 * (d->cell0 + cid), v[0], v[1], v[2]);
+    return d->mbd * ((double)v[0] * v[0] + (double)v[1] * v[1] + (double)v[2] * v[2]);
   }
-  __device__ void add_diss(double d) const { atomicAdd(diss, d); }
+  __device__ void add_diss(double x) const { atomicAdd(d->diss, x); }
   // md_loop_stop's binning with the next shift (src/libcilia/mdobject.cpp:62-72)
   __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
-    const long cid = unwrapped_cell(box, a_next, x, y, z);
+    const long cid = unwrapped_cell(d->box, d->a_next, x, y, z);
     if (cid < 0) {
-      atomicOr(err, kErrCellRange);
+      atomicOr(d->err, kErrCellRange);
       return;
     }
+    const float mb = d->mb;
     const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
-    red_add_v4(sum + cell0 + cid, make_float4(fvx * mb, fvy * mb, fvz * mb, mb * (fvx * fvx + fvy * fvy + fvz * fvz)));
-    atomicAdd(cnt + cell0 + cid, 1u << 16);
+    red_add_v4(d->sum + d->cell0 + cid,
+               make_float4(fvx * mb, fvy * mb, fvz * mb, mb * (fvx * fvx + fvy * fvy + fvz * fvz)));
+    atomicAdd(d->cnt + d->cell0 + cid, 1u << 16);
   }
 };
 
@@ -498,29 +546,34 @@ template <int kCLanes>
 __global__ void __launch_bounds__(1024, 1)
     k_md_cluster_batch(MDState m, BatchTables t, BatchCells c, const int* reps, int ctiles, ClusterLayout lay) {
   __shared__ MDStepArgs sa;
+  __shared__ BatchBinData sb;
   const int r = reps[blockIdx.x / ctiles];
   if (!t.step[r].active) return;
-  if (threadIdx.x == 0) sa = t.step[r].md;
-  __syncthreads();
   const BatchRep& R = t.rep[r];
-  BatchBin bin;
-  bin.sum = c.sum;
-  bin.cnt = c.cnt;
-  bin.par = c.par;
-  bin.cell0 = R.cell0;
-  bin.box = sa.box;
-  bin.a_cur = sa.a_cur;
-  bin.a_next = sa.a_next;
-  bin.mb = (float)R.bead_mass;
-  bin.mbd = R.bead_mass;
-  bin.err = &t.state[r].err;
-  bin.diss = &t.state[r].diss;
+  if (threadIdx.x == 0) {
+    sa = t.step[r].md;
+    sb.sum = c.sum;
+    sb.cnt = c.cnt;
+    sb.par = c.par;
+    sb.cell0 = R.cell0;
+    sb.box = sa.box;
+    for (int q = 0; q < 3; ++q) {
+      sb.a_cur[q] = sa.a_cur[q];
+      sb.a_next[q] = sa.a_next[q];
+    }
+    sb.mb = (float)R.bead_mass;
+    sb.mbd = R.bead_mass;
+    sb.err = &t.state[r].err;
+    sb.diss = &t.state[r].diss;
+  }
+  __syncthreads();
+  const BatchBin bin{&sb};
   md_cluster_body<kCLanes>(m, sa, bin, lay, R.md_tile0 + (int)(blockIdx.x % ctiles));
 }
 
 template <int L, typename Bin>
 cudaError_t launch_cluster_l(const MDState& m, const MDStepArgs& a, const Bin& bin, cudaStream_t s) {
-  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max, m.cl_nbuf};
+  ClusterLayout lay{cl_np(m.tile, m.hmax), m.cl_nsp_max, m.cl_nbond_max, m.cl_nbuf};
   const size_t smem = lay.bytes(m.tile);
   auto kern = k_md_cluster<L, Bin>;
   cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -548,7 +601,7 @@ cudaError_t launch_cluster(const MDState& m, const MDStepArgs& a, const Bin& bin
 }  // namespace
 
 size_t md_cluster_smem(const MDState& m) {
-  ClusterLayout lay{m.tile + m.hmax, m.cl_nsp_max, m.cl_nbond_max, m.cl_nbuf};
+  ClusterLayout lay{cl_np(m.tile, m.hmax), m.cl_nsp_max, m.cl_nbond_max, m.cl_nbuf};
   return lay.bytes(m.tile);
 }
 
@@ -585,7 +638,7 @@ int md_cluster_feasible(const MDState& m) {
 }
 
 size_t md_cluster_batch_smem(int tile, int hmax, int nsp_max, int nbond_max, int nbuf) {
-  ClusterLayout lay{tile + hmax, nsp_max, nbond_max, nbuf};
+  ClusterLayout lay{cl_np(tile, hmax), nsp_max, nbond_max, nbuf};
   return lay.bytes(tile);
 }
 
@@ -634,7 +687,7 @@ int launch_md_cluster_batch(const MDState& m, const BatchTables& t, BatchCells c
                             int ctiles, int hmax, int nsp_max, int nbond_max, int nbuf, cudaStream_t s,
                             cudaError_t* st) {
   if (nreps <= 0) return 0;
-  ClusterLayout lay{m.tile + hmax, nsp_max, nbond_max, nbuf};
+  ClusterLayout lay{cl_np(m.tile, hmax), nsp_max, nbond_max, nbuf};
   const size_t smem = lay.bytes(m.tile);
   cudaLaunchAttribute attr[1];
   if (m.cl_lanes == 2) {

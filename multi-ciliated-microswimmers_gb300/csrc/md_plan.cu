@@ -348,6 +348,35 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     out.srest[d] = in.sp_rest[i];
     out.sm2k[d] = -2.0 * in.sp_kk[i];
   }
+  // cluster layouts: every slot's list sorted (stably) by spring group, so
+  // that the kernel runs one loop per group without testing kinds
+  if (out.cluster) {
+    std::vector<int> idx;
+    for (int sl_ = 0; sl_ < ns; ++sl_) {
+      const int a0 = start[sl_], a1 = start[sl_ + 1];
+      if (a1 - a0 < 2) continue;
+      idx.resize(a1 - a0);
+      for (int k = 0; k < a1 - a0; ++k) idx[k] = a0 + k;
+      std::stable_sort(idx.begin(), idx.end(),
+                       [&](int x, int y) { return spring_group(out.sk[x]) < spring_group(out.sk[y]); });
+      std::vector<int> so(a1 - a0), sk(a1 - a0), sr(a1 - a0);
+      std::vector<double> srest(a1 - a0), sm2k(a1 - a0);
+      for (int k = 0; k < a1 - a0; ++k) {
+        so[k] = out.so[idx[k]];
+        sk[k] = out.sk[idx[k]];
+        sr[k] = out.sr[idx[k]];
+        srest[k] = out.srest[idx[k]];
+        sm2k[k] = out.sm2k[idx[k]];
+      }
+      for (int k = 0; k < a1 - a0; ++k) {
+        out.so[a0 + k] = so[k];
+        out.sk[a0 + k] = sk[k];
+        out.sr[a0 + k] = sr[k];
+        out.srest[a0 + k] = srest[k];
+        out.sm2k[a0 + k] = sm2k[k];
+      }
+    }
+  }
   // halos: per tile the distinct slots of other tiles its springs reach, and
   // every spring's other bead as an index into the tile's staged positions
   out.sl.assign(nspk, 0);

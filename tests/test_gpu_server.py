@@ -14,7 +14,7 @@ collision partners), so:
     2x (+0.5 %) that share between two runs alone;
   - over a longer run (40 steps) the difference between the alone and the
     mixed result is no larger than 5x (+1e-3) the difference between two runs
-    of the request alone, and kT agrees within 1e-3.
+    of the request alone, and kT agrees within 3e-3.
 """
 import numpy as np
 import pytest
@@ -109,7 +109,7 @@ def test_long_run_mix_within_the_run_to_run_spread():
     spread = np.abs(pa - pb).max()
     diff = np.abs(pa - pm).max()
     assert diff < 5 * spread + 1e-3, (diff, spread)
-    assert abs(ia["obs"]["kT"] - im["obs"]["kT"]) < 1e-3
+    assert abs(ia["obs"]["kT"] - im["obs"]["kT"]) < 3e-3
 
 
 def test_admission_respects_the_budget():
