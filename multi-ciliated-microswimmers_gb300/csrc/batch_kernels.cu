@@ -93,17 +93,36 @@ __global__ void k_batch_cell_params(BatchTables t, BatchCells c) {
     const long c1 = min(c0 + kCellPage, R.cell0 + R.ncell);
     const uint64_t seed = R.seed, step = S.step;
     const float mb = S.fbead_mass;
+    const long cell0 = R.cell0;
     float ldiss = 0.0f;
     unsigned errbits = 0;
     bool gfail = false;
-    for (long cid = c0 + threadIdx.x; cid < c1; cid += blockDim.x) {
-      const uint32_t w = c.cnt[cid];
-      if (w == 0) continue;
-      const float4 s = c.sum[cid];
-      c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
-      c.cnt[cid] = 0u;
-      cell_map_f32(s, w, (uint32_t)(cid - R.cell0), seed, step, mb, nullptr, nullptr, c.par + 3 * cid, ldiss,
-                   errbits, gfail);
+    // four cells per thread at a time: their count words and sums are loaded
+    // together, so the latency of the loads is paid once per four cells
+    constexpr int kU = 4;
+    const long stride = blockDim.x;
+    for (long cb = c0 + threadIdx.x; cb < c1; cb += kU * stride) {
+      uint32_t w[kU];
+      float4 sm[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const long cid = cb + u * stride;
+        w[u] = cid < c1 ? __ldcg(c.cnt + cid) : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const long cid = cb + u * stride;
+        sm[u] = w[u] ? __ldcg(c.sum + cid) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (!w[u]) continue;
+        const long cid = cb + u * stride;
+        c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
+        c.cnt[cid] = 0u;
+        cell_map_f32(sm[u], w[u], (uint32_t)(cid - cell0), seed, step, mb, nullptr, nullptr, c.par + 3 * cid, ldiss,
+                     errbits, gfail);
+      }
     }
     if (gfail) errbits |= kErrGammaLoop;
     if (errbits) atomicOr(&t.state[r].err, errbits);
@@ -130,6 +149,7 @@ __global__ void __launch_bounds__(512) k_batch_fluid_step(BatchTables t, BatchFl
     const float4* const par = c.par + 3 * R.cell0;
     float ke_after = 0.0f;
     unsigned bad = 0;
+#pragma unroll 2
     for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const float4 p = f.pos[i];
       const float4 v = f.vel[i];

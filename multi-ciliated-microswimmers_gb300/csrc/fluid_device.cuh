@@ -61,9 +61,11 @@ __device__ __forceinline__ void rewrap_f(float& o, int& i, int L, unsigned& bad)
   }
 }
 
+// Vector reduction into a cell sum.  No "memory" clobber: the sums are only
+// reduced into during a kernel (never read back in it), so the compiler may
+// move the other loads and stores of the thread across it.
 __device__ __forceinline__ void red_add_v4(float4* addr, float4 v) {
-  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
-               : "memory");
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
 }
 
 // Split-precision collision map of one cell (MPCD::next_tstep,

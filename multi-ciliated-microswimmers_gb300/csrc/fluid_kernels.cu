@@ -528,14 +528,28 @@ __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
   float ldiss = 0.0f;
   unsigned errbits = 0;
   bool gfail = false;
-  for (long cid = (long)blockIdx.x * blockDim.x + threadIdx.x; cid < c.ncell; cid += (long)gridDim.x * blockDim.x) {
-    const uint32_t w = c.cnt[cid];
-    if (w == 0) continue;
-    const float4 s = c.sum[cid];
-    c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
-    c.cnt[cid] = 0u;
-    cell_map_f32(s, w, (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 3 * cid, ldiss,
-                 errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt);
+  // four cells per thread at a time, their loads issued together
+  constexpr int kU = 4;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long cb = (long)blockIdx.x * blockDim.x + threadIdx.x; cb < c.ncell; cb += kU * stride) {
+    uint32_t w[kU];
+    float4 sm[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const long cid = cb + u * stride;
+      w[u] = cid < c.ncell ? __ldcg(c.cnt + cid) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) sm[u] = w[u] ? __ldcg(c.sum + cb + u * stride) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (!w[u]) continue;
+      const long cid = cb + u * stride;
+      c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
+      c.cnt[cid] = 0u;
+      cell_map_f32(sm[u], w[u], (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 3 * cid,
+                   ldiss, errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt);
+    }
   }
   if (gfail) errbits |= kErrGammaLoop;
   if (errbits) atomicOr(a.err, errbits);
@@ -550,6 +564,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF3
   const float h = a.fh, gk = a.fgkick;
   float ke_after = 0.0f;
   unsigned bad = 0;
+#pragma unroll 2
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
     const float4 p = f.pos[i];
     const float4 v = f.vel[i];
