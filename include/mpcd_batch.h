@@ -49,7 +49,8 @@ typedef struct {
 
 /* launch configuration chosen by mpcd_batch_autotune (or set by hand) */
 typedef struct {
-  int fluid_threads, fluid_blocks;   /* blocks 0: one per page up to 8 per SM */
+  int fluid_threads, fluid_blocks;   /* blocks 0: one per page up to 8 per SM; threads 0: the fluid pass
+                                        staged through shared memory by bulk copies (TMA) */
   int cell_threads, cell_blocks;
   int sort_interval;
 } mpcd_batch_tuning;

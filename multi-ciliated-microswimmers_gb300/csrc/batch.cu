@@ -1261,7 +1261,8 @@ int mpcd_batch_resident(const mpcd_batch* b) {
 int mpcd_batch_set_tuning(mpcd_batch* b, const mpcd_batch_tuning* t) {
   if (!b || !t) return fail(b, MPCD_EINVAL, "set_tuning: bad arguments");
   cudaSetDevice(b->p.device);
-  if (t->fluid_threads < 32 || t->fluid_threads > 1024 || t->fluid_threads % 32 || t->cell_threads < 32 ||
+  if ((t->fluid_threads != 0 && (t->fluid_threads < 32 || t->fluid_threads > 1024)) || t->fluid_threads % 32 ||
+      t->cell_threads < 32 ||
       t->cell_threads > 1024 || t->cell_threads % 32 || t->fluid_blocks < 0 || t->cell_blocks < 0 ||
       t->sort_interval < 1)
     return fail(b, MPCD_EINVAL, "set_tuning: invalid configuration");
@@ -1321,11 +1322,13 @@ int mpcd_batch_autotune(mpcd_batch* b, int trial_steps, mpcd_batch_tuning* chose
     int rc = mpcd_batch_set_md_layout(b, best_lanes, best_tile);
     if (rc) return rc;
   }
-  // fluid pass: threads per block and grid (persistent multiples of the SM count, or one block per page)
-  const int threads[] = {256, 512};
+  // fluid pass: threads per block and grid (persistent multiples of the SM count, or one block per
+  // page); threads 0 = the variant staged through shared memory by bulk copies (own block and grid)
+  const int threads[] = {0, 256, 512};
   const long grids[] = {0, 4L * sms, 16L * sms, b->npart_pages};
   for (int th : threads)
     for (long g : grids) {
+      if (th == 0 && g != 0) continue;
       mpcd_batch_tuning t = best;
       t.fluid_threads = th;
       t.fluid_blocks = (int)std::min<long>(g, 1L << 30);

@@ -16,6 +16,7 @@
 // company it keeps.
 #include "batch_internal.h"
 #include "fluid_device.cuh"
+#include "tma.cuh"
 
 namespace mpcd {
 
@@ -131,52 +132,169 @@ __global__ void k_batch_cell_params(BatchTables t, BatchCells c) {
   }
 }
 
-__global__ void __launch_bounds__(512) k_batch_fluid_step(BatchTables t, BatchFluid f, BatchCells c) {
+// The replica parameters one fluid page needs.
+struct FluidPage {
+  int L[3];
+  float tc[3], tn[3];
+  float h, gk;
+  float4* sum;
+  uint32_t* cnt;
+  const float4* par;
+};
+
+__device__ __forceinline__ FluidPage fluid_page(const BatchTables& t, const BatchCells& c, int r) {
+  const BatchStep& S = t.step[r];
+  const BatchRep& R = t.rep[r];
+  FluidPage P;
+  for (int q = 0; q < 3; ++q) {
+    P.L[q] = R.L[q];
+    P.tc[q] = S.fta_cur[q];
+    P.tn[q] = S.fta_next[q];
+  }
+  P.h = S.fh;
+  P.gk = S.fgkick;
+  P.sum = c.sum + R.cell0;
+  P.cnt = c.cnt + R.cell0;
+  P.par = c.par + 3 * R.cell0;
+  return P;
+}
+
+// One fluid particle (MPCD::next_tstep's rotation, MPCD::move, Fluid::move,
+// add_impuls: src/libcilia/mpcd.cpp:140-267, src/libcilia/fluid.cpp:152-167):
+// collide with its cell's map, stream, wrap, body force, bin into the sums of
+// the next shift.  Returns the new state.
+__device__ __forceinline__ void fluid_particle(const FluidPage& P, const float4 p, const float4 v, float4& po, float4& vo,
+                                               float& ke_after, unsigned& bad) {
+  const int Lx = P.L[0], Ly = P.L[1], Lz = P.L[2];
+  const uint32_t cp = __float_as_uint(p.w);
+  int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
+  float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
+  const long cid = shifted_f(ix, ox, P.tc[0], Lx) +
+                   (long)Lx * (shifted_f(iy, oy, P.tc[1], Ly) + (long)Ly * shifted_f(iz, oz, P.tc[2], Lz));
+  apply_map_f32(P.par + 3 * cid, vx, vy, vz);
+  ke_after += vx * vx + vy * vy + vz * vz;
+  ox = fmaf(vx, P.h, ox);
+  oy = fmaf(vy, P.h, oy);
+  oz = fmaf(vz, P.h, oz);
+  rewrap_f(ox, ix, Lx, bad);
+  rewrap_f(oy, iy, Ly, bad);
+  rewrap_f(oz, iz, Lz, bad);
+  if (P.gk != 0.0f) vx += P.gk;
+  const long cn = shifted_f(ix, ox, P.tn[0], Lx) +
+                  (long)Lx * (shifted_f(iy, oy, P.tn[1], Ly) + (long)Ly * shifted_f(iz, oz, P.tn[2], Lz));
+  red_add_v4(P.sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
+  atomicAdd(P.cnt + cn, 1u);
+  po = make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz)));
+  vo = make_float4(vx, vy, vz, 0.f);
+}
+
+__global__ void __launch_bounds__(512, 2) k_batch_fluid_step(BatchTables t, BatchFluid f, BatchCells c) {
   for (long pg = blockIdx.x; pg < t.npart_pages; pg += gridDim.x) {
     const int r = t.part_page_rep[pg];
     if (r < 0) continue;
-    const BatchStep& S = t.step[r];
-    if (!S.active) continue;
+    if (!t.step[r].active) continue;
     const BatchRep& R = t.rep[r];
     const long i0 = pg * kPartPage;
     const long i1 = min(i0 + kPartPage, R.p0 + R.n);
-    const int Lx = R.L[0], Ly = R.L[1], Lz = R.L[2];
-    const float tcx = S.fta_cur[0], tcy = S.fta_cur[1], tcz = S.fta_cur[2];
-    const float tnx = S.fta_next[0], tny = S.fta_next[1], tnz = S.fta_next[2];
-    const float h = S.fh, gk = S.fgkick;
-    float4* const sum = c.sum + R.cell0;
-    uint32_t* const cnt = c.cnt + R.cell0;
-    const float4* const par = c.par + 3 * R.cell0;
+    const FluidPage P = fluid_page(t, c, r);
     float ke_after = 0.0f;
     unsigned bad = 0;
 #pragma unroll 2
     for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      const float4 p = f.pos[i];
-      const float4 v = f.vel[i];
-      const uint32_t cp = __float_as_uint(p.w);
-      int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
-      float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
-      const long cid = shifted_f(ix, ox, tcx, Lx) +
-                       (long)Lx * (shifted_f(iy, oy, tcy, Ly) + (long)Ly * shifted_f(iz, oz, tcz, Lz));
-      apply_map_f32(par + 3 * cid, vx, vy, vz);
-      ke_after += vx * vx + vy * vy + vz * vz;
-      ox = fmaf(vx, h, ox);
-      oy = fmaf(vy, h, oy);
-      oz = fmaf(vz, h, oz);
-      rewrap_f(ox, ix, Lx, bad);
-      rewrap_f(oy, iy, Ly, bad);
-      rewrap_f(oz, iz, Lz, bad);
-      if (gk != 0.0f) vx += gk;
-      const long cn = shifted_f(ix, ox, tnx, Lx) +
-                      (long)Lx * (shifted_f(iy, oy, tny, Ly) + (long)Ly * shifted_f(iz, oz, tnz, Lz));
-      red_add_v4(sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
-      atomicAdd(cnt + cn, 1u);
-      f.pos[i] = make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz)));
-      f.vel[i] = make_float4(vx, vy, vz, 0.f);
+      float4 po, vo;
+      fluid_particle(P, f.pos[i], f.vel[i], po, vo, ke_after, bad);
+      f.pos[i] = po;
+      f.vel[i] = vo;
     }
     if (bad) atomicOr(&t.state[r].err, bad);
     const double tot = block_sum_f32(ke_after);
     if (threadIdx.x == 0 && tot != 0.0) atomicAdd(&t.state[r].diss, -tot);
+  }
+}
+
+// The same pass with the particle state staged through shared memory by bulk
+// asynchronous copies (TMA): chunks of kTmaChunk particles, two buffers, the
+// copy of the next chunk in flight while the current one is processed.  The
+// chunks are the pages' quarters, taken in a grid-stride order that every
+// thread of the block derives alike; waits are bounded (a timeout sets
+// kErrBarrier for the chunk's replica and ends the block after its copies
+// are drained).
+constexpr int kTmaChunk = 1024;
+constexpr int kTmaThreads = 256;
+constexpr uint32_t kTmaWaitLimit = 1u << 22;
+
+__global__ void __launch_bounds__(kTmaThreads) k_batch_fluid_step_tma(BatchTables t, BatchFluid f, BatchCells c) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  float4* const buf = reinterpret_cast<float4*>(tma_smem);  // [b][pos | vel][kTmaChunk]
+  __shared__ __align__(8) uint64_t bar[2];
+  constexpr int kParts = kPartPage / kTmaChunk;
+  const long nchunks = t.npart_pages * kParts;
+  auto chunk = [&](long q, long& i0, int& n, int& r) -> bool {
+    const long pg = q / kParts;
+    r = t.part_page_rep[pg];
+    if (r < 0 || !t.step[r].active) return false;
+    const BatchRep& R = t.rep[r];
+    i0 = pg * kPartPage + (q % kParts) * kTmaChunk;
+    const long e = min(i0 + kTmaChunk, R.p0 + R.n);
+    n = (int)(e - i0);
+    return n > 0;
+  };
+  auto issue = [&](long i0, int n, int b) {
+    const uint32_t bytes = (uint32_t)n * sizeof(float4);
+    mbar_arrive_expect_tx(&bar[b], 2 * bytes);
+    bulk_load(buf + (2 * b) * kTmaChunk, f.pos + i0, bytes, &bar[b]);
+    bulk_load(buf + (2 * b + 1) * kTmaChunk, f.vel + i0, bytes, &bar[b]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  long q = blockIdx.x, i0 = 0;
+  int n = 0, r = -1;
+  while (q < nchunks && !chunk(q, i0, n, r)) q += gridDim.x;
+  if (q >= nchunks) return;
+  if (threadIdx.x == 0) issue(i0, n, 0);
+  int b = 0;
+  uint32_t phase = 0u;  // bit k: parity of the next phase of bar[k]
+  for (;;) {
+    long qn = q + gridDim.x, i0n = 0;
+    int nn = 0, rn = -1;
+    while (qn < nchunks && !chunk(qn, i0n, nn, rn)) qn += gridDim.x;
+    const bool has_next = qn < nchunks;
+    if (threadIdx.x == 0 && has_next) {  // buffer b ^ 1 was released by the last barrier
+      fence_proxy_async_smem();
+      issue(i0n, nn, b ^ 1);
+    }
+    const bool ok = mbar_wait(&bar[b], (phase >> b) & 1u, kTmaWaitLimit);
+    phase ^= 1u << b;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(&t.state[r].err, kErrBarrier);
+      if (has_next) mbar_wait(&bar[b ^ 1], (phase >> (b ^ 1)) & 1u, kTmaWaitLimit);  // drain the copy in flight
+      return;
+    }
+    const FluidPage P = fluid_page(t, c, r);
+    const float4* sp = buf + (2 * b) * kTmaChunk;
+    const float4* sv = buf + (2 * b + 1) * kTmaChunk;
+    float ke_after = 0.0f;
+    unsigned bad = 0;
+    for (int j = threadIdx.x; j < n; j += kTmaThreads) {
+      float4 po, vo;
+      fluid_particle(P, sp[j], sv[j], po, vo, ke_after, bad);
+      f.pos[i0 + j] = po;
+      f.vel[i0 + j] = vo;
+    }
+    if (bad) atomicOr(&t.state[r].err, bad);
+    const double tot = block_sum_f32(ke_after);  // its barriers also release buffer b
+    if (threadIdx.x == 0 && tot != 0.0) atomicAdd(&t.state[r].diss, -tot);
+    __syncthreads();
+    if (!has_next) break;
+    q = qn;
+    i0 = i0n;
+    n = nn;
+    r = rn;
+    b ^= 1;
   }
 }
 
@@ -347,6 +465,19 @@ int launch_batch_cell_params(const BatchTables& t, BatchCells c, int threads, in
 
 int launch_batch_fluid_step(const BatchTables& t, BatchFluid f, BatchCells c, int threads, int blocks,
                             cudaStream_t s) {
+  if (threads == 0) {  // shared-memory staged variant: fixed block, two 32 KB buffers, three blocks per SM
+    const size_t smem = 4 * sizeof(float4) * kTmaChunk;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute((const void*)k_batch_fluid_step_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      attr = true;
+    }
+    const long nchunks = t.npart_pages * (kPartPage / kTmaChunk);
+    if (blocks <= 0) blocks = (int)std::min<long>(nchunks, 3L * sm_count_b());
+    k_batch_fluid_step_tma<<<blocks, kTmaThreads, smem, s>>>(t, f, c);
+    return 1;
+  }
   if (blocks <= 0) blocks = page_grid(t.npart_pages);
   k_batch_fluid_step<<<blocks, threads, 0, s>>>(t, f, c);
   return 1;

@@ -216,3 +216,35 @@ def test_md_relayout_continues_the_trajectory():
     p2, v2 = b2.beads(r2, nb)
     assert np.abs(p1 - p2).max() < 1e-3
     assert b2.status(r2)["steps"] == 6 and b2.status(r2)["err"] == 0
+
+
+def test_shared_memory_staged_fluid_pass_matches_the_direct_pass():
+    """The fluid pass staged by bulk copies (tuning fluid_threads = 0) gives the
+    direct pass's trajectory (same arithmetic; only atomics order differs)."""
+    specs = [dict(L=16, n_cilia=0, rodlength=10), dict(L=24, n_cilia=0, rodlength=10)]
+    rng = np.random.default_rng(4)
+    data = []
+    for sp in specs:
+        n = 10 * sp["L"] ** 3
+        pos = rng.uniform(0, sp["L"], (n, 3))
+        vel = rng.normal(size=(n, 3))
+        data.append((pos, vel - vel.mean(axis=0)))
+    out = []
+    for threads in (256, 0):
+        b = make_batch(specs)
+        b.set_tuning(fluid_threads=threads, fluid_blocks=0)
+        rs = []
+        for k, sp in enumerate(specs):
+            r = b.add(sp["L"], seed=40 + k)
+            b.set_fluid(r, *data[k])
+            b.admit(r)
+            b.set_steps(r, 5)
+            rs.append(r)
+        b.run(5)
+        out.append([b.fluid(r, 10 * sp["L"] ** 3) for r, sp in zip(rs, specs)])
+        for r in rs:
+            assert b.status(r)["err"] == 0 and b.status(r)["steps"] == 5
+        b.close()
+    for (p1, v1), (p2, v2), sp in zip(out[0], out[1], specs):
+        ok, worst = fluid_close(p1, v1, p2, v2, sp["L"])
+        assert ok, worst
