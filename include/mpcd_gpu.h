@@ -68,8 +68,10 @@ typedef struct {
   unsigned long long seed; /* counter-based generator seed for free-running steps */
   int device;            /* CUDA device ordinal */
   int sort_interval;     /* reorder particles by cell every this many steps (0 = auto) */
-  int md_split;          /* MD spring arithmetic: -1 auto (split when precision is FP32),
-                            0 float64, 1 split (float on hi/lo position pairs; state stays float64) */
+  int md_split;          /* MD arithmetic: -1 auto (1 when precision is FP32, 2 when FP64),
+                            0 float64, 1 split (float springs on hi/lo position pairs; state
+                            stays float64), 2 double-float (pairs of floats, about 48
+                            significand bits, for forces and substeps; float64 between steps) */
 } mpcd_params;
 
 /* Values that replace the generator for one step (all host arrays).  Used to
@@ -187,6 +189,12 @@ int mpcd_timed_run(mpcd_engine* h, int nsteps, int flush_l2, double* step_ms);
 #define MPCD_K_SORT 4   /* counting-sort reorder */
 int mpcd_set_profiling(mpcd_engine* h, int on);
 int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* launches);
+
+/* Layout the MD kernels run on (built first if the bead set changed).
+ * info[8] receives: cluster (1: one thread-block cluster, 0: cooperative
+ * grid), threads per slot, slots per tile, tiles (CTAs), slots, springs,
+ * largest halo of a tile, arithmetic (0 float64, 1 split, 2 double-float). */
+int mpcd_md_layout(mpcd_engine* h, int* info);
 
 /* ----------------------------------------------------------------------------
  * mpcd_fluid_step_noalloc -- one split-precision MPC step of a plain fluid

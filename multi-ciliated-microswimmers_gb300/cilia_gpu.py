@@ -22,6 +22,8 @@ WALLS_NONE, WALLS_NOSLIP, WALLS_SLIP = 0, 1, 2
 SPRING_CONST, SPRING_GUARDED, SPRING_BOND, SPRING_DIAG = 0, 1, 2, 3
 CILIUM_BASIC, CILIUM_CONSTANT = 0, 1
 K_CELL, K_FLUID, K_BEAD, K_MD, K_SORT = 0, 1, 2, 3, 4
+# MD arithmetic (mpcd_params.md_split): auto, float64, split floats, double-float
+MD_AUTO, MD_F64, MD_SPLIT, MD_DF = -1, 0, 1, 2
 
 _D = ctypes.c_double
 _DP = ctypes.POINTER(ctypes.c_double)
@@ -54,7 +56,8 @@ class MpcdCilium(ctypes.Structure):
 class CiliaOptions(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device", ctypes.c_int), ("seed", ctypes.c_ulonglong),
                 ("ststep", _D), ("create_fluid", ctypes.c_int), ("read_files", ctypes.c_int),
-                ("walls", ctypes.c_int), ("gravity", _D), ("bead_mass", _D), ("sort_interval", ctypes.c_int)]
+                ("walls", ctypes.c_int), ("gravity", _D), ("bead_mass", _D), ("sort_interval", ctypes.c_int),
+                ("md_arith", ctypes.c_int)]
 
 
 class MpcdBatchParams(ctypes.Structure):
@@ -135,6 +138,7 @@ def lib():
             "mpcd_timed_run": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, _DP]),
             "mpcd_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
             "mpcd_kernel_time": (ctypes.c_int, [P, ctypes.c_int, _DP, ctypes.POINTER(ctypes.c_longlong)]),
+            "mpcd_md_layout": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
             "mpcd_fluid_step_noalloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.c_long, P, P, _D, _DP, _DP,
                                                        ctypes.c_ulonglong, ctypes.c_ulonglong, _DP, P]),
             "mpcd_batch_create": (ctypes.c_int, [ctypes.POINTER(MpcdBatchParams), ctypes.POINTER(P)]),
@@ -351,14 +355,22 @@ class Engine:
         self._ck(lib().mpcd_kernel_time(self._h, int(kernel), ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
         return ms.value, n.value
 
+    def md_layout(self):
+        """The MD kernels' layout: cluster or cooperative grid, threads per slot, tile, tiles, slots, springs."""
+        a = (ctypes.c_int * 8)()
+        self._ck(lib().mpcd_md_layout(self._h, a), "md_layout")
+        keys = ("cluster", "lanes", "tile", "ntiles", "nslots", "nsprings", "hmax", "arith")
+        return dict(zip(keys, list(a)))
+
 
 class Sim:
     """The reference's Simulation on the GPU (cilia_sim), from cfg text or a path."""
 
     def __init__(self, cfg, *, is_text=True, precision=MPCD_FP64, seed=1, ststep=0.0, create_fluid=True,
-                 read_files=False, walls=WALLS_NONE, gravity=0.0, bead_mass=5.0, device=0, sort_interval=0):
+                 read_files=False, walls=WALLS_NONE, gravity=0.0, bead_mass=5.0, device=0, sort_interval=0,
+                 md_arith=MD_AUTO):
         o = CiliaOptions(precision, device, seed, ststep, int(create_fluid), int(read_files), walls, gravity,
-                         bead_mass, sort_interval)
+                         bead_mass, sort_interval, int(md_arith) + 1)
         h = ctypes.c_void_p()
         rc = lib().cilia_sim_create(cfg.encode() if isinstance(cfg, str) else cfg, int(is_text),
                                     ctypes.byref(o), ctypes.byref(h))
@@ -476,7 +488,7 @@ class Batch:
 
     def add_cfg(self, cfg, *, is_text=True, seed=1, ststep=0.0, bead_mass=5.0, create_fluid=True):
         """A replica built on the host from a sim.cfg (not yet admitted)."""
-        o = CiliaOptions(MPCD_FP32, 0, seed, ststep, int(create_fluid), 0, WALLS_NONE, 0.0, bead_mass, 0)
+        o = CiliaOptions(MPCD_FP32, 0, seed, ststep, int(create_fluid), 0, WALLS_NONE, 0.0, bead_mass, 0, 0)
         r = ctypes.c_int()
         rc = lib().cilia_batch_add_cfg(self._h, cfg.encode() if isinstance(cfg, str) else cfg, int(is_text),
                                        ctypes.byref(o), ctypes.byref(r))

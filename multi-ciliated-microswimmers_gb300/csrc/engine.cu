@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/mpcd_gpu.h"
+#include "df32.cuh"
 #include "engine_internal.h"
 #include "md_plan.h"
 #include "engine_export.h"
@@ -59,6 +60,7 @@ struct mpcd_engine {
   std::vector<double> newlen, oldlen;
   std::vector<int> slot_of;  // bead -> slot
   MDState md;
+  long md_nsp = 0;  // springs in the device layout
   bool md_dirty = true;
 
   // profiling: event pairs per launch, resolved on query
@@ -162,6 +164,13 @@ void free_md(MDState& m) {
   cudaFree(m.newlen);
   cudaFree(m.oldlen);
   cudaFree(m.tile_cil);
+  for (int b = 0; b < 2; ++b) cudaFree(m.q[b]);
+  cudaFree(m.sp_rest2);
+  cudaFree(m.sp_m2k2);
+  cudaFree(m.sp_code);
+  cudaFree(m.sp_split);
+  cudaFree(m.tile_b0);
+  cudaFree(m.tile_nb);
   GridBarrier bar = m.bar;
   m = MDState{};
   m.bar = bar;
@@ -276,11 +285,19 @@ int build_md(mpcd_engine* h) {
   in.nbond = (long)h->newlen.size();
   in.newlen = h->newlen.data();
   in.oldlen = h->oldlen.data();
-  in.split = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 0) : (h->p.md_split ? 1 : 0);
+  // -1: split springs with float32 cells, double-float with float64 cells
+  const int arith = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 2) : h->p.md_split;
+  if (arith > 2) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1 or 2");
+  in.split = arith == 1;
+  in.df = arith == 2;
   MDPlan pl;
-  const std::string why = plan_md(in, MDForce{}, true, false, h->p.precision == MPCD_FP32 ? 1 : 0, pl);
+  // MPCD_MD_NO_CLUSTER=1 keeps split arithmetic on the cooperative grid layout
+  const char* no_cl = std::getenv("MPCD_MD_NO_CLUSTER");
+  const bool allow_cluster = !(no_cl && std::atoi(no_cl) != 0);
+  const std::string why = plan_md(in, MDForce{}, allow_cluster, false, h->p.precision == MPCD_FP32 ? 1 : 0, pl);
   if (!why.empty()) return fail(h, MPCD_EINVAL, why);
   m.split = pl.split;
+  m.df = pl.df;
   m.cluster = pl.cluster;
   m.cl_lanes = pl.cl_lanes;
   m.cl_nsp_max = pl.cl_nsp_max;
@@ -292,6 +309,7 @@ int build_md(mpcd_engine* h) {
   m.hmax = pl.hmax;
   const int ns = m.nslots;
   const long nspk = pl.nsp_kept();
+  h->md_nsp = nspk;
   const size_t nbond = pl.newlen.size();
   const size_t ncil = pl.cd.size();
   for (int b = 0; b < 2; ++b) {
@@ -356,6 +374,33 @@ int build_md(mpcd_engine* h) {
     CK(up(m.newlen, pl.newlen.data(), nbond * 8));
     CK(up(m.oldlen, pl.oldlen.data(), nbond * 8));
     CK(up(m.diag, pl.diag.data(), nbond * 8));
+  }
+  if (m.df) {
+    // float pairs of the spring data and the packed layout; the position pair
+    // buffers are filled by the kernel
+    std::vector<float2> r2(nspk), k2(nspk);
+    for (long i = 0; i < nspk; ++i) {
+      const dfloat a = df_from_double(pl.srest[i]), b = df_from_double(pl.sm2k[i]);
+      r2[i] = make_float2(a.h, a.l);
+      k2[i] = make_float2(b.h, b.l);
+    }
+    m.df_nsp_max = pl.df_nsp_max;
+    m.df_nb_max = pl.df_nb_max;
+    for (int b = 0; b < 2; ++b) CK(dalloc(&m.q[b], 2 * (size_t)ns));
+    CK(dalloc(&m.sp_rest2, nspk));
+    CK(dalloc(&m.sp_m2k2, nspk));
+    CK(dalloc(&m.sp_code, nspk));
+    CK(dalloc(&m.sp_split, ns));
+    CK(dalloc(&m.tile_b0, m.ntiles));
+    CK(dalloc(&m.tile_nb, m.ntiles));
+    if (nspk) {
+      CK(up(m.sp_rest2, r2.data(), nspk * sizeof(float2)));
+      CK(up(m.sp_m2k2, k2.data(), nspk * sizeof(float2)));
+      CK(up(m.sp_code, pl.df_code.data(), nspk * sizeof(uint32_t)));
+    }
+    CK(up(m.sp_split, pl.df_split.data(), ns * sizeof(int)));
+    CK(up(m.tile_b0, pl.df_b0.data(), m.ntiles * sizeof(int)));
+    CK(up(m.tile_nb, pl.df_nb.data(), m.ntiles * sizeof(int)));
   }
   if (!pl.halo.empty()) CK(up(m.halo, pl.halo.data(), pl.halo.size() * 4));
   CK(up(m.halo_start, pl.hstart.data(), (m.ntiles + 1) * 4));
@@ -955,6 +1000,9 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
     if (h->md.cluster)
       h->launches += f64 ? launch_md_cluster_f64cells(h->md, h->c64, ma, h->stream, &coop)
                          : launch_md_cluster_f32cells(h->md, h->c32, ma, h->stream, &coop);
+    else if (h->md.df)
+      h->launches += f64 ? launch_md_df_f64cells(h->md, h->c64, ma, h->stream, &coop)
+                         : launch_md_df_f32cells(h->md, h->c32, ma, h->stream, &coop);
     else
       h->launches += f64 ? launch_md_f64(h->md, h->c64, ma, h->stream, &coop)
                          : launch_md_f32cells(h->md, h->c32, ma, h->stream, &coop);
@@ -1066,6 +1114,24 @@ int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* la
   resolve_marks(h);
   if (total_ms) *total_ms = h->prof_ms[kernel];
   if (launches) *launches = h->prof_n[kernel];
+  return MPCD_OK;
+}
+
+int mpcd_md_layout(mpcd_engine* h, int* info) {
+  if (!h || !info) return MPCD_EINVAL;
+  if (h->md_dirty) {
+    const int rc = build_md(h);
+    if (rc) return rc;
+  }
+  const MDState& m = h->md;
+  info[0] = m.cluster;
+  info[1] = m.cluster ? m.cl_lanes : 4;
+  info[2] = m.tile;
+  info[3] = m.ntiles;
+  info[4] = m.nslots;
+  info[5] = (int)h->md_nsp;
+  info[6] = m.hmax;
+  info[7] = m.df ? 2 : m.split;
   return MPCD_OK;
 }
 

@@ -119,6 +119,21 @@ struct MDState {
   int* sp_ref = nullptr;
   double* sp_rest = nullptr;
   double* sp_m2k = nullptr;  // -2k
+  // double-float arithmetic (md_df.cu): float pairs of the spring data,
+  // packed spring codes (other bead's staged index | kind << 16 | bond index
+  // within the tile << 18), per slot the end of its in-tile springs, per tile
+  // its bond range, and two position buffers of pairs, two float4 per slot
+  // ({hx, hy, hz, lx}, {ly, lz, 0, 0})
+  int df = 0;
+  int df_nsp_max = 0;  // most springs of one tile
+  int df_nb_max = 0;   // most bonds of one tile
+  float2* sp_rest2 = nullptr;
+  float2* sp_m2k2 = nullptr;
+  uint32_t* sp_code = nullptr;
+  int* sp_split = nullptr;
+  int* tile_b0 = nullptr;
+  int* tile_nb = nullptr;
+  float4* q[2] = {nullptr, nullptr};
   // cilia
   int ncil = 0;
   CiliumDev* cil = nullptr;
@@ -149,6 +164,9 @@ int launch_bin_fluid_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a
 int launch_bead_collide_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s);
 int launch_bin_beads_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s);
 int launch_md_f64(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+int launch_md_df_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+int launch_md_df_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+int md_df_max_coresident_blocks(const MDState& m, int f32cells);
 // reduce observables: out[0..2] sum m v, out[3] sum m v^2 (all), out[4] N, out[5] M,
 // out[6] sum v^2 over fluid, out[7] N fluid
 int launch_observables_f64(const FluidF64& f, const MDState& m, double bead_mass, double* out, cudaStream_t s);

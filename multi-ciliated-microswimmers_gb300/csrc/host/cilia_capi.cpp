@@ -51,6 +51,7 @@ cilia::SimOptions to_options(const cilia_options* o) {
   s.gravity = o->gravity;
   s.bead_mass = o->bead_mass > 0 ? o->bead_mass : 5.0;
   s.sort_interval = o->sort_interval;
+  s.md_split = o->md_arith > 0 ? o->md_arith - 1 : -1;
   return s;
 }
 }  // namespace

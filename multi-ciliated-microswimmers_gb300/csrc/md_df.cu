@@ -1,0 +1,493 @@
+// MD substeps of one MPC step for the float64 path, in double-float
+// arithmetic on the FP32 pipes.
+//
+// Same integrator and forces as md_kernels.cu (velocity Verlet of
+// src/libcilia/mdobject.cpp:36-72 inside the loop of src/simulation.cpp:217-265;
+// springs of src/cilia.cpp:127-239, src/sphere.cpp:87-119, src/clami.cpp:188-198)
+// on the same cooperative-grid tile layout (md_plan.cu: a CTA per tile, four
+// lanes per slot, helper slots for long spring lists, halos).  The difference
+// is the arithmetic: GB300 issues float64 at a small fraction of its float32
+// rate, and the float64 MD kernel spent most of its time on the FP64 pipe.
+// Here every bead's position and velocity live in registers as double-float
+// pairs (about 48 significand bits) for the whole MPC step; spring forces,
+// their sums and the Verlet updates are double-float operations built from
+// float adds, multiplies and fused multiply-adds.  The state is read from and
+// written back to the float64 arrays once per MPC step.  Rest lengths and
+// spring constants come as float pairs prepared on the host.
+//
+// Each CTA keeps its tile's spring table, bond table and halo slot list in
+// shared memory for the whole launch.  Positions are exchanged between tiles
+// through two global buffers of pairs (two float4 per bead) after a bounded
+// grid barrier: the halo arrives by asynchronous copies (cp.async, through
+// L2) while the lanes work on the springs between beads of their own tile,
+// and is waited for before the springs that reach it.  A bead with helper
+// slots sums their partial forces in blocks (the block leaders in parallel,
+// then the primary over the block sums), always in slot order.
+//
+// The cilia's rest lengths: the beat's target length of every bond is fixed
+// during one MPC step's substeps (the midpoint moves after them), so it is
+// computed once per launch in float64; the bending-rate limit that uses the
+// current bond length runs in pairs at every refresh (every 0.01 time units).
+#include "../../include/mpcd_gpu.h"
+#include "df32.cuh"
+#include "md_common.cuh"
+
+namespace mpcd {
+
+namespace {
+
+constexpr int kDfLanes = 4;
+constexpr int kHelpBlock = 8;  // helper partial sums added in blocks of this many slots
+
+// 16-byte asynchronous global -> shared copy through L2 (cp.async.cg)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Staged positions: entry i is two float4, {hx, hy, hz, lx} and {ly, lz, 0, 0}.
+struct StageDF {
+  const float4* p;
+  __device__ dfloat cx(int i) const { return {p[2 * i].x, p[2 * i].w}; }
+  __device__ dfloat cy(int i) const { return {p[2 * i].y, p[2 * i + 1].x}; }
+  __device__ dfloat cz(int i) const { return {p[2 * i].z, p[2 * i + 1].y}; }
+  // float64 distance (switch_logic's bend measure)
+  __device__ double dist(int i, int j) const {
+    const double dx = df_to_double(cx(i)) - df_to_double(cx(j));
+    const double dy = df_to_double(cy(i)) - df_to_double(cy(j));
+    const double dz = df_to_double(cz(i)) - df_to_double(cz(j));
+    return sqrt(dx * dx + dy * dy + dz * dz);
+  }
+};
+
+// Difference of two staged positions as pairs (exact high parts, low parts
+// added) and its squared length as a normalised pair.
+struct DfDiff {
+  dfloat dx, dy, dz, d2;
+};
+__device__ __forceinline__ DfDiff df_diff(const float4 a0, const float4 a1, const float4 b0, const float4 b1) {
+  DfDiff r;
+  r.dx = df_two_sum(a0.x, -b0.x);
+  r.dy = df_two_sum(a0.y, -b0.y);
+  r.dz = df_two_sum(a0.z, -b0.z);
+  r.dx.l = __fadd_rn(r.dx.l, __fsub_rn(a0.w, b0.w));
+  r.dy.l = __fadd_rn(r.dy.l, __fsub_rn(a1.x, b1.x));
+  r.dz.l = __fadd_rn(r.dz.l, __fsub_rn(a1.y, b1.y));
+  const dfloat px = df_two_prod(r.dx.h, r.dx.h), py = df_two_prod(r.dy.h, r.dy.h), pz = df_two_prod(r.dz.h, r.dz.h);
+  const dfloat q1 = df_two_sum(px.h, py.h);
+  const dfloat q2 = df_two_sum(q1.h, pz.h);
+  float low = (q1.l + q2.l) + (px.l + py.l + pz.l);
+  low += 2.0f * (r.dx.h * r.dx.l + r.dy.h * r.dy.l + r.dz.h * r.dz.l);
+  low += r.dx.l * r.dx.l + r.dy.l * r.dy.l + r.dz.l * r.dz.l;
+  r.d2 = df_fast_two_sum(q2.h, low);
+  return r;
+}
+
+// Tile-resident spring and bond tables in shared memory.
+struct Tables {
+  const uint32_t* code;  // other bead | kind << 16 | bond << 18
+  const float2* rest;    // static rest length (kinds CONST, GUARDED)
+  const float2* m2k;     // -2k
+  const float2* nl;      // bonds: current rest length (newlength)
+  const float2* dg;      // bonds: diagonal rest length sqrt(0.5^2 + 0.5 newlength)
+};
+
+// Force on staged bead `me` from springs [a, b) step kDfLanes (indices local
+// to the tile's table).  Per spring, with d = x_me - x_o and rest length b:
+// fac = -2k (1 - b / |d|), F += fac d, all in pairs; components accumulate as
+// compensated sums (h, l).
+__device__ __forceinline__ void springs_df(const Tables& tb, const float4* st, const float4 m0, const float4 m1, int a,
+                                           int b, float& fxh, float& fxl, float& fyh, float& fyl, float& fzh,
+                                           float& fzl) {
+  for (int s = a; s < b; s += kDfLanes) {
+    const uint32_t code = tb.code[s];
+    const int o = (int)(code & 0xffffu);
+    const int kind = (int)((code >> 16) & 3u);
+    const int lref = (int)(code >> 18);
+    const float2 b2 = kind <= MPCD_SPRING_GUARDED ? tb.rest[s] : (kind == MPCD_SPRING_BOND ? tb.nl[lref] : tb.dg[lref]);
+    const float2 k2 = tb.m2k[s];
+    const DfDiff d = df_diff(m0, m1, st[2 * o], st[2 * o + 1]);
+    if (kind == MPCD_SPRING_GUARDED && d.d2.h == 0.0f) continue;  // vector-form spring: no force at zero distance
+    const dfloat r = df_rsqrt(d.d2);
+    // w = 1 - b r
+    const dfloat u = df_two_prod(b2.x, r.h);
+    const dfloat w = df_two_sum(1.0f, -u.h);
+    const float wl = ((w.l - u.l) - b2.x * r.l) - b2.y * r.h;
+    // fac = -2k w
+    const dfloat f = df_two_prod(k2.x, w.h);
+    const float fl = (f.l + k2.x * wl) + k2.y * w.h;
+    const dfloat gx = df_two_prod(f.h, d.dx.h), gy = df_two_prod(f.h, d.dy.h), gz = df_two_prod(f.h, d.dz.h);
+    df_acc(fxh, fxl, gx.h, (gx.l + f.h * d.dx.l) + fl * d.dx.h);
+    df_acc(fyh, fyl, gy.h, (gy.l + f.h * d.dy.l) + fl * d.dy.h);
+    df_acc(fzh, fzl, gz.h, (gz.l + f.h * d.dz.l) + fl * d.dz.h);
+  }
+}
+
+// v += F c (pairs)
+__device__ __forceinline__ void kick(dfloat& v, dfloat f, dfloat c) { v = df_add(v, df_mul(f, c)); }
+
+// shared-memory layout of one tile
+struct DfSmem {
+  size_t st, code, rest, m2k, nl, ol, dg, tg, bd, part, bsum, hidx, total;
+  __host__ __device__ DfSmem(int T, int hmax, int nsp, int nb) {
+    size_t o = 0;
+    auto take = [&](size_t bytes, size_t align) {
+      o = (o + align - 1) / align * align;
+      const size_t r = o;
+      o += bytes;
+      return r;
+    };
+    st = take(32 * (size_t)(T + hmax), 16);
+    rest = take(8 * (size_t)nsp, 8);
+    m2k = take(8 * (size_t)nsp, 8);
+    nl = take(8 * (size_t)nb, 8);
+    ol = take(8 * (size_t)nb, 8);
+    dg = take(8 * (size_t)nb, 8);
+    tg = take(8 * (size_t)nb, 8);
+    bd = take(8 * (size_t)nb, 8);
+    code = take(4 * (size_t)nsp, 4);
+    part = take(24 * (size_t)T, 4);
+    bsum = take(24 * (size_t)T, 4);
+    hidx = take(4 * (size_t)hmax, 4);
+    total = o;
+  }
+};
+
+template <typename Bin>
+__device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int T = m.tile;
+  const DfSmem L(T, m.hmax, m.df_nsp_max, m.df_nb_max);
+  float4* st = reinterpret_cast<float4*>(smem + L.st);
+  uint32_t* s_code = reinterpret_cast<uint32_t*>(smem + L.code);
+  float2* s_rest = reinterpret_cast<float2*>(smem + L.rest);
+  float2* s_m2k = reinterpret_cast<float2*>(smem + L.m2k);
+  float2* s_nl = reinterpret_cast<float2*>(smem + L.nl);
+  float2* s_ol = reinterpret_cast<float2*>(smem + L.ol);
+  float2* s_dg = reinterpret_cast<float2*>(smem + L.dg);
+  float2* s_tg = reinterpret_cast<float2*>(smem + L.tg);
+  float2* s_bd = reinterpret_cast<float2*>(smem + L.bd);
+  float* part = reinterpret_cast<float*>(smem + L.part);  // per slot: its lanes' force (6 floats)
+  float* bsum = reinterpret_cast<float*>(smem + L.bsum);  // per helper block leader: block sum
+  int* hidx = reinterpret_cast<int*>(smem + L.hidx);
+  const Tables tb{s_code, s_rest, s_m2k, s_nl, s_dg};
+  const StageDF sv{st};
+
+  const int tile = blockIdx.x;
+  const int base = tile * T;
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+  // spring lanes: four per slot; springs [s0, sm) reach in-tile beads, [sm, s1) the halo
+  const int q = tid / kDfLanes, lane = tid % kDfLanes;
+  const int slot = base + q;
+  const int S0 = m.sp_start[base];
+  const int mv = m.moves[slot];
+  const int me = mv >= 0 ? m.prim[slot] - base : 0;
+  const int s0 = m.sp_start[slot] - S0, sm = m.sp_split[slot] - S0, s1 = m.sp_start[slot + 1] - S0;
+  // bead owners: thread tid < T owns slot base + tid
+  const int oslot = base + tid;
+  const int omv = tid < T ? m.moves[oslot] : -1;
+  const bool oprim = omv == 0 || omv == 1, omoves = omv == 1;
+  const bool helpers = m.tile_help[tile] != 0;
+  // helper blocks: a primary and its helpers form a run of 1 + nh slots; the
+  // slots at offsets 0, kHelpBlock, 2 kHelpBlock ... of the run sum the parts
+  // of their block, and the primary sums the block sums, all in slot order
+  int blk_n = 0, run_blocks = 0;
+  if (helpers && tid < T && omv >= 0) {
+    const int p = m.prim[oslot] - base;
+    const int j = tid - p;
+    const int nh = m.nhelp[base + p];
+    if (j % kHelpBlock == 0) blk_n = min(kHelpBlock, nh + 1 - j);
+    if (j == 0) run_blocks = (nh + kHelpBlock) / kHelpBlock;
+  }
+  const int h0 = m.halo_start[tile], hn = m.halo_start[tile + 1] - h0;
+  const int c0 = m.tile_cil[tile], c1 = m.tile_cil[tile + 1];
+  const int b0 = m.tile_b0[tile], nb = m.tile_nb[tile];
+  const int nsp = m.sp_start[base + T] - S0;
+  const dfloat dt = df_from_double(a.dt), dt2 = df_from_double(a.dt / 2.0);
+
+  // tile-resident tables
+  for (int i = tid; i < hn; i += nthr) hidx[i] = m.halo[h0 + i];
+  for (int i = tid; i < nsp; i += nthr) {
+    s_code[i] = __ldg(m.sp_code + S0 + i);
+    s_rest[i] = __ldg(m.sp_rest2 + S0 + i);
+    s_m2k[i] = __ldg(m.sp_m2k2 + S0 + i);
+  }
+  for (int i = tid; i < nb; i += nthr) {
+    const dfloat n = df_from_double(m.newlen[b0 + i]), o = df_from_double(m.oldlen[b0 + i]);
+    const dfloat g = df_from_double(m.diag[b0 + i]);
+    s_nl[i] = make_float2(n.h, n.l);
+    s_ol[i] = make_float2(o.h, o.l);
+    s_dg[i] = make_float2(g.h, g.l);
+  }
+  // the beat's rest length of every refreshed bond for this step, and the bending limit
+  {
+    int off = 0;
+    for (int c = c0; c < c1; ++c) {
+      const CiliumDev cl = m.cil[c];
+      const int nbnd = cl.len - cl.num_anker;
+      const int w = tid - off;
+      if (w >= 0 && w < nbnd) {
+        const int i = cl.num_anker - 1 + w;
+        const int k = cl.bond_base + i - b0;
+        const dfloat t = df_from_double(cilium_target(cl, i, m.midpnt[c]));
+        const dfloat bd = df_from_double(cl.bending);
+        s_tg[k] = make_float2(t.h, t.l);
+        s_bd[k] = make_float2(bd.h, bd.l);
+      }
+      off += nbnd;
+    }
+  }
+  dfloat x{0.f, 0.f}, y{0.f, 0.f}, z{0.f, 0.f}, vx{0.f, 0.f}, vy{0.f, 0.f}, vz{0.f, 0.f};
+  dfloat fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
+  if (oprim) {
+    x = df_from_double(m.x[0][oslot]);
+    y = df_from_double(m.y[0][oslot]);
+    z = df_from_double(m.z[0][oslot]);
+    vx = df_from_double(m.vx[oslot]);
+    vy = df_from_double(m.vy[oslot]);
+    vz = df_from_double(m.vz[oslot]);
+  }
+  const unsigned nblocks = gridDim.x;
+  unsigned barriers = 0;
+  int eval = 0;
+  bool refreshed = false;
+
+  // own beads into shared memory and the global pair buffer b
+  auto publish = [&](int b) {
+    if (oprim) {
+      const float4 p0 = make_float4(x.h, y.h, z.h, x.l), p1 = make_float4(y.l, z.l, 0.f, 0.f);
+      st[2 * tid] = p0;
+      st[2 * tid + 1] = p1;
+      m.q[b][2 * oslot] = p0;
+      m.q[b][2 * oslot + 1] = p1;
+    }
+  };
+  // forces on the owned beads; buffer b holds the other tiles' beads
+  auto evaluate = [&](int b) {
+    // other tiles' beads: asynchronous copies, waited for before the halo springs
+    const float4* src = m.q[b];
+    for (int i = tid; i < hn; i += nthr) {
+      const int g = hidx[i];
+      cp_async16(st + 2 * (T + i), src + 2 * g);
+      cp_async16(st + 2 * (T + i) + 1, src + 2 * g + 1);
+    }
+    if (c1 > c0 && refresh_due(a, eval)) {
+      // Cilia::length (src/cilia.cpp:79-121) for every refreshed bond, in pairs
+      refreshed = true;
+      int off = 0;
+      for (int c = c0; c < c1; ++c) {
+        const CiliumDev cl = m.cil[c];
+        const int nbnd = cl.len - cl.num_anker;
+        const int w = tid - off;
+        if (w >= 0 && w < nbnd) {
+          const int i = cl.num_anker - 1 + w;
+          const int k = cl.bond_base + i - b0;
+          const int l0 = cl.slot0 - base;
+          const int ia = l0 + cl.stride * i, ib = l0 + cl.stride * (i + 1);
+          const DfDiff d = df_diff(st[2 * ia], st[2 * ia + 1], st[2 * ib], st[2 * ib + 1]);
+          const dfloat tl = df_mul(d.d2, df_rsqrt(d.d2));
+          const dfloat tg{s_tg[k].x, s_tg[k].y}, bd{s_bd[k].x, s_bd[k].y}, ol{s_ol[k].x, s_ol[k].y};
+          dfloat l = tg;
+          if (df_lt(bd, df_abs(df_sub(tg, tl)))) {
+            const dfloat t2 = df_lt(tg, tl) ? df_sub(tl, bd) : df_add(tl, bd);
+            l = df_sign(df_sub(tg, ol)) * df_sign(df_sub(t2, ol)) > 0 ? t2 : ol;
+          }
+          const dfloat g = df_sqrt(df_add(dfloat{0.25f, 0.f}, df_mul(dfloat{0.5f, 0.f}, l)));
+          s_nl[k] = make_float2(l.h, l.l);
+          s_ol[k] = make_float2(l.h, l.l);
+          s_dg[k] = make_float2(g.h, g.l);
+        }
+        off += nbnd;
+      }
+      __syncthreads();
+    }
+    ++eval;
+    float axh = 0.f, axl = 0.f, ayh = 0.f, ayl = 0.f, azh = 0.f, azl = 0.f;
+    float4 m0 = make_float4(0.f, 0.f, 0.f, 0.f), m1 = m0;
+    if (mv >= 0) {
+      m0 = st[2 * me];
+      m1 = st[2 * me + 1];
+      springs_df(tb, st, m0, m1, s0 + lane, sm, axh, axl, ayh, ayl, azh, azl);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (mv >= 0) springs_df(tb, st, m0, m1, sm + lane, s1, axh, axl, ayh, ayl, azh, azl);
+    // fixed-order combination of the four lanes
+#pragma unroll
+    for (int o = 1; o < kDfLanes; o <<= 1) {
+      const float bxh = __shfl_xor_sync(0xffffffffu, axh, o), bxl = __shfl_xor_sync(0xffffffffu, axl, o);
+      const float byh = __shfl_xor_sync(0xffffffffu, ayh, o), byl = __shfl_xor_sync(0xffffffffu, ayl, o);
+      const float bzh = __shfl_xor_sync(0xffffffffu, azh, o), bzl = __shfl_xor_sync(0xffffffffu, azl, o);
+      df_acc(axh, axl, bxh, bxl);
+      df_acc(ayh, ayl, byh, byl);
+      df_acc(azh, azl, bzh, bzl);
+    }
+    if (lane == 0) {
+      float* pp = part + 6 * q;
+      pp[0] = axh;
+      pp[1] = axl;
+      pp[2] = ayh;
+      pp[3] = ayl;
+      pp[4] = azh;
+      pp[5] = azl;
+    }
+    __syncthreads();
+    if (helpers) {
+      if (blk_n > 0) {
+        const float* pp = part + 6 * tid;
+        float gxh = pp[0], gxl = pp[1], gyh = pp[2], gyl = pp[3], gzh = pp[4], gzl = pp[5];
+        for (int k = 1; k < blk_n; ++k) {
+          const float* ph = pp + 6 * k;
+          df_acc(gxh, gxl, ph[0], ph[1]);
+          df_acc(gyh, gyl, ph[2], ph[3]);
+          df_acc(gzh, gzl, ph[4], ph[5]);
+        }
+        float* bs = bsum + 6 * tid;
+        bs[0] = gxh;
+        bs[1] = gxl;
+        bs[2] = gyh;
+        bs[3] = gyl;
+        bs[4] = gzh;
+        bs[5] = gzl;
+      }
+      __syncthreads();
+      if (oprim) {
+        const float* pp = bsum + 6 * tid;
+        float gxh = pp[0], gxl = pp[1], gyh = pp[2], gyl = pp[3], gzh = pp[4], gzl = pp[5];
+        for (int k = 1; k < run_blocks; ++k) {
+          const float* ph = pp + 6 * kHelpBlock * k;
+          df_acc(gxh, gxl, ph[0], ph[1]);
+          df_acc(gyh, gyl, ph[2], ph[3]);
+          df_acc(gzh, gzl, ph[4], ph[5]);
+        }
+        fx = df_norm(gxh, gxl);
+        fy = df_norm(gyh, gyl);
+        fz = df_norm(gzh, gzl);
+      }
+    } else if (oprim) {
+      const float* pp = part + 6 * tid;
+      fx = df_norm(pp[0], pp[1]);
+      fy = df_norm(pp[2], pp[3]);
+      fz = df_norm(pp[4], pp[5]);
+    }
+  };
+  auto barrier = [&]() { return grid_sync(m.bar, ++barriers * nblocks, a.err); };
+
+  // md_loop_start: forces at t0, v += F dt/2, x += v dt
+  publish(0);
+  if (!barrier()) return;
+  evaluate(0);
+  int cur = 0;
+  if (omoves) {
+    kick(vx, fx, dt2);
+    kick(vy, fy, dt2);
+    kick(vz, fz, dt2);
+    kick(x, vx, dt);
+    kick(y, vy, dt);
+    kick(z, vz, dt);
+  }
+  publish(cur ^ 1);
+  if (!barrier()) return;
+  cur ^= 1;
+  evaluate(cur);
+  // md_loop: v += F dt, x += v dt, forces
+  for (int k = 1; k < a.n; ++k) {
+    if (omoves) {
+      kick(vx, fx, dt);
+      kick(vy, fy, dt);
+      kick(vz, fz, dt);
+      kick(x, vx, dt);
+      kick(y, vy, dt);
+      kick(z, vz, dt);
+    }
+    publish(cur ^ 1);
+    if (!barrier()) return;
+    cur ^= 1;
+    evaluate(cur);
+  }
+  // md_loop_stop: v += F dt/2, then bin with the next shift
+  if (omoves) {
+    kick(vx, fx, dt2);
+    kick(vy, fy, dt2);
+    kick(vz, fz, dt2);
+  }
+  if (oprim) {
+    const double X = df_to_double(x), Y = df_to_double(y), Z = df_to_double(z);
+    const double VX = df_to_double(vx), VY = df_to_double(vy), VZ = df_to_double(vz);
+    m.x[0][oslot] = X;
+    m.y[0][oslot] = Y;
+    m.z[0][oslot] = Z;
+    m.vx[oslot] = VX;
+    m.vy[oslot] = VY;
+    m.vz[oslot] = VZ;
+    if (omoves) bin(X, Y, Z, VX, VY, VZ);
+  }
+  // refreshed bonds back to float64
+  if (refreshed) {
+    int off = 0;
+    for (int c = c0; c < c1; ++c) {
+      const CiliumDev cl = m.cil[c];
+      const int nbnd = cl.len - cl.num_anker;
+      const int w = tid - off;
+      if (w >= 0 && w < nbnd) {
+        const int k = cl.bond_base + cl.num_anker - 1 + w;
+        const double l = df_to_double(dfloat{s_nl[k - b0].x, s_nl[k - b0].y});
+        m.newlen[k] = l;
+        m.oldlen[k] = l;
+        m.diag[k] = df_to_double(dfloat{s_dg[k - b0].x, s_dg[k - b0].y});
+      }
+      off += nbnd;
+    }
+  }
+  // switch_logic for the cilia of this tile (the staged positions are the final ones)
+  for (int c = c0 + tid; c < c1; c += nthr) cilium_switch(m, a, c, a.t_end, base, sv);
+}
+
+template <typename Bin>
+__global__ void __launch_bounds__(512) k_md_df(MDState m, typename Bin::Cells c, MDStepArgs a) {
+  md_df_body(m, a, Bin{c, &a});
+}
+
+size_t md_df_smem(const MDState& m) { return DfSmem(m.tile, m.hmax, m.df_nsp_max, m.df_nb_max).total; }
+
+template <typename Bin>
+int launch_df(const MDState& m, const typename Bin::Cells& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st) {
+  if (m.nslots == 0 || m.ntiles == 0) return 0;
+  cudaMemsetAsync(m.bar.count, 0, 2 * sizeof(unsigned), s);  // count and gen are adjacent
+  MDState mm = m;
+  typename Bin::Cells cc = c;
+  MDStepArgs aa = a;
+  void* args[] = {&mm, &cc, &aa};
+  const size_t smem = md_df_smem(m);
+  const void* k = (const void*)k_md_df<Bin>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  *st = cudaLaunchCooperativeKernel(k, dim3(m.ntiles), dim3(kDfLanes * m.tile), args, smem, s);
+  return 1;
+}
+
+}  // namespace
+
+int launch_md_df_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st) {
+  return launch_df<BinF64>(m, c, a, s, st);
+}
+
+int launch_md_df_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st) {
+  return launch_df<BinF32>(m, c, a, s, st);
+}
+
+int md_df_max_coresident_blocks(const MDState& m, int f32cells) {
+  int dev = 0, sms = 0, per_sm = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t smem = md_df_smem(m);
+  if (smem > (size_t)optin) return 0;
+  const void* k = f32cells ? (const void*)k_md_df<BinF32> : (const void*)k_md_df<BinF64>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kDfLanes * m.tile, smem);
+  return per_sm * sms;
+}
+
+}  // namespace mpcd

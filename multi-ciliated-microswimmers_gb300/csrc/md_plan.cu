@@ -6,6 +6,7 @@
 // one chunk).  Every cilium occupies contiguous slots of one tile, so that its
 // beat bookkeeping needs no synchronisation beyond its CTA.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <utility>
@@ -19,11 +20,13 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
   // springs per helper slot: the longest serial spring chain of any thread.
   // Odd, so that the helper slots' spring lists start in different
   // shared-memory banks.
-  int kChunk = 31;
+  // The double-float grid kernel's springs cost more per lane: shorter chunks.
+  int kChunk = in.df && !in.split ? 15 : 31;
   if (const char* env = std::getenv("MPCD_MD_CHUNK")) kChunk = std::max(2, std::min(256, std::atoi(env)));
   out = MDPlan{};
   const bool forced = force.lanes > 0;
   out.split = in.split;
+  out.df = in.df && !in.split;
   if (in.nb == 0) return "";
   const long nb = in.nb;
   const long nsp = in.nsp;
@@ -262,7 +265,8 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     std::fill(dropped.begin(), dropped.end(), 0);
     maxw = widest();
     tile = std::max(32, ((maxw + 15) / 16) * 16);
-    if (tile > 1024) return "an MD group needs more than 1024 slots";
+    if (tile > 256) return "an MD group needs more than 256 slots";  // four threads per slot
+    if (tile > 128) out.df = 0;  // the double-float kernel runs at most 512 threads per CTA
     pack(tile);
   }
   // a hub and all its partners must share one tile, one hub per tile
@@ -400,12 +404,75 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     hmax = std::max(hmax, (int)ext.size());
   }
   out.hmax = hmax;
+  // double-float grid kernel: per slot, the springs whose other bead is in the
+  // tile first (they run while the halo loads are in flight); per tile, the
+  // bond range its BOND/DIAG springs and cilia use; packed spring codes
+  if (out.df) {
+    out.df_split.assign(ns, 0);
+    out.df_code.assign(nspk, 0u);
+    out.df_b0.assign(out.ntiles, 0);
+    out.df_nb.assign(out.ntiles, 0);
+    std::vector<int> b0(out.ntiles, INT_MAX), b1(out.ntiles, 0);
+    for (int c = 0; c < ncil; ++c) {
+      const int t = cil_tile[c];
+      b0[t] = std::min(b0[t], in.cil[c].bond_base);
+      b1[t] = std::max(b1[t], in.cil[c].bond_base + in.cil[c].rodlength);
+    }
+    for (int t = 0; t < out.ntiles; ++t) {
+      if (b0[t] > b1[t]) b0[t] = b1[t] = 0;
+      out.df_b0[t] = b0[t];
+      out.df_nb[t] = b1[t] - b0[t];
+      out.df_nb_max = std::max(out.df_nb_max, out.df_nb[t]);
+      out.df_nsp_max = std::max(out.df_nsp_max, start[(t + 1) * tile] - start[t * tile]);
+    }
+    std::vector<long> idx;
+    for (int sl_ = 0; sl_ < ns; ++sl_) {
+      const int a0 = start[sl_], a1 = start[sl_ + 1];
+      idx.clear();
+      for (int k = a0; k < a1; ++k)
+        if (out.sl[k] < tile) idx.push_back(k);
+      out.df_split[sl_] = a0 + (int)idx.size();
+      for (int k = a0; k < a1; ++k)
+        if (out.sl[k] >= tile) idx.push_back(k);
+      std::vector<int> so(a1 - a0), sk(a1 - a0), sr(a1 - a0), slv(a1 - a0);
+      std::vector<double> srest(a1 - a0), sm2k(a1 - a0);
+      for (int k = 0; k < a1 - a0; ++k) {
+        so[k] = out.so[idx[k]];
+        sk[k] = out.sk[idx[k]];
+        sr[k] = out.sr[idx[k]];
+        slv[k] = out.sl[idx[k]];
+        srest[k] = out.srest[idx[k]];
+        sm2k[k] = out.sm2k[idx[k]];
+      }
+      const int t = sl_ / tile;
+      for (int k = 0; k < a1 - a0; ++k) {
+        const int d = a0 + k;
+        out.so[d] = so[k];
+        out.sk[d] = sk[k];
+        out.sr[d] = sr[k];
+        out.sl[d] = slv[k];
+        out.srest[d] = srest[k];
+        out.sm2k[d] = sm2k[k];
+        const int kind = sk[k] & 3;
+        int lref = 0;
+        if (kind >= MPCD_SPRING_BOND) {
+          lref = sr[k] - out.df_b0[t];
+          if (lref < 0 || lref >= out.df_nb[t]) return "a bond spring refers to a bond outside its tile's cilia";
+        }
+        if (slv[k] >= (1 << 16) || lref >= (1 << 14)) return "an MD tile is too large for packed spring codes";
+        out.df_code[d] = (uint32_t)slv[k] | ((uint32_t)kind << 16) | ((uint32_t)lref << 18);
+      }
+    }
+  }
   MDState probe;  // the fields the feasibility checks read
   probe.tile = tile;
   probe.ntiles = out.ntiles;
   probe.nslots = ns;
   probe.hmax = hmax;
   probe.split = out.split;
+  probe.df = out.df;
+  probe.df_nsp_max = out.df_nsp_max;
+  probe.df_nb_max = out.df_nb_max;
   probe.cluster = out.cluster;
   probe.cl_lanes = out.cl_lanes;
   if (out.cluster) {

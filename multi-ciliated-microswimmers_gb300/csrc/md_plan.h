@@ -25,6 +25,7 @@ struct MDInput {
   long nbond = 0;
   const double *newlen = nullptr, *oldlen = nullptr;
   int split = 0;  // 1: float spring arithmetic on hi/lo position pairs
+  int df = 0;     // 1: double-float arithmetic (md_df.cu; grid layout, split 0)
 };
 
 // A fixed cluster layout (lanes per slot, slots per tile), or {0, 0} to let
@@ -37,7 +38,7 @@ struct MDForce {
 // Host arrays of an MDState (engine_internal.h), indices local to the box.
 struct MDPlan {
   int tile = 0, ntiles = 0, nslots = 0, hmax = 0;
-  int split = 0, cluster = 0, cl_nsp_max = 0, cl_nbond_max = 0, cl_lanes = 2, cl_nbuf = 2;
+  int split = 0, df = 0, cluster = 0, cl_nsp_max = 0, cl_nbond_max = 0, cl_lanes = 2, cl_nbuf = 2;
   std::vector<double> X, Y, Z, VX, VY, VZ;
   std::vector<int> mv, prim, nhelp, thelp, tile_react;
   std::vector<int> start, so, sl, sk, sr;
@@ -47,6 +48,10 @@ struct MDPlan {
   std::vector<double> mid, ts, newlen, oldlen, diag;
   std::vector<int> tcil;
   std::vector<int> slot_of;  // bead -> primary slot
+  // double-float grid kernel (md_df.cu)
+  std::vector<int> df_split, df_b0, df_nb;
+  std::vector<uint32_t> df_code;
+  int df_nsp_max = 0, df_nb_max = 0;
   long nsp_kept() const { return (long)so.size(); }
 };
 

@@ -58,13 +58,16 @@ def test_fluid_matches_reference_golden(case):
     assert abs(obs["diss_energy"] - g[f"step{int(steps)}_meta"][1]) < 1e-8 * max(1, abs(g[f"step{int(steps)}_meta"][1]))
 
 
+@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64])
 @pytest.mark.parametrize("case", ["clami10", "objects8"])
-def test_swimmer_matches_reference_golden(case):
+def test_swimmer_matches_reference_golden(case, arith):
+    """MD substeps in double-float (the float64 path's default) and in float64."""
     g = golden(case)
     seed, steps, ststep = g["params"]
     text = open(f"{GOLDEN}/cases/{case}.cfg").read()
-    s = cg.Sim(text, precision=cg.MPCD_FP64, ststep=float(ststep), create_fluid=False)
+    s = cg.Sim(text, precision=cg.MPCD_FP64, ststep=float(ststep), create_fluid=False, md_arith=arith)
     e = s.engine
+    assert e.md_layout()["arith"] == arith
     # geometry built by the host object model equals the reference's
     bp, bv = s.beads()
     rp, rv = ref_beads(g, "step0")
@@ -83,6 +86,38 @@ def test_swimmer_matches_reference_golden(case):
     assert np.abs(bp - rp).max() < POS_TOL
     assert np.abs(bv - rv).max() < 1e-8
     assert abs(e.time - g[f"step{int(steps)}_meta"][0]) < 1e-12
+
+
+@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64])
+def test_multi_tile_swimmer_matches_oracle(arith):
+    """A Clami whose cilia fill many MD tiles (halos between tiles, a sphere
+    centre with helper slots) against the C oracle, injected randomness, 6 MPC
+    steps of 50 substeps."""
+    cfg = simcfg.swimmer_config(16, radius=4.0, n_cilia=24, rodlength=10, seed=3, ststep=0.002)
+    o = build_from_cfg(cfg, seed=5, ststep=0.002)
+    s = cg.Sim(simcfg.dumps(cfg), precision=cg.MPCD_FP64, ststep=0.002, create_fluid=False, md_arith=arith)
+    e = s.engine
+    lay = e.md_layout()
+    assert lay["arith"] == arith and lay["cluster"] == 0 and lay["ntiles"] > 4 and lay["hmax"] > 0
+    p0, v0 = o.fluid()
+    e.set_fluid(p0, v0)
+    e.shift = o.shift
+    bp, _ = s.beads()
+    op, _ = o.beads()
+    assert np.abs(bp - op).max() < 1e-13
+    L = (16, 16, 16)
+    for _ in range(6):
+        rs, rg, ra, _ = o.step(record=True)
+        s.next_tstep(rs, rg, ra)
+    bp, bv = s.beads()
+    op, ov = o.beads()
+    assert np.abs(bp - op).max() < POS_TOL
+    assert np.abs(bv - ov).max() < 1e-8
+    p, v = e.fluid()
+    po, vo = o.fluid()
+    assert np.abs(periodic_diff(p, po, L)).max() < POS_TOL
+    assert np.abs(v - vo).max() < VEL_TOL
+    s.close()
 
 
 def _oracle_fluid(L, seed, ststep=0.002):
