@@ -171,6 +171,10 @@ void free_md(MDState& m) {
   cudaFree(m.sp_split);
   cudaFree(m.tile_b0);
   cudaFree(m.tile_nb);
+  cudaFree(m.halo_run);
+  cudaFree(m.halo_run_start);
+  cudaFree(m.halo_single);
+  cudaFree(m.halo_single_start);
   GridBarrier bar = m.bar;
   m = MDState{};
   m.bar = bar;
@@ -296,6 +300,8 @@ int build_md(mpcd_engine* h) {
   const bool allow_cluster = !(no_cl && std::atoi(no_cl) != 0);
   const std::string why = plan_md(in, MDForce{}, allow_cluster, false, h->p.precision == MPCD_FP32 ? 1 : 0, pl);
   if (!why.empty()) return fail(h, MPCD_EINVAL, why);
+  if (pl.hstart.size() != (size_t)pl.ntiles + 1 || pl.halo.size() != (size_t)pl.hstart.back())
+    return fail(h, MPCD_EINVAL, "MD plan: halo lists inconsistent with their offsets");
   m.split = pl.split;
   m.df = pl.df;
   m.cluster = pl.cluster;
@@ -386,6 +392,8 @@ int build_md(mpcd_engine* h) {
     }
     m.df_nsp_max = pl.df_nsp_max;
     m.df_nb_max = pl.df_nb_max;
+    m.df_nrun_max = pl.df_nrun_max;
+    m.df_nsingle_max = pl.df_nsingle_max;
     for (int b = 0; b < 2; ++b) CK(dalloc(&m.q[b], 2 * (size_t)ns));
     CK(dalloc(&m.sp_rest2, nspk));
     CK(dalloc(&m.sp_m2k2, nspk));
@@ -401,6 +409,14 @@ int build_md(mpcd_engine* h) {
     CK(up(m.sp_split, pl.df_split.data(), ns * sizeof(int)));
     CK(up(m.tile_b0, pl.df_b0.data(), m.ntiles * sizeof(int)));
     CK(up(m.tile_nb, pl.df_nb.data(), m.ntiles * sizeof(int)));
+    CK(dalloc(&m.halo_run, std::max<size_t>(1, pl.df_runs.size())));
+    CK(dalloc(&m.halo_run_start, m.ntiles + 1));
+    if (!pl.df_runs.empty()) CK(up(m.halo_run, pl.df_runs.data(), pl.df_runs.size() * sizeof(int4)));
+    CK(up(m.halo_run_start, pl.df_run_start.data(), (m.ntiles + 1) * sizeof(int)));
+    CK(dalloc(&m.halo_single, std::max<size_t>(1, pl.df_single.size())));
+    CK(dalloc(&m.halo_single_start, m.ntiles + 1));
+    if (!pl.df_single.empty()) CK(up(m.halo_single, pl.df_single.data(), pl.df_single.size() * sizeof(int2)));
+    CK(up(m.halo_single_start, pl.df_single_start.data(), (m.ntiles + 1) * sizeof(int)));
   }
   if (!pl.halo.empty()) CK(up(m.halo, pl.halo.data(), pl.halo.size() * 4));
   CK(up(m.halo_start, pl.hstart.data(), (m.ntiles + 1) * 4));
@@ -1125,7 +1141,7 @@ int mpcd_md_layout(mpcd_engine* h, int* info) {
   }
   const MDState& m = h->md;
   info[0] = m.cluster;
-  info[1] = m.cluster ? m.cl_lanes : 4;
+  info[1] = m.cluster ? m.cl_lanes : (m.df ? md_df_lanes(m.tile) : 4);
   info[2] = m.tile;
   info[3] = m.ntiles;
   info[4] = m.nslots;

@@ -127,12 +127,18 @@ struct MDState {
   int df = 0;
   int df_nsp_max = 0;  // most springs of one tile
   int df_nb_max = 0;   // most bonds of one tile
+  int df_nrun_max = 0;     // most long halo runs of one tile
+  int df_nsingle_max = 0;  // most other halo entries of one tile
   float2* sp_rest2 = nullptr;
   float2* sp_m2k2 = nullptr;
   uint32_t* sp_code = nullptr;
   int* sp_split = nullptr;
   int* tile_b0 = nullptr;
   int* tile_nb = nullptr;
+  int4* halo_run = nullptr;        // per tile: runs of consecutive halo slots {first, rank, length, 0}
+  int* halo_run_start = nullptr;   // ntiles + 1
+  int2* halo_single = nullptr;     // per tile: halo entries outside long runs {slot, rank}
+  int* halo_single_start = nullptr;
   float4* q[2] = {nullptr, nullptr};
   // cilia
   int ncil = 0;
@@ -167,6 +173,7 @@ int launch_md_f64(const MDState& m, const CellsF64& c, const MDStepArgs& a, cuda
 int launch_md_df_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
 int launch_md_df_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
 int md_df_max_coresident_blocks(const MDState& m, int f32cells);
+int md_df_lanes(int tile);  // threads per slot of the double-float kernel
 // reduce observables: out[0..2] sum m v, out[3] sum m v^2 (all), out[4] N, out[5] M,
 // out[6] sum v^2 over fluid, out[7] N fluid
 int launch_observables_f64(const FluidF64& f, const MDState& m, double bead_mass, double* out, cudaStream_t s);

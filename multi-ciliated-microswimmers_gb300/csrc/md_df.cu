@@ -4,8 +4,9 @@
 // Same integrator and forces as md_kernels.cu (velocity Verlet of
 // src/libcilia/mdobject.cpp:36-72 inside the loop of src/simulation.cpp:217-265;
 // springs of src/cilia.cpp:127-239, src/sphere.cpp:87-119, src/clami.cpp:188-198)
-// on the same cooperative-grid tile layout (md_plan.cu: a CTA per tile, four
-// lanes per slot, helper slots for long spring lists, halos).  The difference
+// on the same cooperative-grid tile layout (md_plan.cu: a CTA per tile, helper
+// slots for long spring lists, halos), with eight lanes per slot (four for
+// tiles over 64 slots).  The difference
 // is the arithmetic: GB300 issues float64 at a small fraction of its float32
 // rate, and the float64 MD kernel spent most of its time on the FP64 pipe.
 // Here every bead's position and velocity live in registers as double-float
@@ -15,12 +16,13 @@
 // written back to the float64 arrays once per MPC step.  Rest lengths and
 // spring constants come as float pairs prepared on the host.
 //
-// Each CTA keeps its tile's spring table, bond table and halo slot list in
-// shared memory for the whole launch.  Positions are exchanged between tiles
-// through two global buffers of pairs (two float4 per bead) after a bounded
-// grid barrier: the halo arrives by asynchronous copies (cp.async, through
-// L2) while the lanes work on the springs between beads of their own tile,
-// and is waited for before the springs that reach it.  A bead with helper
+// Each CTA keeps its tile's spring and bond tables in shared memory for the
+// whole launch.  Positions are exchanged between tiles through two global
+// buffers of pairs (two float4 per bead) after a bounded grid barrier: the
+// halo arrives by bulk asynchronous copies (TMA, one per run of consecutive
+// slots, completing on an mbarrier) while the lanes work on the springs
+// between beads of their own tile, and is waited for (bounded) before the
+// springs that reach it.  A bead with helper
 // slots sums their partial forces in blocks (the block leaders in parallel,
 // then the primary over the block sums), always in slot order.
 //
@@ -28,52 +30,96 @@
 // during one MPC step's substeps (the midpoint moves after them), so it is
 // computed once per launch in float64; the bending-rate limit that uses the
 // current bond length runs in pairs at every refresh (every 0.01 time units).
+#include <cstdlib>
+
 #include "../../include/mpcd_gpu.h"
 #include "df32.cuh"
 #include "md_common.cuh"
+#include "tma.cuh"
 
 namespace mpcd {
 
 namespace {
 
-constexpr int kDfLanes = 4;
-constexpr int kHelpBlock = 8;  // helper partial sums added in blocks of this many slots
+constexpr int kHelpBlock = 8;            // helper partial sums added in blocks of this many slots
+constexpr uint32_t kHaloWait = 1u << 22;  // polls of the halo's mbarrier before giving up
 
 // 16-byte asynchronous global -> shared copy through L2 (cp.async.cg)
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-               : "memory");
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Staged positions: entry i is two float4, {hx, hy, hz, lx} and {ly, lz, 0, 0}.
+// A bead coordinate is an integer c plus an offset o in [0, 1) held as a
+// pair: o.h on the grid of multiples of 2^-24 (so that the difference of two
+// offsets is exact in float) and o.l the rest, |o.l| <= 2^-25.  Its resolution
+// (about 2^-48) does not depend on the distance from the origin.  Staged and
+// published entry: two float4,
+//   {ohx, ohy, ohz, olx} and {oly, olz, bits(cx | cy << 16), cz}
+// (cx, cy as 16-bit integers, cz as a float).
+struct BeadCoord {
+  int c;
+  dfloat o;
+};
+constexpr float kGrid = 16777216.0f;  // 2^24
+__device__ __forceinline__ BeadCoord coord_from_double(double x) {
+  const double c = floor(x);
+  const double o = x - c;                     // exact
+  const double h = floor(o * 16777216.0) / 16777216.0;  // exact, on the grid
+  return {(int)c, {(float)h, (float)(o - h)}};
+}
+__device__ __forceinline__ double coord_to_double(const BeadCoord& q) {
+  return (double)q.c + ((double)q.o.h + (double)q.o.l);
+}
+// q += v c; the offset's high part back on the grid and in [0, 1)
+__device__ __forceinline__ void coord_kick(BeadCoord& q, dfloat v, dfloat c) {
+  const dfloat o = df_add(q.o, df_mul(v, c));
+  float g = __fmul_rn(rintf(__fmul_rn(o.h, kGrid)), 1.0f / kGrid);  // exact
+  const float lo = __fadd_rn(__fsub_rn(o.h, g), o.l);                  // o.h - g exact
+  const float k = floorf(g);
+  g = __fsub_rn(g, k);  // exact: a grid value minus an integer
+  q.c += (int)k;
+  q.o = {g, lo};
+}
+__device__ __forceinline__ void pack_coords(const BeadCoord& x, const BeadCoord& y, const BeadCoord& z, float4& p0,
+                                            float4& p1) {
+  p0 = make_float4(x.o.h, y.o.h, z.o.h, x.o.l);
+  p1 = make_float4(y.o.l, z.o.l, __uint_as_float(((uint32_t)x.c & 0xffffu) | ((uint32_t)y.c << 16)), (float)z.c);
+}
+__device__ __forceinline__ int cell_x(const float4 p1) { return (int)(short)(__float_as_uint(p1.z) & 0xffffu); }
+__device__ __forceinline__ int cell_y(const float4 p1) { return (int)__float_as_uint(p1.z) >> 16; }
+
 struct StageDF {
   const float4* p;
-  __device__ dfloat cx(int i) const { return {p[2 * i].x, p[2 * i].w}; }
-  __device__ dfloat cy(int i) const { return {p[2 * i].y, p[2 * i + 1].x}; }
-  __device__ dfloat cz(int i) const { return {p[2 * i].z, p[2 * i + 1].y}; }
   // float64 distance (switch_logic's bend measure)
   __device__ double dist(int i, int j) const {
-    const double dx = df_to_double(cx(i)) - df_to_double(cx(j));
-    const double dy = df_to_double(cy(i)) - df_to_double(cy(j));
-    const double dz = df_to_double(cz(i)) - df_to_double(cz(j));
+    const float4 a0 = p[2 * i], a1 = p[2 * i + 1], b0 = p[2 * j], b1 = p[2 * j + 1];
+    const double dx = (double)(cell_x(a1) - cell_x(b1)) + (df_to_double({a0.x, a0.w}) - df_to_double({b0.x, b0.w}));
+    const double dy = (double)(cell_y(a1) - cell_y(b1)) + (df_to_double({a0.y, a1.x}) - df_to_double({b0.y, b1.x}));
+    const double dz = ((double)a1.w - (double)b1.w) + (df_to_double({a0.z, a1.y}) - df_to_double({b0.z, b1.y}));
     return sqrt(dx * dx + dy * dy + dz * dz);
   }
 };
 
-// Difference of two staged positions as pairs (exact high parts, low parts
-// added) and its squared length as a normalised pair.
+// one component of a difference: the cells' difference dc (an exact small
+// integer) plus the high parts' (exact: both on the 2^-24 grid, |difference|
+// < 1), summed exactly (FastTwoSum: |dc| >= 1 > |s| or dc == 0), then the
+// low parts
+__device__ __forceinline__ dfloat coord_diff(float dc, float ha, float hb, float la, float lb) {
+  const dfloat t = df_fast_two_sum(dc, __fsub_rn(ha, hb));
+  return {t.h, __fadd_rn(t.l, __fsub_rn(la, lb))};
+}
+
+// Difference of two staged positions as pairs and its squared length as a
+// normalised pair.
 struct DfDiff {
   dfloat dx, dy, dz, d2;
 };
 __device__ __forceinline__ DfDiff df_diff(const float4 a0, const float4 a1, const float4 b0, const float4 b1) {
   DfDiff r;
-  r.dx = df_two_sum(a0.x, -b0.x);
-  r.dy = df_two_sum(a0.y, -b0.y);
-  r.dz = df_two_sum(a0.z, -b0.z);
-  r.dx.l = __fadd_rn(r.dx.l, __fsub_rn(a0.w, b0.w));
-  r.dy.l = __fadd_rn(r.dy.l, __fsub_rn(a1.x, b1.x));
-  r.dz.l = __fadd_rn(r.dz.l, __fsub_rn(a1.y, b1.y));
+  r.dx = coord_diff((float)(cell_x(a1) - cell_x(b1)), a0.x, b0.x, a0.w, b0.w);
+  r.dy = coord_diff((float)(cell_y(a1) - cell_y(b1)), a0.y, b0.y, a1.x, b1.x);
+  r.dz = coord_diff(__fsub_rn(a1.w, b1.w), a0.z, b0.z, a1.y, b1.y);
   const dfloat px = df_two_prod(r.dx.h, r.dx.h), py = df_two_prod(r.dy.h, r.dy.h), pz = df_two_prod(r.dz.h, r.dz.h);
   const dfloat q1 = df_two_sum(px.h, py.h);
   const dfloat q2 = df_two_sum(q1.h, pz.h);
@@ -93,14 +139,15 @@ struct Tables {
   const float2* dg;      // bonds: diagonal rest length sqrt(0.5^2 + 0.5 newlength)
 };
 
-// Force on staged bead `me` from springs [a, b) step kDfLanes (indices local
+// Force on staged bead `me` from springs [a, b) step LANES (indices local
 // to the tile's table).  Per spring, with d = x_me - x_o and rest length b:
 // fac = -2k (1 - b / |d|), F += fac d, all in pairs; components accumulate as
 // compensated sums (h, l).
+template <int LANES>
 __device__ __forceinline__ void springs_df(const Tables& tb, const float4* st, const float4 m0, const float4 m1, int a,
                                            int b, float& fxh, float& fxl, float& fyh, float& fyl, float& fzh,
                                            float& fzl) {
-  for (int s = a; s < b; s += kDfLanes) {
+  for (int s = a; s < b; s += LANES) {
     const uint32_t code = tb.code[s];
     const int o = (int)(code & 0xffffu);
     const int kind = (int)((code >> 16) & 3u);
@@ -129,8 +176,8 @@ __device__ __forceinline__ void kick(dfloat& v, dfloat f, dfloat c) { v = df_add
 
 // shared-memory layout of one tile
 struct DfSmem {
-  size_t st, code, rest, m2k, nl, ol, dg, tg, bd, part, bsum, hidx, total;
-  __host__ __device__ DfSmem(int T, int hmax, int nsp, int nb) {
+  size_t st, bar, flag, runs, single, code, rest, m2k, nl, ol, dg, tg, bd, part, bsum, total;
+  __host__ __device__ DfSmem(int T, int hmax, int nsp, int nb, int nrun, int nsingle) {
     size_t o = 0;
     auto take = [&](size_t bytes, size_t align) {
       o = (o + align - 1) / align * align;
@@ -139,6 +186,10 @@ struct DfSmem {
       return r;
     };
     st = take(32 * (size_t)(T + hmax), 16);
+    bar = take(8, 8);
+    flag = take(4, 4);
+    runs = take(16 * (size_t)nrun, 16);
+    single = take(8 * (size_t)nsingle, 8);
     rest = take(8 * (size_t)nsp, 8);
     m2k = take(8 * (size_t)nsp, 8);
     nl = take(8 * (size_t)nb, 8);
@@ -149,16 +200,15 @@ struct DfSmem {
     code = take(4 * (size_t)nsp, 4);
     part = take(24 * (size_t)T, 4);
     bsum = take(24 * (size_t)T, 4);
-    hidx = take(4 * (size_t)hmax, 4);
     total = o;
   }
 };
 
-template <typename Bin>
+template <int LANES, typename Bin>
 __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int T = m.tile;
-  const DfSmem L(T, m.hmax, m.df_nsp_max, m.df_nb_max);
+  const DfSmem L(T, m.hmax, m.df_nsp_max, m.df_nb_max, m.df_nrun_max, m.df_nsingle_max);
   float4* st = reinterpret_cast<float4*>(smem + L.st);
   uint32_t* s_code = reinterpret_cast<uint32_t*>(smem + L.code);
   float2* s_rest = reinterpret_cast<float2*>(smem + L.rest);
@@ -170,7 +220,10 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   float2* s_bd = reinterpret_cast<float2*>(smem + L.bd);
   float* part = reinterpret_cast<float*>(smem + L.part);  // per slot: its lanes' force (6 floats)
   float* bsum = reinterpret_cast<float*>(smem + L.bsum);  // per helper block leader: block sum
-  int* hidx = reinterpret_cast<int*>(smem + L.hidx);
+  uint64_t* hbar = reinterpret_cast<uint64_t*>(smem + L.bar);  // halo copies' completion
+  int* hflag = reinterpret_cast<int*>(smem + L.flag);           // 1: the halo runs are valid
+  int4* s_runs = reinterpret_cast<int4*>(smem + L.runs);         // this tile's long halo runs
+  int2* s_single = reinterpret_cast<int2*>(smem + L.single);     // and its other halo entries
   const Tables tb{s_code, s_rest, s_m2k, s_nl, s_dg};
   const StageDF sv{st};
 
@@ -178,8 +231,8 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   const int base = tile * T;
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
-  // spring lanes: four per slot; springs [s0, sm) reach in-tile beads, [sm, s1) the halo
-  const int q = tid / kDfLanes, lane = tid % kDfLanes;
+  // spring lanes: LANES per slot; springs [s0, sm) reach in-tile beads, [sm, s1) the halo
+  const int q = tid / LANES, lane = tid % LANES;
   const int slot = base + q;
   const int S0 = m.sp_start[base];
   const int mv = m.moves[slot];
@@ -201,14 +254,45 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     if (j % kHelpBlock == 0) blk_n = min(kHelpBlock, nh + 1 - j);
     if (j == 0) run_blocks = (nh + kHelpBlock) / kHelpBlock;
   }
-  const int h0 = m.halo_start[tile], hn = m.halo_start[tile + 1] - h0;
+  const int h0 = m.halo_start[tile], hn0 = m.halo_start[tile + 1] - h0;
   const int c0 = m.tile_cil[tile], c1 = m.tile_cil[tile + 1];
   const int b0 = m.tile_b0[tile], nb = m.tile_nb[tile];
   const int nsp = m.sp_start[base + T] - S0;
   const dfloat dt = df_from_double(a.dt), dt2 = df_from_double(a.dt / 2.0);
 
+  // halo copies: long runs of consecutive slots by bulk copies (TMA) that
+  // complete on an mbarrier, the other entries by per-thread cp.async
+  const int r0 = m.halo_run_start[tile], nrun = m.halo_run_start[tile + 1] - r0;
+  const int e0 = m.halo_single_start[tile], nsingle = m.halo_single_start[tile + 1] - e0;
+  for (int r = tid; r < nrun && nrun <= m.df_nrun_max; r += nthr) s_runs[r] = m.halo_run[r0 + r];
+  for (int i = tid; i < nsingle && nsingle <= m.df_nsingle_max; i += nthr) s_single[i] = m.halo_single[e0 + i];
+  if (tid == 0) {
+    // every copy must stay inside the staged halo and the position buffers,
+    // and the copies must cover the halo exactly
+    int ok = 1, tot = nsingle;
+    for (int r = 0; r < nrun; ++r) {
+      const int4 run = m.halo_run[r0 + r];
+      ok &= run.z > 0 && run.y >= 0 && run.y + run.z <= m.hmax && run.x >= 0 && run.x + run.z <= m.nslots;
+      tot += run.z;
+    }
+    for (int i = 0; i < nsingle; ++i) {
+      const int2 e = m.halo_single[e0 + i];
+      ok &= e.y >= 0 && e.y < m.hmax && e.x >= 0 && e.x < m.nslots;
+    }
+    ok &= tot == hn0 && nrun <= m.df_nrun_max && nsingle <= m.df_nsingle_max;
+    if (!ok) atomicOr(a.err, kErrLayout);
+    *hflag = ok;
+    mbar_init(hbar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool halo_ok = *hflag != 0;  // no halo copies (and an error) for an inconsistent plan
+  const int hn = halo_ok ? hn0 : 0;
+  uint32_t long_bytes = 0;
+  if (halo_ok)
+    for (int r = 0; r < nrun; ++r) long_bytes += 32u * (uint32_t)s_runs[r].z;
+  uint32_t hphase = 0;
   // tile-resident tables
-  for (int i = tid; i < hn; i += nthr) hidx[i] = m.halo[h0 + i];
   for (int i = tid; i < nsp; i += nthr) {
     s_code[i] = __ldg(m.sp_code + S0 + i);
     s_rest[i] = __ldg(m.sp_rest2 + S0 + i);
@@ -239,12 +323,13 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
       off += nbnd;
     }
   }
-  dfloat x{0.f, 0.f}, y{0.f, 0.f}, z{0.f, 0.f}, vx{0.f, 0.f}, vy{0.f, 0.f}, vz{0.f, 0.f};
+  BeadCoord x{0, {0.f, 0.f}}, y{0, {0.f, 0.f}}, z{0, {0.f, 0.f}};
+  dfloat vx{0.f, 0.f}, vy{0.f, 0.f}, vz{0.f, 0.f};
   dfloat fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
   if (oprim) {
-    x = df_from_double(m.x[0][oslot]);
-    y = df_from_double(m.y[0][oslot]);
-    z = df_from_double(m.z[0][oslot]);
+    x = coord_from_double(m.x[0][oslot]);
+    y = coord_from_double(m.y[0][oslot]);
+    z = coord_from_double(m.z[0][oslot]);
     vx = df_from_double(m.vx[oslot]);
     vy = df_from_double(m.vy[oslot]);
     vz = df_from_double(m.vz[oslot]);
@@ -257,7 +342,8 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   // own beads into shared memory and the global pair buffer b
   auto publish = [&](int b) {
     if (oprim) {
-      const float4 p0 = make_float4(x.h, y.h, z.h, x.l), p1 = make_float4(y.l, z.l, 0.f, 0.f);
+      float4 p0, p1;
+      pack_coords(x, y, z, p0, p1);
       st[2 * tid] = p0;
       st[2 * tid + 1] = p1;
       m.q[b][2 * oslot] = p0;
@@ -266,12 +352,19 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   };
   // forces on the owned beads; buffer b holds the other tiles' beads
   auto evaluate = [&](int b) {
-    // other tiles' beads: asynchronous copies, waited for before the halo springs
-    const float4* src = m.q[b];
-    for (int i = tid; i < hn; i += nthr) {
-      const int g = hidx[i];
-      cp_async16(st + 2 * (T + i), src + 2 * g);
-      cp_async16(st + 2 * (T + i) + 1, src + 2 * g + 1);
+    // other tiles' beads: one bulk asynchronous copy (TMA) per run of
+    // consecutive slots, completing on the mbarrier; waited for before the
+    // halo springs
+    if (hn > 0) {
+      for (int r = tid; r < nrun; r += nthr) {
+        const int4 run = s_runs[r];
+        bulk_load(st + 2 * (T + run.y), m.q[b] + 2 * (size_t)run.x, 32u * (uint32_t)run.z, hbar);
+      }
+      for (int i = tid; i < nsingle; i += nthr) {
+        const int2 e = s_single[i];
+        cp_async16(st + 2 * (T + e.y), m.q[b] + 2 * (size_t)e.x);
+        cp_async16(st + 2 * (T + e.y) + 1, m.q[b] + 2 * (size_t)e.x + 1);
+      }
     }
     if (c1 > c0 && refresh_due(a, eval)) {
       // Cilia::length (src/cilia.cpp:79-121) for every refreshed bond, in pairs
@@ -309,14 +402,22 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     if (mv >= 0) {
       m0 = st[2 * me];
       m1 = st[2 * me + 1];
-      springs_df(tb, st, m0, m1, s0 + lane, sm, axh, axl, ayh, ayl, azh, azl);
+      springs_df<LANES>(tb, st, m0, m1, s0 + lane, sm, axh, axl, ayh, ayl, azh, azl);
     }
-    cp_async_wait_all();
-    __syncthreads();
-    if (mv >= 0) springs_df(tb, st, m0, m1, sm + lane, s1, axh, axl, ayh, ayl, azh, azl);
+    if (hn > 0) {
+      if (long_bytes) {
+        if (!mbar_wait(hbar, hphase & 1u, kHaloWait)) atomicOr(a.err, kErrBarrier);
+        ++hphase;
+      }
+      cp_async_wait_all();
+      __syncthreads();
+    }
+    if (mv >= 0) springs_df<LANES>(tb, st, m0, m1, sm + lane, s1, axh, axl, ayh, ayl, azh, azl);
+    // the halo region is refilled by the async proxy next substep
+    fence_proxy_async_smem();
     // fixed-order combination of the four lanes
 #pragma unroll
-    for (int o = 1; o < kDfLanes; o <<= 1) {
+    for (int o = 1; o < LANES; o <<= 1) {
       const float bxh = __shfl_xor_sync(0xffffffffu, axh, o), bxl = __shfl_xor_sync(0xffffffffu, axl, o);
       const float byh = __shfl_xor_sync(0xffffffffu, ayh, o), byl = __shfl_xor_sync(0xffffffffu, ayl, o);
       const float bzh = __shfl_xor_sync(0xffffffffu, azh, o), bzl = __shfl_xor_sync(0xffffffffu, azl, o);
@@ -373,7 +474,12 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
       fz = df_norm(pp[4], pp[5]);
     }
   };
-  auto barrier = [&]() { return grid_sync(m.bar, ++barriers * nblocks, a.err); };
+  // the grid barrier before every evaluation; the halo's mbarrier is armed
+  // with the next copies' bytes before any of them can be issued
+  auto barrier = [&]() {
+    if (tid == 0 && long_bytes) mbar_arrive_expect_tx(hbar, long_bytes);
+    return grid_sync(m.bar, ++barriers * nblocks, a.err);
+  };
 
   // md_loop_start: forces at t0, v += F dt/2, x += v dt
   publish(0);
@@ -384,9 +490,9 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     kick(vx, fx, dt2);
     kick(vy, fy, dt2);
     kick(vz, fz, dt2);
-    kick(x, vx, dt);
-    kick(y, vy, dt);
-    kick(z, vz, dt);
+    coord_kick(x, vx, dt);
+    coord_kick(y, vy, dt);
+    coord_kick(z, vz, dt);
   }
   publish(cur ^ 1);
   if (!barrier()) return;
@@ -398,9 +504,9 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
       kick(vx, fx, dt);
       kick(vy, fy, dt);
       kick(vz, fz, dt);
-      kick(x, vx, dt);
-      kick(y, vy, dt);
-      kick(z, vz, dt);
+      coord_kick(x, vx, dt);
+      coord_kick(y, vy, dt);
+      coord_kick(z, vz, dt);
     }
     publish(cur ^ 1);
     if (!barrier()) return;
@@ -414,7 +520,7 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     kick(vz, fz, dt2);
   }
   if (oprim) {
-    const double X = df_to_double(x), Y = df_to_double(y), Z = df_to_double(z);
+    const double X = coord_to_double(x), Y = coord_to_double(y), Z = coord_to_double(z);
     const double VX = df_to_double(vx), VY = df_to_double(vy), VZ = df_to_double(vz);
     m.x[0][oslot] = X;
     m.y[0][oslot] = Y;
@@ -443,14 +549,32 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   }
   // switch_logic for the cilia of this tile (the staged positions are the final ones)
   for (int c = c0 + tid; c < c1; c += nthr) cilium_switch(m, a, c, a.t_end, base, sv);
+  __syncthreads();
+  if (tid == 0) mbar_inval(hbar);
 }
 
-template <typename Bin>
+template <int LANES, typename Bin>
 __global__ void __launch_bounds__(512) k_md_df(MDState m, typename Bin::Cells c, MDStepArgs a) {
-  md_df_body(m, a, Bin{c, &a});
+  md_df_body<LANES>(m, a, Bin{c, &a});
 }
 
-size_t md_df_smem(const MDState& m) { return DfSmem(m.tile, m.hmax, m.df_nsp_max, m.df_nb_max).total; }
+}  // namespace
+
+// eight lanes per slot when the tile allows it (more warps in flight), else four
+int md_df_lanes(int tile) {
+  static const int forced = [] {
+    const char* env = std::getenv("MPCD_MD_DF_LANES");  // 4 or 8
+    return env ? std::atoi(env) : 0;
+  }();
+  if (forced == 4 || (forced == 8 && tile <= 64)) return forced;
+  return tile <= 64 ? 8 : 4;
+}
+
+namespace {
+
+size_t md_df_smem(const MDState& m) {
+  return DfSmem(m.tile, m.hmax, m.df_nsp_max, m.df_nb_max, m.df_nrun_max, m.df_nsingle_max).total;
+}
 
 template <typename Bin>
 int launch_df(const MDState& m, const typename Bin::Cells& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st) {
@@ -461,9 +585,10 @@ int launch_df(const MDState& m, const typename Bin::Cells& c, const MDStepArgs& 
   MDStepArgs aa = a;
   void* args[] = {&mm, &cc, &aa};
   const size_t smem = md_df_smem(m);
-  const void* k = (const void*)k_md_df<Bin>;
+  const int lanes = md_df_lanes(m.tile);
+  const void* k = lanes == 8 ? (const void*)k_md_df<8, Bin> : (const void*)k_md_df<4, Bin>;
   if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  *st = cudaLaunchCooperativeKernel(k, dim3(m.ntiles), dim3(kDfLanes * m.tile), args, smem, s);
+  *st = cudaLaunchCooperativeKernel(k, dim3(m.ntiles), dim3(lanes * m.tile), args, smem, s);
   return 1;
 }
 
@@ -484,9 +609,11 @@ int md_df_max_coresident_blocks(const MDState& m, int f32cells) {
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t smem = md_df_smem(m);
   if (smem > (size_t)optin) return 0;
-  const void* k = f32cells ? (const void*)k_md_df<BinF32> : (const void*)k_md_df<BinF64>;
+  const int lanes = md_df_lanes(m.tile);
+  const void* k = f32cells ? (lanes == 8 ? (const void*)k_md_df<8, BinF32> : (const void*)k_md_df<4, BinF32>)
+                           : (lanes == 8 ? (const void*)k_md_df<8, BinF64> : (const void*)k_md_df<4, BinF64>);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kDfLanes * m.tile, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, lanes * m.tile, smem);
   return per_sm * sms;
 }
 

@@ -385,6 +385,10 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
   // every spring's other bead as an index into the tile's staged positions
   out.sl.assign(nspk, 0);
   out.hstart.assign(out.ntiles + 1, 0);
+  out.df_runs.clear();
+  out.df_run_start.assign(1, 0);
+  out.df_single.clear();
+  out.df_single_start.assign(1, 0);
   int hmax = 0;
   for (int t = 0; t < out.ntiles; ++t) {
     const int b0 = t * tile, b1 = b0 + tile;
@@ -401,6 +405,25 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     }
     out.hstart[t + 1] = out.hstart[t] + (int)ext.size();
     out.halo.insert(out.halo.end(), ext.begin(), ext.end());
+    // double-float kernel: entries are copied one by one (cp.async); with
+    // MPCD_MD_LONG_RUN=n, runs of at least n consecutive slots go as one bulk
+    // copy (TMA) each instead -- measured slower on these halos (many short
+    // runs), so off by default
+    const char* lr_env = std::getenv("MPCD_MD_LONG_RUN");
+    const size_t kLongRun = lr_env ? (size_t)std::max(1, std::atoi(lr_env)) : (size_t)1 << 30;
+    for (size_t i = 0; i < ext.size();) {
+      size_t e = i + 1;
+      while (e < ext.size() && ext[e] == ext[e - 1] + 1) ++e;
+      if (e - i >= kLongRun)
+        out.df_runs.push_back({ext[i], (int)i, (int)(e - i), 0});
+      else
+        for (size_t k = i; k < e; ++k) out.df_single.push_back({ext[k], (int)k});
+      i = e;
+    }
+    out.df_run_start.push_back((int)out.df_runs.size());
+    out.df_single_start.push_back((int)out.df_single.size());
+    out.df_nrun_max = std::max(out.df_nrun_max, out.df_run_start[t + 1] - out.df_run_start[t]);
+    out.df_nsingle_max = std::max(out.df_nsingle_max, out.df_single_start[t + 1] - out.df_single_start[t]);
     hmax = std::max(hmax, (int)ext.size());
   }
   out.hmax = hmax;
@@ -473,6 +496,8 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
   probe.df = out.df;
   probe.df_nsp_max = out.df_nsp_max;
   probe.df_nb_max = out.df_nb_max;
+  probe.df_nrun_max = out.df_nrun_max;
+  probe.df_nsingle_max = out.df_nsingle_max;
   probe.cluster = out.cluster;
   probe.cl_lanes = out.cl_lanes;
   if (out.cluster) {

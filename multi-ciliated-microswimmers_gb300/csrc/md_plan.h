@@ -51,7 +51,11 @@ struct MDPlan {
   // double-float grid kernel (md_df.cu)
   std::vector<int> df_split, df_b0, df_nb;
   std::vector<uint32_t> df_code;
-  int df_nsp_max = 0, df_nb_max = 0;
+  std::vector<int4> df_runs;       // halo runs {first slot, staged rank, length, 0}
+  std::vector<int> df_run_start;  // ntiles + 1
+  std::vector<int2> df_single;     // other halo entries {slot, staged rank}
+  std::vector<int> df_single_start;
+  int df_nsp_max = 0, df_nb_max = 0, df_nrun_max = 0, df_nsingle_max = 0;
   long nsp_kept() const { return (long)so.size(); }
 };
 
