@@ -117,6 +117,13 @@ def workload_cfg(name, seed):
     return cfg
 
 
+MD_ARITH_NAMES = {
+    0: "float64",
+    1: "split (float springs on hi/lo position pairs)",
+    2: "double-float (pairs of floats, 48-bit significand; integer cell + offset coordinates)",
+}
+
+
 def describe(name, nf, nb, precision):
     if name == "swimmer64":
         geo = "64^3 cells x 10 fluid, Clami R=8 with 100 cilia (3x15 beads) on a Fibonacci lattice, 50 MD substeps"
@@ -129,13 +136,15 @@ def describe(name, nf, nb, precision):
 
 # ------------------------------------------------------------------ GPU arm --
 
-def run_gpu(args, rank=0):
+def run_gpu(args, rank=0, md_arith=None, steps=None):
     import cilia_gpu as cg
 
     prec = cg.MPCD_FP64 if args.precision == "fp64" else cg.MPCD_FP32
     cfg = workload_cfg(args.workload, seed=1000 + rank)
     text = simcfg.dumps(cfg)
-    sim = cg.Sim(text, precision=prec, seed=1000 + rank, device=args.device)
+    sim = cg.Sim(text, precision=prec, seed=1000 + rank, device=args.device,
+                 md_arith=cg.MD_AUTO if md_arith is None else md_arith)
+    steps = args.steps if steps is None else steps
     eng = sim.engine
     nf = len(eng.fluid()[1]) if args.verify_counts else int(cfg["sizex"]) ** 3 * 10
     nb = sim.nbeads
@@ -144,21 +153,23 @@ def run_gpu(args, rank=0):
     eng.sync()
     launches0 = eng.launch_count()
     with ClockSampler(args.device) as clk:
-        step_ms = eng.timed_run(args.steps, flush_l2=True)
+        step_ms = eng.timed_run(steps, flush_l2=True)
     launches = eng.launch_count() - launches0
     total_s = float(step_ms.sum()) / 1e3
-    value = ntot * args.steps / total_s
+    value = ntot * steps / total_s
     # per-kernel times on a short profiled run (events around every launch)
-    prof_steps = min(args.steps, 20)
+    prof_steps = min(steps, 20)
     eng.set_profiling(True)
     eng.timed_run(prof_steps, flush_l2=True)
     kt = {k: eng.kernel_time(i) for k, i in (("cell", cg.K_CELL), ("fluid", cg.K_FLUID), ("bead", cg.K_BEAD),
                                               ("md", cg.K_MD), ("sort", cg.K_SORT))}
     eng.set_profiling(False)
     obs = eng.observables()
+    md_arith = eng.md_layout()["arith"] if nb else None
     sim.close()
-    return dict(value=value, ms_per_step=1e3 * total_s / args.steps, nf=nf, nb=nb, kernels=kt,
-                launches=launches, clocks=clk.summary(), kT=obs["kT"], step_ms=step_ms, prof_steps=prof_steps)
+    return dict(value=value, ms_per_step=1e3 * total_s / steps, nf=nf, nb=nb, kernels=kt,
+                launches=launches, clocks=clk.summary(), kT=obs["kT"], step_ms=step_ms, prof_steps=prof_steps,
+                md_arith=md_arith)
 
 
 def run_e2e(args):
@@ -469,6 +480,16 @@ def main():
         "clocks": g["clocks"],
         "kT": g["kT"],
     }
+    if g["md_arith"] is not None:
+        line["config"]["md_arith"] = MD_ARITH_NAMES[g["md_arith"]]
+    if args.precision == "fp64" and g["nb"] and not args.no_extra:
+        # the same workload with the MD substeps in IEEE float64 arithmetic
+        import cilia_gpu as cg
+
+        f = run_gpu(args, rank, md_arith=cg.MD_F64, steps=min(args.steps, 30))
+        line["plain_md_float64"] = {"value": f["value"], "unit": UNIT, "ms_per_step": f["ms_per_step"],
+                                    "md_ms_per_step": f["kernels"]["md"][0] / max(f["prof_steps"], 1),
+                                    "steps": min(args.steps, 30), "md_arith": MD_ARITH_NAMES[0]}
     if not args.no_extra:
         e = run_e2e(args)
         line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],

@@ -289,8 +289,9 @@ int build_md(mpcd_engine* h) {
   in.nbond = (long)h->newlen.size();
   in.newlen = h->newlen.data();
   in.oldlen = h->oldlen.data();
-  // -1: split springs with float32 cells, double-float with float64 cells
-  const int arith = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 1 : 2) : h->p.md_split;
+  // -1: double-float (the grid kernel of md_df.cu, faster on GB300 than the
+  // float64 kernel and than the split-arithmetic cluster kernel for one box)
+  const int arith = h->p.md_split < 0 ? 2 : h->p.md_split;
   if (arith > 2) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1 or 2");
   in.split = arith == 1;
   in.df = arith == 2;

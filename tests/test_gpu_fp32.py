@@ -1,6 +1,6 @@
 """Split-precision path (int cell + float32 offset, float32 velocities and
-cell sums, split-precision MD springs) against the float64 path and the
-reference fixtures.  Stated errors: positions 2e-4 and velocities 2e-4
+cell sums; MD in double-float by default, or split-precision springs) against
+the float64 path and the reference fixtures.  Stated errors: positions 2e-4 and velocities 2e-4
 absolute after 4 MPC steps of identical injected randomness; kT within 1 %
 and total momentum per particle below 1e-5 over free-running steps."""
 import numpy as np
@@ -35,11 +35,15 @@ def test_fp32_fluid_tracks_reference_golden():
     assert np.mean(dv < 2e-4) > 0.995
 
 
-def test_fp32_swimmer_tracks_reference_golden():
+@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_SPLIT])
+def test_fp32_swimmer_tracks_reference_golden(arith):
+    """MD in double-float (the default) and in split arithmetic on one
+    thread-block cluster (the replica batch's MD)."""
     g = golden("clami10")
     text = open(f"{GOLDEN}/cases/clami10.cfg").read()
-    s = cg.Sim(text, precision=cg.MPCD_FP32, ststep=0.002, create_fluid=False)
+    s = cg.Sim(text, precision=cg.MPCD_FP32, ststep=0.002, create_fluid=False, md_arith=arith)
     e = s.engine
+    assert e.md_layout()["arith"] == (cg.MD_DF if arith == cg.MD_AUTO else arith)
     e.set_fluid(g["step0_fluid_pos"], g["step0_fluid_vel"])
     e.shift = g["shift_0"]
     for k in range(1, 5):
