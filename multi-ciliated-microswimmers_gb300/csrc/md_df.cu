@@ -22,9 +22,9 @@
 // halo arrives by bulk asynchronous copies (TMA, one per run of consecutive
 // slots, completing on an mbarrier) while the lanes work on the springs
 // between beads of their own tile, and is waited for (bounded) before the
-// springs that reach it.  A bead with helper
-// slots sums their partial forces in blocks (the block leaders in parallel,
-// then the primary over the block sums), always in slot order.
+// springs that reach it.  The partial forces of a bead's helper slots are
+// added in a fixed order: by one warp (lane-strided, then a xor tree) for
+// long runs, by the primary in slot order for short ones.
 //
 // The cilia's rest lengths: the beat's target length of every bond is fixed
 // during one MPC step's substeps (the midpoint moves after them), so it is
@@ -41,7 +41,6 @@ namespace mpcd {
 
 namespace {
 
-constexpr int kHelpBlock = 8;            // helper partial sums added in blocks of this many slots
 constexpr uint32_t kHaloWait = 1u << 22;  // polls of the halo's mbarrier before giving up
 
 // 16-byte asynchronous global -> shared copy through L2 (cp.async.cg)
@@ -176,7 +175,7 @@ __device__ __forceinline__ void kick(dfloat& v, dfloat f, dfloat c) { v = df_add
 
 // shared-memory layout of one tile
 struct DfSmem {
-  size_t st, bar, flag, runs, single, code, rest, m2k, nl, ol, dg, tg, bd, part, bsum, total;
+  size_t st, bar, flag, runs, single, code, rest, m2k, nl, ol, dg, tg, bd, part, total;
   __host__ __device__ DfSmem(int T, int hmax, int nsp, int nb, int nrun, int nsingle) {
     size_t o = 0;
     auto take = [&](size_t bytes, size_t align) {
@@ -199,7 +198,6 @@ struct DfSmem {
     bd = take(8 * (size_t)nb, 8);
     code = take(4 * (size_t)nsp, 4);
     part = take(24 * (size_t)T, 4);
-    bsum = take(24 * (size_t)T, 4);
     total = o;
   }
 };
@@ -219,7 +217,6 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   float2* s_tg = reinterpret_cast<float2*>(smem + L.tg);
   float2* s_bd = reinterpret_cast<float2*>(smem + L.bd);
   float* part = reinterpret_cast<float*>(smem + L.part);  // per slot: its lanes' force (6 floats)
-  float* bsum = reinterpret_cast<float*>(smem + L.bsum);  // per helper block leader: block sum
   uint64_t* hbar = reinterpret_cast<uint64_t*>(smem + L.bar);  // halo copies' completion
   int* hflag = reinterpret_cast<int*>(smem + L.flag);           // 1: the halo runs are valid
   int4* s_runs = reinterpret_cast<int4*>(smem + L.runs);         // this tile's long halo runs
@@ -243,17 +240,11 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   const int omv = tid < T ? m.moves[oslot] : -1;
   const bool oprim = omv == 0 || omv == 1, omoves = omv == 1;
   const bool helpers = m.tile_help[tile] != 0;
-  // helper blocks: a primary and its helpers form a run of 1 + nh slots; the
-  // slots at offsets 0, kHelpBlock, 2 kHelpBlock ... of the run sum the parts
-  // of their block, and the primary sums the block sums, all in slot order
-  int blk_n = 0, run_blocks = 0;
-  if (helpers && tid < T && omv >= 0) {
-    const int p = m.prim[oslot] - base;
-    const int j = tid - p;
-    const int nh = m.nhelp[base + p];
-    if (j % kHelpBlock == 0) blk_n = min(kHelpBlock, nh + 1 - j);
-    if (j == 0) run_blocks = (nh + kHelpBlock) / kHelpBlock;
-  }
+  // a primary with helpers and its helper slots form a run of 1 + nh slots;
+  // runs longer than kTreeRun are summed by a warp, shorter ones by the primary
+  constexpr int kTreeRun = 8;
+  const int onh = oprim ? m.nhelp[oslot] : 0;
+  const int owarps = (T + 31) / 32;  // warps holding the owner threads
   const int h0 = m.halo_start[tile], hn0 = m.halo_start[tile + 1] - h0;
   const int c0 = m.tile_cil[tile], c1 = m.tile_cil[tile + 1];
   const int b0 = m.tile_b0[tile], nb = m.tile_nb[tile];
@@ -435,39 +426,53 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
       pp[5] = azl;
     }
     __syncthreads();
-    if (helpers) {
-      if (blk_n > 0) {
-        const float* pp = part + 6 * tid;
-        float gxh = pp[0], gxl = pp[1], gyh = pp[2], gyl = pp[3], gzh = pp[4], gzl = pp[5];
-        for (int k = 1; k < blk_n; ++k) {
-          const float* ph = pp + 6 * k;
+    if (helpers && tid < 32 * owarps) {
+      // long runs: the warp holding the primary's owner thread adds the run's
+      // slot sums, lane-strided and then by a xor tree -- a fixed order
+      const int lane32 = tid & 31;
+      unsigned runs = __ballot_sync(0xffffffffu, onh + 1 > kTreeRun);
+      while (runs) {
+        const int src = __ffs(runs) - 1;
+        runs &= runs - 1;
+        const int p = (tid & ~31) + src;
+        const int len = 1 + __shfl_sync(0xffffffffu, onh, src);
+        float gxh = 0.f, gxl = 0.f, gyh = 0.f, gyl = 0.f, gzh = 0.f, gzl = 0.f;
+        for (int k = lane32; k < len; k += 32) {
+          const float* ph = part + 6 * (p + k);
           df_acc(gxh, gxl, ph[0], ph[1]);
           df_acc(gyh, gyl, ph[2], ph[3]);
           df_acc(gzh, gzl, ph[4], ph[5]);
         }
-        float* bs = bsum + 6 * tid;
-        bs[0] = gxh;
-        bs[1] = gxl;
-        bs[2] = gyh;
-        bs[3] = gyl;
-        bs[4] = gzh;
-        bs[5] = gzl;
-      }
-      __syncthreads();
-      if (oprim) {
-        const float* pp = bsum + 6 * tid;
-        float gxh = pp[0], gxl = pp[1], gyh = pp[2], gyl = pp[3], gzh = pp[4], gzl = pp[5];
-        for (int k = 1; k < run_blocks; ++k) {
-          const float* ph = pp + 6 * kHelpBlock * k;
-          df_acc(gxh, gxl, ph[0], ph[1]);
-          df_acc(gyh, gyl, ph[2], ph[3]);
-          df_acc(gzh, gzl, ph[4], ph[5]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float bxh = __shfl_xor_sync(0xffffffffu, gxh, o), bxl = __shfl_xor_sync(0xffffffffu, gxl, o);
+          const float byh = __shfl_xor_sync(0xffffffffu, gyh, o), byl = __shfl_xor_sync(0xffffffffu, gyl, o);
+          const float bzh = __shfl_xor_sync(0xffffffffu, gzh, o), bzl = __shfl_xor_sync(0xffffffffu, gzl, o);
+          df_acc(gxh, gxl, bxh, bxl);
+          df_acc(gyh, gyl, byh, byl);
+          df_acc(gzh, gzl, bzh, bzl);
         }
-        fx = df_norm(gxh, gxl);
-        fy = df_norm(gyh, gyl);
-        fz = df_norm(gzh, gzl);
+        if (lane32 == src) {
+          fx = df_norm(gxh, gxl);
+          fy = df_norm(gyh, gyl);
+          fz = df_norm(gzh, gzl);
+        }
       }
-    } else if (oprim) {
+    }
+    if (oprim && onh > 0 && onh + 1 <= kTreeRun) {  // short runs, in slot order
+      const float* pp = part + 6 * tid;
+      float gxh = pp[0], gxl = pp[1], gyh = pp[2], gyl = pp[3], gzh = pp[4], gzl = pp[5];
+      for (int k = 1; k <= onh; ++k) {
+        const float* ph = pp + 6 * k;
+        df_acc(gxh, gxl, ph[0], ph[1]);
+        df_acc(gyh, gyl, ph[2], ph[3]);
+        df_acc(gzh, gzl, ph[4], ph[5]);
+      }
+      fx = df_norm(gxh, gxl);
+      fy = df_norm(gyh, gyl);
+      fz = df_norm(gzh, gzl);
+    }
+    if (oprim && onh == 0) {
       const float* pp = part + 6 * tid;
       fx = df_norm(pp[0], pp[1]);
       fy = df_norm(pp[2], pp[3]);
