@@ -217,7 +217,7 @@ int mpcd_md_layout(mpcd_engine* h, int* info);
  * for the default stream); the call returns after the stream has finished.
  *
  * Its per-cell scratch is a file-scope static device array for at most
- * MPCD_NOALLOC_MAX_CELLS cells (about 4.5 MB), held by every GPU that loads the
+ * MPCD_NOALLOC_MAX_CELLS cells (about 3.4 MB), held by every GPU that loads the
  * library until the process exits.  Larger boxes are rejected with
  * MPCD_EINVAL.  The first call on a device looks the array's address up
  * (cudaGetSymbolAddress) with that device current; make that first call

@@ -697,7 +697,7 @@ int mpcd_batch_create(const mpcd_batch_params* params, mpcd_batch** out) {
   }
   if ((e = dalloc(&b->cells.sum, b->cell_cap)) != cudaSuccess) return bail(e, "alloc cells");
   if ((e = dalloc(&b->cells.cnt, b->cell_cap)) != cudaSuccess) return bail(e, "alloc cells");
-  if ((e = dalloc(&b->cells.par, 3 * b->cell_cap)) != cudaSuccess) return bail(e, "alloc cells");
+  if ((e = dalloc(&b->cells.par, 2 * b->cell_cap)) != cudaSuccess) return bail(e, "alloc cells");
   if ((e = dalloc(&b->d_count, b->cell_cap)) != cudaSuccess) return bail(e, "alloc sort");
   if ((e = dalloc(&b->d_start, b->cell_cap)) != cudaSuccess) return bail(e, "alloc sort");
   if ((e = dalloc(&b->d_rank, b->part_cap)) != cudaSuccess) return bail(e, "alloc sort");

@@ -121,7 +121,7 @@ __global__ void k_batch_cell_params(BatchTables t, BatchCells c) {
         const long cid = cb + u * stride;
         c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
         c.cnt[cid] = 0u;
-        cell_map_f32(sm[u], w[u], (uint32_t)(cid - cell0), seed, step, mb, nullptr, nullptr, c.par + 3 * cid, ldiss,
+        cell_map_f32(sm[u], w[u], (uint32_t)(cid - cell0), seed, step, mb, nullptr, nullptr, c.par + 2 * cid, ldiss,
                      errbits, gfail);
       }
     }
@@ -155,7 +155,7 @@ __device__ __forceinline__ FluidPage fluid_page(const BatchTables& t, const Batc
   P.gk = S.fgkick;
   P.sum = c.sum + R.cell0;
   P.cnt = c.cnt + R.cell0;
-  P.par = c.par + 3 * R.cell0;
+  P.par = c.par + 2 * R.cell0;
   return P;
 }
 
@@ -171,7 +171,7 @@ __device__ __forceinline__ void fluid_particle(const FluidPage& P, const float4 
   float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
   const long cid = shifted_f(ix, ox, P.tc[0], Lx) +
                    (long)Lx * (shifted_f(iy, oy, P.tc[1], Ly) + (long)Ly * shifted_f(iz, oz, P.tc[2], Lz));
-  apply_map_f32(P.par + 3 * cid, vx, vy, vz);
+  apply_map_f32(P.par + 2 * cid, vx, vy, vz);
   ke_after += vx * vx + vy * vy + vz * vz;
   ox = fmaf(vx, P.h, ox);
   oy = fmaf(vy, P.h, oy);

@@ -617,7 +617,7 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
     h->c32.ncell = nc;
     if ((e = dalloc(&h->c32.sum, nc)) != cudaSuccess) return bail(e, "alloc cells");
     if ((e = dalloc(&h->c32.cnt, nc)) != cudaSuccess) return bail(e, "alloc cells");
-    if ((e = dalloc(&h->c32.par, 3 * nc)) != cudaSuccess) return bail(e, "alloc cells");
+    if ((e = dalloc(&h->c32.par, 2 * nc)) != cudaSuccess) return bail(e, "alloc cells");
     cudaMemset(h->c32.sum, 0, nc * sizeof(float4));
     cudaMemset(h->c32.cnt, 0, nc * sizeof(uint32_t));
   }

@@ -41,7 +41,7 @@ struct CellsF32 {
   long ncell = 0;
   float4* sum = nullptr;
   uint32_t* cnt = nullptr;
-  float4* par = nullptr;  // 3 float4 per cell: (A row 0, b0), (A row 1, b1), (A row 2, b2)
+  float4* par = nullptr;  // 2 float4 per cell: (axis, thermostat factor), (mean velocity, 0)
 };
 
 // Per-step scalars for the fluid kernels.

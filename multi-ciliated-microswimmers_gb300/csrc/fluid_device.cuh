@@ -133,27 +133,25 @@ __device__ __forceinline__ void cell_map_f32(const float4 s0, const uint32_t w, 
     ry = st * sp;
     rz = ct;
   }
-  const float A00 = sc * (rx * rx + (1.0f - rx * rx) * ca), A01 = sc * (rx * ry * oc - rz * sa),
-              A02 = sc * (rx * rz * oc + ry * sa);
-  const float A10 = sc * (rx * ry * oc + rz * sa), A11 = sc * (ry * ry + (1.0f - ry * ry) * ca),
-              A12 = sc * (ry * rz * oc - rx * sa);
-  const float A20 = sc * (rx * rz * oc - ry * sa), A21 = sc * (ry * rz * oc + rx * sa),
-              A22 = sc * (rz * rz + (1.0f - rz * rz) * ca);
+  // v' = u + sc R (v - u), R the rotation about (rx, ry, rz) with the
+  // reference's matrix entries (src/libcilia/mpcd.cpp:285-293), applied as
+  // R w = ca w + sa (r x w) + (1 - ca) (r . w) r: one 32-byte map per cell
   float4* p = par_out;
-  p[0] = make_float4(A00, A01, A02, ux - (A00 * ux + A01 * uy + A02 * uz));
-  p[1] = make_float4(A10, A11, A12, uy - (A10 * ux + A11 * uy + A12 * uz));
-  p[2] = make_float4(A20, A21, A22, uz - (A20 * ux + A21 * uy + A22 * uz));
+  p[0] = make_float4(rx, ry, rz, sc);
+  p[1] = make_float4(ux, uy, uz, 0.0f);
   ldiss += s.w;
 }
 
+// v' = u + sc R (v - u) with the map {rx, ry, rz, sc}, {ux, uy, uz, 0}
 __device__ __forceinline__ void apply_map_f32(const float4* par, float& vx, float& vy, float& vz) {
-  const float4 r0 = __ldg(par + 0), r1 = __ldg(par + 1), r2 = __ldg(par + 2);
-  const float nx = fmaf(r0.x, vx, fmaf(r0.y, vy, fmaf(r0.z, vz, r0.w)));
-  const float ny = fmaf(r1.x, vx, fmaf(r1.y, vy, fmaf(r1.z, vz, r1.w)));
-  const float nz = fmaf(r2.x, vx, fmaf(r2.y, vy, fmaf(r2.z, vz, r2.w)));
-  vx = nx;
-  vy = ny;
-  vz = nz;
+  const float ca = (float)kCosAlpha, sa = (float)kSinAlpha, oc = 1.0f - (float)kCosAlpha;
+  const float4 k = __ldg(par + 0), u = __ldg(par + 1);
+  const float wx = vx - u.x, wy = vy - u.y, wz = vz - u.z;
+  const float kw = oc * (k.x * wx + k.y * wy + k.z * wz);
+  const float cx = k.y * wz - k.z * wy, cy = k.z * wx - k.x * wz, cz = k.x * wy - k.y * wx;
+  vx = fmaf(k.w, fmaf(ca, wx, fmaf(sa, cx, kw * k.x)), u.x);
+  vy = fmaf(k.w, fmaf(ca, wy, fmaf(sa, cy, kw * k.y)), u.y);
+  vz = fmaf(k.w, fmaf(ca, wz, fmaf(sa, cz, kw * k.z)), u.z);
 }
 
 }  // namespace mpcd

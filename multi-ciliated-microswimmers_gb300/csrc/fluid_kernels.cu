@@ -547,7 +547,7 @@ __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
       const long cid = cb + u * stride;
       c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
       c.cnt[cid] = 0u;
-      cell_map_f32(sm[u], w[u], (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 3 * cid,
+      cell_map_f32(sm[u], w[u], (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 2 * cid,
                    ldiss, errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt);
     }
   }
@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF3
     int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
     float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
     const long cid = shifted_f(ix, ox, tcx, Lx) + (long)Lx * (shifted_f(iy, oy, tcy, Ly) + (long)Ly * shifted_f(iz, oz, tcz, Lz));
-    apply_map_f32(c.par + 3 * cid, vx, vy, vz);
+    apply_map_f32(c.par + 2 * cid, vx, vy, vz);
     ke_after += vx * vx + vy * vy + vz * vz;
     if (a.walls == 0) {
       ox = fmaf(vx, h, ox);
@@ -635,7 +635,7 @@ __global__ void k_bead_collide_f32(MDState m, CellsF32 c, StepArgs a) {
       continue;
     }
     float vx = (float)m.vx[s], vy = (float)m.vy[s], vz = (float)m.vz[s];
-    apply_map_f32(c.par + 3 * cid, vx, vy, vz);
+    apply_map_f32(c.par + 2 * cid, vx, vy, vz);
     ke_after += a.bead_mass * ((double)vx * vx + (double)vy * vy + (double)vz * vz);
     m.vx[s] = vx;
     m.vy[s] = vy;

@@ -521,7 +521,7 @@ struct BatchBin {
       atomicOr(d->err, kErrCellRange);
       return 0.0;
     }
-    apply_map_f32(d->par + 3 * (d->cell0 + cid), v[0], v[1], v[2]);
+    apply_map_f32(d->par + 2 * (d->cell0 + cid), v[0], v[1], v[2]);
     return d->mbd * ((double)v[0] * v[0] + (double)v[1] * v[1] + (double)v[2] * v[2]);
   }
   __device__ void add_diss(double x) const { atomicAdd(d->diss, x); }

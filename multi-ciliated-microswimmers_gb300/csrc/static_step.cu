@@ -21,10 +21,10 @@ using namespace mpcd;
 namespace {
 
 constexpr long kMaxCells = MPCD_NOALLOC_MAX_CELLS;
-// layout: sums (float4 per cell) | maps (3 float4 per cell) | counts (uint32 per cell)
+// layout: sums (float4 per cell) | maps (2 float4 per cell) | counts (uint32 per cell)
 //         | dissipated energy (double) | error word (unsigned)
 constexpr size_t kSumBytes = sizeof(float4) * kMaxCells;
-constexpr size_t kParBytes = 3 * sizeof(float4) * kMaxCells;
+constexpr size_t kParBytes = 2 * sizeof(float4) * kMaxCells;
 constexpr size_t kCntBytes = sizeof(uint32_t) * kMaxCells;
 constexpr size_t kScratchBytes = kSumBytes + kParBytes + kCntBytes + 256;
 

@@ -60,8 +60,9 @@ def test_walls_fp32_tracks_reference_golden():
     p, v = out[5]
     dp = np.abs(periodic_diff(p, g["step5_fluid_pos"], L)).max(axis=1)
     dv = np.abs(v - g["step5_fluid_vel"]).max(axis=1)
-    assert np.mean(dp < 2e-4) > 0.995
-    assert np.mean(dv < 2e-4) > 0.995
+    fp, fv = np.mean(dp < 2e-4), np.mean(dv < 2e-4)
+    print("walls fp32 within 2e-4:", fp, fv, dp.max(), dv.max())
+    assert fp > 0.995 and fv > 0.995, (fp, fv, dp.max(), dv.max())
 
 
 @pytest.mark.parametrize("precision", [cg.MPCD_FP64, cg.MPCD_FP32])
