@@ -71,7 +71,8 @@ typedef struct {
   int md_split;          /* MD arithmetic: -1 auto (2),
                             0 float64, 1 split (float springs on hi/lo position pairs; state
                             stays float64), 2 double-float (pairs of floats, about 48
-                            significand bits, for forces and substeps; float64 between steps) */
+                            significand bits, for forces and substeps; float64 between steps),
+                            3 float springs (split arithmetic) on the layout of 2 */
 } mpcd_params;
 
 /* Values that replace the generator for one step (all host arrays).  Used to
@@ -193,7 +194,8 @@ int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* la
 /* Layout the MD kernels run on (built first if the bead set changed).
  * info[8] receives: cluster (1: one thread-block cluster, 0: cooperative
  * grid), threads per slot, slots per tile, tiles (CTAs), slots, springs,
- * largest halo of a tile, arithmetic (0 float64, 1 split, 2 double-float). */
+ * largest halo of a tile, arithmetic (0 float64, 1 split, 2 double-float,
+ * 3 float springs on the double-float layout). */
 int mpcd_md_layout(mpcd_engine* h, int* info);
 
 /* ----------------------------------------------------------------------------

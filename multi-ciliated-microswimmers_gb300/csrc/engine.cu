@@ -292,9 +292,9 @@ int build_md(mpcd_engine* h) {
   // -1: double-float (the grid kernel of md_df.cu, faster on GB300 than the
   // float64 kernel and than the split-arithmetic cluster kernel for one box)
   const int arith = h->p.md_split < 0 ? 2 : h->p.md_split;
-  if (arith > 2) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1 or 2");
+  if (arith > 3) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1, 2 or 3");
   in.split = arith == 1;
-  in.df = arith == 2;
+  in.df = arith == 2 || arith == 3;
   MDPlan pl;
   // MPCD_MD_NO_CLUSTER=1 keeps split arithmetic on the cooperative grid layout
   const char* no_cl = std::getenv("MPCD_MD_NO_CLUSTER");
@@ -304,7 +304,7 @@ int build_md(mpcd_engine* h) {
   if (pl.hstart.size() != (size_t)pl.ntiles + 1 || pl.halo.size() != (size_t)pl.hstart.back())
     return fail(h, MPCD_EINVAL, "MD plan: halo lists inconsistent with their offsets");
   m.split = pl.split;
-  m.df = pl.df;
+  m.df = pl.df ? (arith == 3 ? 2 : 1) : 0;
   m.cluster = pl.cluster;
   m.cl_lanes = pl.cl_lanes;
   m.cl_nsp_max = pl.cl_nsp_max;
@@ -1148,7 +1148,7 @@ int mpcd_md_layout(mpcd_engine* h, int* info) {
   info[4] = m.nslots;
   info[5] = (int)h->md_nsp;
   info[6] = m.hmax;
-  info[7] = m.df ? 2 : m.split;
+  info[7] = m.df ? m.df + 1 : m.split;
   return MPCD_OK;
 }
 

@@ -124,7 +124,7 @@ struct MDState {
   // within the tile << 18), per slot the end of its in-tile springs, per tile
   // its bond range, and two position buffers of pairs, two float4 per slot
   // ({hx, hy, hz, lx}, {ly, lz, 0, 0})
-  int df = 0;
+  int df = 0;          // 1: double-float springs, 2: float springs (split arithmetic) on this layout
   int df_nsp_max = 0;  // most springs of one tile
   int df_nb_max = 0;   // most bonds of one tile
   int df_nrun_max = 0;     // most long halo runs of one tile

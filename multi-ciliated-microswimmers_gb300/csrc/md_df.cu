@@ -141,8 +141,10 @@ struct Tables {
 // Force on staged bead `me` from springs [a, b) step LANES (indices local
 // to the tile's table).  Per spring, with d = x_me - x_o and rest length b:
 // fac = -2k (1 - b / |d|), F += fac d, all in pairs; components accumulate as
-// compensated sums (h, l).
-template <int LANES>
+// compensated sums (h, l).  kFloat: the difference d is formed exactly as a
+// pair and rounded to float, the rest of the spring in float (the split
+// arithmetic of the float32 path); the sums stay compensated.
+template <int LANES, bool kFloat>
 __device__ __forceinline__ void springs_df(const Tables& tb, const float4* st, const float4 m0, const float4 m1, int a,
                                            int b, float& fxh, float& fxl, float& fyh, float& fyl, float& fzh,
                                            float& fzl) {
@@ -153,6 +155,20 @@ __device__ __forceinline__ void springs_df(const Tables& tb, const float4* st, c
     const int lref = (int)(code >> 18);
     const float2 b2 = kind <= MPCD_SPRING_GUARDED ? tb.rest[s] : (kind == MPCD_SPRING_BOND ? tb.nl[lref] : tb.dg[lref]);
     const float2 k2 = tb.m2k[s];
+    if constexpr (kFloat) {
+      const float4 o0 = st[2 * o], o1 = st[2 * o + 1];
+      const dfloat ex = coord_diff((float)(cell_x(m1) - cell_x(o1)), m0.x, o0.x, m0.w, o0.w);
+      const dfloat ey = coord_diff((float)(cell_y(m1) - cell_y(o1)), m0.y, o0.y, m1.x, o1.x);
+      const dfloat ez = coord_diff(__fsub_rn(m1.w, o1.w), m0.z, o0.z, m1.y, o1.y);
+      const float dx = ex.h + ex.l, dy = ey.h + ey.l, dz = ez.h + ez.l;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (kind == MPCD_SPRING_GUARDED && d2 == 0.0f) continue;
+      const float fac = k2.x * (1.0f - b2.x * rsqrtf(d2));
+      fxh += fac * dx;
+      fyh += fac * dy;
+      fzh += fac * dz;
+      continue;
+    }
     const DfDiff d = df_diff(m0, m1, st[2 * o], st[2 * o + 1]);
     if (kind == MPCD_SPRING_GUARDED && d.d2.h == 0.0f) continue;  // vector-form spring: no force at zero distance
     const dfloat r = df_rsqrt(d.d2);
@@ -202,7 +218,7 @@ struct DfSmem {
   }
 };
 
-template <int LANES, typename Bin>
+template <int LANES, bool kFloat, typename Bin>
 __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int T = m.tile;
@@ -393,7 +409,7 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     if (mv >= 0) {
       m0 = st[2 * me];
       m1 = st[2 * me + 1];
-      springs_df<LANES>(tb, st, m0, m1, s0 + lane, sm, axh, axl, ayh, ayl, azh, azl);
+      springs_df<LANES, kFloat>(tb, st, m0, m1, s0 + lane, sm, axh, axl, ayh, ayl, azh, azl);
     }
     if (hn > 0) {
       if (long_bytes) {
@@ -403,7 +419,7 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
       cp_async_wait_all();
       __syncthreads();
     }
-    if (mv >= 0) springs_df<LANES>(tb, st, m0, m1, sm + lane, s1, axh, axl, ayh, ayl, azh, azl);
+    if (mv >= 0) springs_df<LANES, kFloat>(tb, st, m0, m1, sm + lane, s1, axh, axl, ayh, ayl, azh, azl);
     // the halo region is refilled by the async proxy next substep
     fence_proxy_async_smem();
     // fixed-order combination of the four lanes
@@ -558,9 +574,17 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   if (tid == 0) mbar_inval(hbar);
 }
 
-template <int LANES, typename Bin>
+template <int LANES, bool kFloat, typename Bin>
 __global__ void __launch_bounds__(512) k_md_df(MDState m, typename Bin::Cells c, MDStepArgs a) {
-  md_df_body<LANES>(m, a, Bin{c, &a});
+  md_df_body<LANES, kFloat>(m, a, Bin{c, &a});
+}
+
+// the kernel for a layout: lanes per slot, double-float (m.df == 1) or float springs (2)
+template <typename Bin>
+const void* df_kernel(const MDState& m, int lanes) {
+  const bool fl = m.df == 2;
+  if (lanes == 8) return fl ? (const void*)k_md_df<8, true, Bin> : (const void*)k_md_df<8, false, Bin>;
+  return fl ? (const void*)k_md_df<4, true, Bin> : (const void*)k_md_df<4, false, Bin>;
 }
 
 }  // namespace
@@ -591,7 +615,7 @@ int launch_df(const MDState& m, const typename Bin::Cells& c, const MDStepArgs& 
   void* args[] = {&mm, &cc, &aa};
   const size_t smem = md_df_smem(m);
   const int lanes = md_df_lanes(m.tile);
-  const void* k = lanes == 8 ? (const void*)k_md_df<8, Bin> : (const void*)k_md_df<4, Bin>;
+  const void* k = df_kernel<Bin>(m, lanes);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   *st = cudaLaunchCooperativeKernel(k, dim3(m.ntiles), dim3(lanes * m.tile), args, smem, s);
   return 1;
@@ -615,8 +639,7 @@ int md_df_max_coresident_blocks(const MDState& m, int f32cells) {
   const size_t smem = md_df_smem(m);
   if (smem > (size_t)optin) return 0;
   const int lanes = md_df_lanes(m.tile);
-  const void* k = f32cells ? (lanes == 8 ? (const void*)k_md_df<8, BinF32> : (const void*)k_md_df<4, BinF32>)
-                           : (lanes == 8 ? (const void*)k_md_df<8, BinF64> : (const void*)k_md_df<4, BinF64>);
+  const void* k = f32cells ? df_kernel<BinF32>(m, lanes) : df_kernel<BinF64>(m, lanes);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, lanes * m.tile, smem);
   return per_sm * sms;

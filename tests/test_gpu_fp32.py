@@ -35,10 +35,11 @@ def test_fp32_fluid_tracks_reference_golden():
     assert np.mean(dv < 2e-4) > 0.995
 
 
-@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_SPLIT])
+@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_SPLIT, cg.MD_FLOAT])
 def test_fp32_swimmer_tracks_reference_golden(arith):
-    """MD in double-float (the default) and in split arithmetic on one
-    thread-block cluster (the replica batch's MD)."""
+    """MD in double-float (the default), in split arithmetic on one
+    thread-block cluster (the replica batch's MD), and in split arithmetic on
+    the double-float kernel's grid layout."""
     g = golden("clami10")
     text = open(f"{GOLDEN}/cases/clami10.cfg").read()
     s = cg.Sim(text, precision=cg.MPCD_FP32, ststep=0.002, create_fluid=False, md_arith=arith)
