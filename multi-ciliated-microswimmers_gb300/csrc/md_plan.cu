@@ -405,12 +405,12 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     }
     out.hstart[t + 1] = out.hstart[t] + (int)ext.size();
     out.halo.insert(out.halo.end(), ext.begin(), ext.end());
-    // double-float kernel: entries are copied one by one (cp.async); with
-    // MPCD_MD_LONG_RUN=n, runs of at least n consecutive slots go as one bulk
-    // copy (TMA) each instead -- measured slower on these halos (many short
-    // runs), so off by default
+    // double-float kernel: runs of at least kLongRun consecutive slots (the
+    // sphere centre's tile reaches the whole sphere in a few such runs) go as
+    // one bulk copy (TMA) each, the other entries one by one (cp.async); short
+    // runs by bulk copy measured slower.  MPCD_MD_LONG_RUN=n overrides.
     const char* lr_env = std::getenv("MPCD_MD_LONG_RUN");
-    const size_t kLongRun = lr_env ? (size_t)std::max(1, std::atoi(lr_env)) : (size_t)1 << 30;
+    const size_t kLongRun = lr_env ? (size_t)std::max(1, std::atoi(lr_env)) : (size_t)32;
     for (size_t i = 0; i < ext.size();) {
       size_t e = i + 1;
       while (e < ext.size() && ext[e] == ext[e - 1] + 1) ++e;
