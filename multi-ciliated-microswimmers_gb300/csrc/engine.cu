@@ -33,6 +33,12 @@ struct mpcd_engine {
   long ncell = 0;
   int nsub = 0;
   cudaStream_t stream = nullptr;
+  // the beads' collision and the MD substeps run on their own (higher
+  // priority) stream, concurrently with the fluid pass: both only read the
+  // step's collision maps and add into the next step's cell sums
+  cudaStream_t smd = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool overlap = true;
   std::string error;
   long long launches = 0;
 
@@ -484,17 +490,18 @@ int device_error(mpcd_engine* h) {
 struct ProfScope {
   mpcd_engine* h;
   int kernel;
+  cudaStream_t s;
   cudaEvent_t a = nullptr, b = nullptr;
-  ProfScope(mpcd_engine* hh, int k) : h(hh), kernel(k) {
+  ProfScope(mpcd_engine* hh, int k, cudaStream_t st = nullptr) : h(hh), kernel(k), s(st ? st : hh->stream) {
     if (h->profiling) {
       cudaEventCreate(&a);
       cudaEventCreate(&b);
-      cudaEventRecord(a, h->stream);
+      cudaEventRecord(a, s);
     }
   }
   ~ProfScope() {
     if (h->profiling) {
-      cudaEventRecord(b, h->stream);
+      cudaEventRecord(b, s);
       h->marks.push_back({kernel, a, b});
     }
   }
@@ -598,6 +605,16 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
   cudaError_t e;
   if ((e = cudaSetDevice(p.device)) != cudaSuccess) return bail(e, "cudaSetDevice");
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+  {
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if ((e = cudaStreamCreateWithPriority(&h->smd, cudaStreamNonBlocking, prio_greatest)) != cudaSuccess)
+      return bail(e, "stream");
+    if ((e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
+    if ((e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
+    const char* env = std::getenv("MPCD_MD_OVERLAP");  // 0: MD after the fluid pass on one stream
+    h->overlap = !(env && std::atoi(env) == 0);
+  }
   if ((e = dalloc(&h->d_err, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_diss, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs, 16)) != cudaSuccess) return bail(e, "alloc");
@@ -663,6 +680,9 @@ int mpcd_destroy(mpcd_engine* h) {
     cudaEventDestroy(m.b);
   }
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->smd) cudaStreamDestroy(h->smd);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   delete h;
   return MPCD_OK;
 }
@@ -1002,27 +1022,40 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
     ProfScope ps(h, MPCD_K_CELL);
     h->launches += f64 ? launch_cell_params_f64(h->c64, s, h->stream) : launch_cell_params_f32(h->c32, s, h->stream);
   }
+  // fluid pass on the engine's stream; beads' collision and MD on smd, forked
+  // after the collision maps and joined before anything reads the new state
+  // (kernel timing runs them one after the other, so that each is timed alone)
+  const bool md = h->md.nslots > 0;
+  const bool fork = md && h->overlap && !h->profiling;
+  cudaStream_t sm = fork ? h->smd : h->stream;
+  if (fork) {
+    CK(cudaEventRecord(h->ev_fork, h->stream));
+    CK(cudaStreamWaitEvent(h->smd, h->ev_fork, 0));
+  }
+  if (md) {
+    {
+      ProfScope ps(h, MPCD_K_BEAD, sm);
+      h->launches += f64 ? launch_bead_collide_f64(h->md, h->c64, s, sm) : launch_bead_collide_f32(h->md, h->c32, s, sm);
+    }
+    ProfScope ps(h, MPCD_K_MD, sm);
+    if (h->md.cluster)
+      h->launches += f64 ? launch_md_cluster_f64cells(h->md, h->c64, ma, sm, &coop)
+                         : launch_md_cluster_f32cells(h->md, h->c32, ma, sm, &coop);
+    else if (h->md.df)
+      h->launches += f64 ? launch_md_df_f64cells(h->md, h->c64, ma, sm, &coop)
+                         : launch_md_df_f32cells(h->md, h->c32, ma, sm, &coop);
+    else
+      h->launches += f64 ? launch_md_f64(h->md, h->c64, ma, sm, &coop)
+                         : launch_md_f32cells(h->md, h->c32, ma, sm, &coop);
+  }
   {
     ProfScope ps(h, MPCD_K_FLUID);
     h->launches += f64 ? launch_fluid_step_f64(h->f64, h->c64, s, h->stream)
                        : launch_fluid_step_f32(h->f32, h->c32, s, h->stream);
   }
-  if (h->md.nslots) {
-    {
-      ProfScope ps(h, MPCD_K_BEAD);
-      h->launches += f64 ? launch_bead_collide_f64(h->md, h->c64, s, h->stream)
-                         : launch_bead_collide_f32(h->md, h->c32, s, h->stream);
-    }
-    ProfScope ps(h, MPCD_K_MD);
-    if (h->md.cluster)
-      h->launches += f64 ? launch_md_cluster_f64cells(h->md, h->c64, ma, h->stream, &coop)
-                         : launch_md_cluster_f32cells(h->md, h->c32, ma, h->stream, &coop);
-    else if (h->md.df)
-      h->launches += f64 ? launch_md_df_f64cells(h->md, h->c64, ma, h->stream, &coop)
-                         : launch_md_df_f32cells(h->md, h->c32, ma, h->stream, &coop);
-    else
-      h->launches += f64 ? launch_md_f64(h->md, h->c64, ma, h->stream, &coop)
-                         : launch_md_f32cells(h->md, h->c32, ma, h->stream, &coop);
+  if (fork) {
+    CK(cudaEventRecord(h->ev_join, h->smd));
+    CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
   }
   if (coop != cudaSuccess) return cuda_fail(h, coop, "cooperative MD launch");
   int rc = check_launch(h, "step");
