@@ -165,7 +165,8 @@ struct MDStepArgs {
 // ------------------------------------------------------------ launchers ---
 // All launchers enqueue on `s` and return the number of kernel launches.
 int launch_cell_params_f64(const CellsF64& c, const StepArgs& a, cudaStream_t s);
-int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s);
+// per_sm: resident CTAs per SM of the persistent grid (fewer leave room for a concurrent MD launch)
+int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s, int per_sm = 4);
 int launch_bin_fluid_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s);
 int launch_bead_collide_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s);
 int launch_bin_beads_f64(const MDState& m, const CellsF64& c, const StepArgs& a, cudaStream_t s);
@@ -182,7 +183,7 @@ int launch_sort_f64(FluidF64& f, FluidF64& tmp, const Box& box, uint32_t* count,
                     uint32_t* rank, uint32_t* blocksums, cudaStream_t s);
 
 int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s);
-int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s);
+int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s, int per_sm = 4);
 int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s);
 int launch_bead_collide_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);
 int launch_bin_beads_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);

@@ -701,9 +701,9 @@ int launch_cell_params_f64(const CellsF64& c, const StepArgs& a, cudaStream_t s)
   k_cell_params_f64<<<grid_for(c.ncell), kThreads, 0, s>>>(c, a);
   return 1;
 }
-int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s) {
+int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s, int per_sm) {
   if (f.n == 0) return 0;
-  k_fluid_step_f64<<<grid_for(f.n), kThreads, 0, s>>>(f, c, a);
+  k_fluid_step_f64<<<grid_for(f.n, kThreads, per_sm), kThreads, 0, s>>>(f, c, a);
   return 1;
 }
 int launch_bin_fluid_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s) {
@@ -748,9 +748,9 @@ int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s)
   k_cell_params_f32<<<grid_for(c.ncell), kThreads, 0, s>>>(c, a);
   return 1;
 }
-int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s) {
+int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s, int per_sm) {
   if (f.n == 0) return 0;
-  k_fluid_step_f32<<<grid_for(f.n), kThreads, 0, s>>>(f, c, a);
+  k_fluid_step_f32<<<grid_for(f.n, kThreads, per_sm), kThreads, 0, s>>>(f, c, a);
   return 1;
 }
 int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s) {
