@@ -159,19 +159,27 @@ __device__ __forceinline__ FluidPage fluid_page(const BatchTables& t, const Batc
   return P;
 }
 
+// The shifted cell of a fluid particle under the current grid shift: the
+// cell whose collision map it takes.
+// (box cells < 2^30: 32-bit index)
+__device__ __forceinline__ uint32_t fluid_cell_cur(const FluidPage& P, const float4 p) {
+  const uint32_t cp = __float_as_uint(p.w);
+  return (uint32_t)shifted_f(cell_x(cp), p.x, P.tc[0], P.L[0]) +
+         (uint32_t)P.L[0] * ((uint32_t)shifted_f(cell_y(cp), p.y, P.tc[1], P.L[1]) +
+                             (uint32_t)P.L[1] * (uint32_t)shifted_f(cell_z(cp), p.z, P.tc[2], P.L[2]));
+}
+
 // One fluid particle (MPCD::next_tstep's rotation, MPCD::move, Fluid::move,
 // add_impuls: src/libcilia/mpcd.cpp:140-267, src/libcilia/fluid.cpp:152-167):
-// collide with its cell's map, stream, wrap, body force, bin into the sums of
-// the next shift.  Returns the new state.
-__device__ __forceinline__ void fluid_particle(const FluidPage& P, const float4 p, const float4 v, float4& po, float4& vo,
-                                               float& ke_after, unsigned& bad) {
+// collide with its cell's map (mk, mu), stream, wrap, body force, bin into the
+// sums of the next shift.  Returns the new state.
+__device__ __forceinline__ void fluid_particle(const FluidPage& P, const float4 p, const float4 v, const float4 mk,
+                                               const float4 mu, float4& po, float4& vo, float& ke_after, unsigned& bad) {
   const int Lx = P.L[0], Ly = P.L[1], Lz = P.L[2];
   const uint32_t cp = __float_as_uint(p.w);
   int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
   float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
-  const long cid = shifted_f(ix, ox, P.tc[0], Lx) +
-                   (long)Lx * (shifted_f(iy, oy, P.tc[1], Ly) + (long)Ly * shifted_f(iz, oz, P.tc[2], Lz));
-  apply_map_f32(P.par + 2 * cid, vx, vy, vz);
+  apply_map_f32(mk, mu, vx, vy, vz);
   ke_after += vx * vx + vy * vy + vz * vz;
   ox = fmaf(vx, P.h, ox);
   oy = fmaf(vy, P.h, oy);
@@ -180,13 +188,24 @@ __device__ __forceinline__ void fluid_particle(const FluidPage& P, const float4 
   rewrap_f(oy, iy, Ly, bad);
   rewrap_f(oz, iz, Lz, bad);
   if (P.gk != 0.0f) vx += P.gk;
-  const long cn = shifted_f(ix, ox, P.tn[0], Lx) +
-                  (long)Lx * (shifted_f(iy, oy, P.tn[1], Ly) + (long)Ly * shifted_f(iz, oz, P.tn[2], Lz));
+  const uint32_t cn = (uint32_t)shifted_f(ix, ox, P.tn[0], Lx) +
+                      (uint32_t)Lx * ((uint32_t)shifted_f(iy, oy, P.tn[1], Ly) + (uint32_t)Ly * (uint32_t)shifted_f(iz, oz, P.tn[2], Lz));
   red_add_v4(P.sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
   atomicAdd(P.cnt + cn, 1u);
   po = make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz)));
   vo = make_float4(vx, vy, vz, 0.f);
 }
+
+__device__ __forceinline__ void fluid_particle(const FluidPage& P, const float4 p, const float4 v, float4& po,
+                                               float4& vo, float& ke_after, unsigned& bad) {
+  const float4* m = P.par + 2 * (size_t)fluid_cell_cur(P, p);
+  fluid_particle(P, p, v, __ldg(m), __ldg(m + 1), po, vo, ke_after, bad);
+}
+
+// Particles per thread whose loads (state, then collision map) are issued
+// together before their reductions and stores (the pass is bound by the
+// latency of the chain particle -> cell -> map).
+constexpr int kFluidBatchB = 2;
 
 __global__ void __launch_bounds__(512, 2) k_batch_fluid_step(BatchTables t, BatchFluid f, BatchCells c) {
   for (long pg = blockIdx.x; pg < t.npart_pages; pg += gridDim.x) {
@@ -199,12 +218,39 @@ __global__ void __launch_bounds__(512, 2) k_batch_fluid_step(BatchTables t, Batc
     const FluidPage P = fluid_page(t, c, r);
     float ke_after = 0.0f;
     unsigned bad = 0;
-#pragma unroll 2
-    for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      float4 po, vo;
-      fluid_particle(P, f.pos[i], f.vel[i], po, vo, ke_after, bad);
-      f.pos[i] = po;
-      f.vel[i] = vo;
+    constexpr int U = kFluidBatchB;
+    const int np = (int)(i1 - i0);  // page-local indices: 32-bit
+    float4* const pos = f.pos + i0;
+    float4* const vel = f.vel + i0;
+    for (int base = threadIdx.x; base < np; base += U * blockDim.x) {
+      float4 p[U], v[U], mk[U], mu[U];
+#pragma unroll
+      for (int q = 0; q < U; ++q) {
+        const int j = base + q * blockDim.x;
+        if (j < np) {
+          p[q] = __ldcs(pos + j);
+          v[q] = __ldcs(vel + j);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < U; ++q) {
+        const int j = base + q * blockDim.x;
+        if (j < np) {
+          const float4* m = P.par + 2 * (size_t)fluid_cell_cur(P, p[q]);
+          mk[q] = __ldg(m);
+          mu[q] = __ldg(m + 1);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < U; ++q) {
+        const int j = base + q * blockDim.x;
+        if (j < np) {
+          float4 po, vo;
+          fluid_particle(P, p[q], v[q], mk[q], mu[q], po, vo, ke_after, bad);
+          __stcs(pos + j, po);
+          __stcs(vel + j, vo);
+        }
+      }
     }
     if (bad) atomicOr(&t.state[r].err, bad);
     const double tot = block_sum_f32(ke_after);

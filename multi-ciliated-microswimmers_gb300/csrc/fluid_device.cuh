@@ -142,16 +142,19 @@ __device__ __forceinline__ void cell_map_f32(const float4 s0, const uint32_t w, 
   ldiss += s.w;
 }
 
-// v' = u + sc R (v - u) with the map {rx, ry, rz, sc}, {ux, uy, uz, 0}
-__device__ __forceinline__ void apply_map_f32(const float4* par, float& vx, float& vy, float& vz) {
+// v' = u + sc R (v - u) with the map k = {rx, ry, rz, sc}, u = {ux, uy, uz, 0}
+__device__ __forceinline__ void apply_map_f32(const float4 k, const float4 u, float& vx, float& vy, float& vz) {
   const float ca = (float)kCosAlpha, sa = (float)kSinAlpha, oc = 1.0f - (float)kCosAlpha;
-  const float4 k = __ldg(par + 0), u = __ldg(par + 1);
   const float wx = vx - u.x, wy = vy - u.y, wz = vz - u.z;
   const float kw = oc * (k.x * wx + k.y * wy + k.z * wz);
   const float cx = k.y * wz - k.z * wy, cy = k.z * wx - k.x * wz, cz = k.x * wy - k.y * wx;
   vx = fmaf(k.w, fmaf(ca, wx, fmaf(sa, cx, kw * k.x)), u.x);
   vy = fmaf(k.w, fmaf(ca, wy, fmaf(sa, cy, kw * k.y)), u.y);
   vz = fmaf(k.w, fmaf(ca, wz, fmaf(sa, cz, kw * k.z)), u.z);
+}
+
+__device__ __forceinline__ void apply_map_f32(const float4* par, float& vx, float& vy, float& vz) {
+  apply_map_f32(__ldg(par + 0), __ldg(par + 1), vx, vy, vz);
 }
 
 }  // namespace mpcd

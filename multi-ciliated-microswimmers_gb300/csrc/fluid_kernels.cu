@@ -11,7 +11,9 @@
 //   fluid_step  : per particle: v' = A v + b with the map of its shifted cell,
 //                 x' = x + v' h with periodic wrap, bin into the next shifted cell
 //                 (atomic sums).  One read and one write of the particle state.
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 
 #include "engine_internal.h"
 #include "fluid_device.cuh"
@@ -38,22 +40,42 @@ inline int sm_count() {
 inline int grid_for(long n, int threads = kThreads, int per_sm = 4) {
   long g = (n + threads - 1) / threads;
   if (g < 1) g = 1;
+  if (per_sm <= 0) {  // not persistent: -per_sm items per thread, short-lived CTAs
+    const long per = (long)threads * (per_sm < 0 ? -per_sm : 1);
+    g = (n + per - 1) / per;
+    return (int)(g < 1 ? 1 : (g > 0x7fffffffL ? 0x7fffffffL : g));
+  }
   const long cap = (long)sm_count() * per_sm;
   return (int)(g < cap ? g : cap);
 }
 
+// Threshold 1 - a of one axis as the two 32-bit halves of its IEEE pattern.
+struct Thresh {
+  int hi;
+  uint32_t lo;
+};
+__device__ __forceinline__ Thresh thresh(double t) { return {__double2hiint(t), (uint32_t)__double2loint(t)}; }
+
 // shifted cell along one axis from the cell index and the in-cell offset:
 // floor(i + o + a) = i + (o >= 1 - a), compared on the IEEE bit patterns
-// (both operands are non-negative doubles, so integer order = numeric order)
-__device__ __forceinline__ int shifted(int i, double o, long long ta_bits, int L) {
-  int s = i + (__double_as_longlong(o) >= ta_bits ? 1 : 0);
+// (for a non-negative threshold, integer order of the patterns = numeric
+// order), high word signed then low word unsigned: 32-bit integer
+// instructions only (64-bit compares take GB300's small FP64 pipe)
+__device__ __forceinline__ int shifted(int i, double o, Thresh t, int L) {
+  const int hi = __double2hiint(o);
+  const bool ge = hi > t.hi || (hi == t.hi && (uint32_t)__double2loint(o) >= t.lo);
+  const int s = i + (ge ? 1 : 0);
   return s == L ? 0 : s;
 }
 
+// true unless 0 <= o < 1 (negative, -0, >= 1, NaN): one 32-bit compare of the
+// high word (0x3FF00000 = high word of 1.0; the sign bit makes a negative
+// pattern larger)
+__device__ __forceinline__ bool off_unit(double o) { return (uint32_t)__double2hiint(o) >= 0x3FF00000u; }
+
 // reduce an offset that left [0,1) back into the cell (rare path)
 __device__ __forceinline__ void rewrap(double& o, int& i, int L, unsigned& bad) {
-  long long b = __double_as_longlong(o);
-  if (b < 0 || b >= 0x3FF0000000000000LL) {
+  if (off_unit(o)) {
     if (!(o > -1.0e9 && o < 1.0e9)) {  // non-finite: keep the particle in its cell and report
       o = 0.5;
       bad |= kErrCellRange;
@@ -231,27 +253,31 @@ __device__ __forceinline__ void wall_bounce(int walls, double ztop, double& x, d
   }
 }
 
+// I: particle index type (32-bit whenever the particle count allows, so that
+// no 64-bit integer work competes with the float64 arithmetic)
+template <typename I>
 __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF64 c, StepArgs a) {
   const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
-  const long long tcx = __double_as_longlong(a.ta_cur[0]), tcy = __double_as_longlong(a.ta_cur[1]),
-                  tcz = __double_as_longlong(a.ta_cur[2]);
-  const long long tnx = __double_as_longlong(a.ta_next[0]), tny = __double_as_longlong(a.ta_next[1]),
-                  tnz = __double_as_longlong(a.ta_next[2]);
-  const double h = a.h;
+  const Thresh tcx = thresh(a.ta_cur[0]), tcy = thresh(a.ta_cur[1]), tcz = thresh(a.ta_cur[2]);
+  const Thresh tnx = thresh(a.ta_next[0]), tny = thresh(a.ta_next[1]), tnz = thresh(a.ta_next[2]);
+  const double h = a.h, gk = a.gkick;
+  const bool kick = gk != 0.0, walls = a.walls != 0;
+  const I n = (I)f.n;
   double ke_after = 0.0;
   unsigned bad = 0;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+  for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (I)gridDim.x * blockDim.x) {
     const uint32_t cp = f.cell[i];
     int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
     double ox = f.ox[i], oy = f.oy[i], oz = f.oz[i];
     double vx = f.vx[i], vy = f.vy[i], vz = f.vz[i];
-    // collision with the map of the shifted cell
-    const long cid = shifted(ix, ox, tcx, Lx) + (long)Lx * (shifted(iy, oy, tcy, Ly) + (long)Ly * shifted(iz, oz, tcz, Lz));
-    apply_map_f64(c.par + 12 * cid, vx, vy, vz);
+    // collision with the map of the shifted cell (box cells < 2^30: 32-bit index)
+    const uint32_t cid = (uint32_t)shifted(ix, ox, tcx, Lx) +
+                         (uint32_t)Lx * ((uint32_t)shifted(iy, oy, tcy, Ly) + (uint32_t)Ly * (uint32_t)shifted(iz, oz, tcz, Lz));
+    apply_map_f64(c.par + 12 * (size_t)cid, vx, vy, vz);
     const double k_post = vx * vx + vy * vy + vz * vz;
     ke_after += k_post;
     // streaming
-    if (a.walls == 0) {
+    if (!walls) {
       ox = fma(vx, h, ox);
       oy = fma(vy, h, oy);
       oz = fma(vz, h, oz);
@@ -272,10 +298,11 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
     rewrap(ox, ix, Lx, bad);
     rewrap(oy, iy, Ly, bad);
     rewrap(oz, iz, Lz, bad);
-    if (a.gkick != 0.0) vx += a.gkick;
+    if (kick) vx += gk;
     // bin with the next shift
-    const long cn = shifted(ix, ox, tnx, Lx) + (long)Lx * (shifted(iy, oy, tny, Ly) + (long)Ly * shifted(iz, oz, tnz, Lz));
-    const double K = (a.gkick != 0.0 || a.walls != 0) ? vx * vx + vy * vy + vz * vz : k_post;
+    const uint32_t cn = (uint32_t)shifted(ix, ox, tnx, Lx) +
+                        (uint32_t)Lx * ((uint32_t)shifted(iy, oy, tny, Ly) + (uint32_t)Ly * (uint32_t)shifted(iz, oz, tnz, Lz));
+    const double K = (kick || walls) ? vx * vx + vy * vy + vz * vz : k_post;
     double* sp = reinterpret_cast<double*>(c.sum + cn);
     atomicAdd(sp + 0, vx);
     atomicAdd(sp + 1, vy);
@@ -297,8 +324,7 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
 
 __global__ void k_bin_fluid_f64(FluidF64 f, CellsF64 c, StepArgs a) {
   const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
-  const long long tcx = __double_as_longlong(a.ta_cur[0]), tcy = __double_as_longlong(a.ta_cur[1]),
-                  tcz = __double_as_longlong(a.ta_cur[2]);
+  const Thresh tcx = thresh(a.ta_cur[0]), tcy = thresh(a.ta_cur[1]), tcz = thresh(a.ta_cur[2]);
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
     const uint32_t cp = f.cell[i];
     const long cid = shifted(cell_x(cp), f.ox[i], tcx, Lx) +
@@ -557,54 +583,94 @@ __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
   if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
 }
 
-__global__ void __launch_bounds__(kThreads) k_fluid_step_f32(FluidF32 f, CellsF32 c, StepArgs a) {
+// Particles per thread whose loads (state, then collision map) are issued
+// together before any of their reductions and stores: the pass is bound by
+// the latency of the dependent chain particle -> cell -> map, so several
+// independent chains per thread keep more bytes in flight.
+constexpr int kFluidBatch = 2;
+// resident CTAs per SM the register budget of a batch size allows
+template <int U>
+struct FluidMinBlocks {
+  static constexpr int value = U >= 4 ? 2 : 4;
+};
+
+// kWalls: the bounce-back path (its float64 temporaries would otherwise
+// crowd the registers of the batched loads).
+template <int U, bool kWalls, typename I>
+__global__ void __launch_bounds__(kThreads, FluidMinBlocks<U>::value) k_fluid_step_f32(FluidF32 f, CellsF32 c, StepArgs a) {
   const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
   const float tcx = a.fta_cur[0], tcy = a.fta_cur[1], tcz = a.fta_cur[2];
   const float tnx = a.fta_next[0], tny = a.fta_next[1], tnz = a.fta_next[2];
   const float h = a.fh, gk = a.fgkick;
   float ke_after = 0.0f;
   unsigned bad = 0;
-#pragma unroll 2
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
-    const float4 p = f.pos[i];
-    const float4 v = f.vel[i];
-    const uint32_t cp = __float_as_uint(p.w);
-    int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
-    float ox = p.x, oy = p.y, oz = p.z, vx = v.x, vy = v.y, vz = v.z;
-    const long cid = shifted_f(ix, ox, tcx, Lx) + (long)Lx * (shifted_f(iy, oy, tcy, Ly) + (long)Ly * shifted_f(iz, oz, tcz, Lz));
-    apply_map_f32(c.par + 2 * cid, vx, vy, vz);
-    ke_after += vx * vx + vy * vy + vz * vz;
-    if (a.walls == 0) {
-      ox = fmaf(vx, h, ox);
-      oy = fmaf(vy, h, oy);
-      oz = fmaf(vz, h, oz);
-    } else {
-      double x = ix + (double)ox, y = iy + (double)oy, z = iz + (double)oz;
-      double dvx = vx, dvy = vy, dvz = vz;
-      x += dvx * a.h;
-      y += dvy * a.h;
-      z += dvz * a.h;
-      wall_bounce(a.walls, (double)(Lz - 1), x, y, z, dvx, dvy, dvz);
-      double fx = floor(x), fy = floor(y), fz = floor(z);
-      ox = (float)(x - fx);
-      oy = (float)(y - fy);
-      oz = (float)(z - fz);
-      ix = (((int)fx % Lx) + Lx) % Lx;
-      iy = (((int)fy % Ly) + Ly) % Ly;
-      iz = (((int)fz % Lz) + Lz) % Lz;
-      vx = (float)dvx;
-      vy = (float)dvy;
-      vz = (float)dvz;
+  const I n = (I)f.n;
+  // each block takes U x blockDim consecutive particles per round
+  for (I base = (I)blockIdx.x * U * blockDim.x + threadIdx.x; base < n; base += (I)gridDim.x * U * blockDim.x) {
+    float4 p[U], v[U], mk[U], mu[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const I i = base + (I)q * blockDim.x;
+      if (i < n) {
+        p[q] = __ldcs(f.pos + i);
+        v[q] = __ldcs(f.vel + i);
+      }
     }
-    rewrap_f(ox, ix, Lx, bad);
-    rewrap_f(oy, iy, Ly, bad);
-    rewrap_f(oz, iz, Lz, bad);
-    if (gk != 0.0f) vx += gk;
-    const long cn = shifted_f(ix, ox, tnx, Lx) + (long)Lx * (shifted_f(iy, oy, tny, Ly) + (long)Ly * shifted_f(iz, oz, tnz, Lz));
-    red_add_v4(c.sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
-    atomicAdd(c.cnt + cn, 1u);
-    f.pos[i] = make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz)));
-    f.vel[i] = make_float4(vx, vy, vz, 0.f);
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const I i = base + (I)q * blockDim.x;
+      if (i < n) {
+        const uint32_t cp = __float_as_uint(p[q].w);
+        const uint32_t cid = (uint32_t)shifted_f(cell_x(cp), p[q].x, tcx, Lx) +
+                             (uint32_t)Lx * ((uint32_t)shifted_f(cell_y(cp), p[q].y, tcy, Ly) +
+                                             (uint32_t)Ly * (uint32_t)shifted_f(cell_z(cp), p[q].z, tcz, Lz));
+        const float4* m = c.par + 2 * (size_t)cid;
+        mk[q] = __ldg(m);
+        mu[q] = __ldg(m + 1);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const I i = base + (I)q * blockDim.x;
+      if (i >= n) continue;
+      const uint32_t cp = __float_as_uint(p[q].w);
+      int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
+      float ox = p[q].x, oy = p[q].y, oz = p[q].z, vx = v[q].x, vy = v[q].y, vz = v[q].z;
+      apply_map_f32(mk[q], mu[q], vx, vy, vz);
+      ke_after += vx * vx + vy * vy + vz * vz;
+      if (!kWalls) {
+        ox = fmaf(vx, h, ox);
+        oy = fmaf(vy, h, oy);
+        oz = fmaf(vz, h, oz);
+      } else {
+        double x = ix + (double)ox, y = iy + (double)oy, z = iz + (double)oz;
+        double dvx = vx, dvy = vy, dvz = vz;
+        x += dvx * a.h;
+        y += dvy * a.h;
+        z += dvz * a.h;
+        wall_bounce(a.walls, (double)(Lz - 1), x, y, z, dvx, dvy, dvz);
+        double fx = floor(x), fy = floor(y), fz = floor(z);
+        ox = (float)(x - fx);
+        oy = (float)(y - fy);
+        oz = (float)(z - fz);
+        ix = (((int)fx % Lx) + Lx) % Lx;
+        iy = (((int)fy % Ly) + Ly) % Ly;
+        iz = (((int)fz % Lz) + Lz) % Lz;
+        vx = (float)dvx;
+        vy = (float)dvy;
+        vz = (float)dvz;
+      }
+      rewrap_f(ox, ix, Lx, bad);
+      rewrap_f(oy, iy, Ly, bad);
+      rewrap_f(oz, iz, Lz, bad);
+      if (gk != 0.0f) vx += gk;
+      const uint32_t cn = (uint32_t)shifted_f(ix, ox, tnx, Lx) +
+                          (uint32_t)Lx * ((uint32_t)shifted_f(iy, oy, tny, Ly) + (uint32_t)Ly * (uint32_t)shifted_f(iz, oz, tnz, Lz));
+      red_add_v4(c.sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
+      atomicAdd(c.cnt + cn, 1u);
+      __stcs(f.pos + i, make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz))));
+      __stcs(f.vel + i, make_float4(vx, vy, vz, 0.f));
+    }
   }
   if (bad) atomicOr(a.err, bad);
   const double tot = block_sum_f32(ke_after);
@@ -703,7 +769,11 @@ int launch_cell_params_f64(const CellsF64& c, const StepArgs& a, cudaStream_t s)
 }
 int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s, int per_sm) {
   if (f.n == 0) return 0;
-  k_fluid_step_f64<<<grid_for(f.n, kThreads, per_sm), kThreads, 0, s>>>(f, c, a);
+  const int grid = grid_for(f.n, kThreads, per_sm);
+  if (f.n + (long)grid * kThreads < (1L << 32))
+    k_fluid_step_f64<uint32_t><<<grid, kThreads, 0, s>>>(f, c, a);
+  else
+    k_fluid_step_f64<long><<<grid, kThreads, 0, s>>>(f, c, a);
   return 1;
 }
 int launch_bin_fluid_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s) {
@@ -750,7 +820,30 @@ int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s)
 }
 int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s, int per_sm) {
   if (f.n == 0) return 0;
-  k_fluid_step_f32<<<grid_for(f.n, kThreads, per_sm), kThreads, 0, s>>>(f, c, a);
+  const int g1 = grid_for(f.n, kThreads, per_sm);
+  const bool i32 = f.n + 4L * g1 * kThreads < (1L << 32);
+  if (a.walls != 0) {
+    i32 ? k_fluid_step_f32<1, true, uint32_t><<<g1, kThreads, 0, s>>>(f, c, a)
+        : k_fluid_step_f32<1, true, long><<<g1, kThreads, 0, s>>>(f, c, a);
+    return 1;
+  }
+  // particles per thread and round: kFluidBatch unless MPCD_FLUID_BATCH (1, 2, 4) says otherwise
+  static const int batch = [] {
+    const char* e = std::getenv("MPCD_FLUID_BATCH");
+    const int b = e ? std::atoi(e) : kFluidBatch;
+    return b == 1 || b == 4 ? b : 2;
+  }();
+  const int ps = per_sm <= 0 ? per_sm : std::min(per_sm, batch == 4 ? FluidMinBlocks<4>::value : FluidMinBlocks<2>::value);
+  const int gb = grid_for((f.n + batch - 1) / batch, kThreads, ps);
+  if (batch == 4)
+    i32 ? k_fluid_step_f32<4, false, uint32_t><<<gb, kThreads, 0, s>>>(f, c, a)
+        : k_fluid_step_f32<4, false, long><<<gb, kThreads, 0, s>>>(f, c, a);
+  else if (batch == 2)
+    i32 ? k_fluid_step_f32<2, false, uint32_t><<<gb, kThreads, 0, s>>>(f, c, a)
+        : k_fluid_step_f32<2, false, long><<<gb, kThreads, 0, s>>>(f, c, a);
+  else
+    i32 ? k_fluid_step_f32<1, false, uint32_t><<<gb, kThreads, 0, s>>>(f, c, a)
+        : k_fluid_step_f32<1, false, long><<<gb, kThreads, 0, s>>>(f, c, a);
   return 1;
 }
 int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s) {

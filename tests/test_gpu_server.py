@@ -13,8 +13,13 @@ collision partners), so:
     swimmer's cells, which feel its float-rounded bead velocities) is at most
     2x (+0.5 %) that share between two runs alone;
   - over a longer run (40 steps) the difference between the alone and the
-    mixed result is no larger than 5x (+1e-3) the difference between two runs
-    of the request alone, and kT agrees within 3e-3.
+    mixed result is of the size of the differences among runs alone.  Those
+    scatter widely (maximum bead deviations between two runs alone measured
+    from 0.005 to 0.09 after 40 steps), so the reference is the largest of
+    the three pairwise differences among three runs alone, and the mixed
+    result's difference is the median over those three runs; it must stay
+    within 3x (+1e-3) of the reference, both in the largest and in the RMS
+    bead deviation; kT agrees within 3e-3.
 """
 import numpy as np
 import pytest
@@ -103,13 +108,21 @@ def test_result_same_alone_and_in_the_mix():
 
 def test_long_run_mix_within_the_run_to_run_spread():
     target = request_cfg(16, 5, seed=3)
-    ia, (pa, _), _ = run_alone(target, 40, 77)
-    ib, (pb, _), _ = run_alone(target, 40, 77)
+    alone = [run_alone(target, 40, 77) for _ in range(3)]
     im, (pm, _), _, _ = run_in_mix(target, 40, 77)
-    spread = np.abs(pa - pb).max()
-    diff = np.abs(pa - pm).max()
-    assert diff < 5 * spread + 1e-3, (diff, spread)
-    assert abs(ia["obs"]["kT"] - im["obs"]["kT"]) < 3e-3
+    pos = [b[0] for _, b, _ in alone]
+
+    def dev(a, b):
+        d = np.abs(a - b)
+        return d.max(), float(np.sqrt((d ** 2).mean()))
+
+    ref = [dev(pos[i], pos[j]) for i, j in ((0, 1), (0, 2), (1, 2))]
+    mix = [dev(p, pm) for p in pos]
+    ref_max, ref_rms = max(r[0] for r in ref), max(r[1] for r in ref)
+    mix_max, mix_rms = float(np.median([m[0] for m in mix])), float(np.median([m[1] for m in mix]))
+    assert mix_max < 3 * ref_max + 1e-3, (mix_max, ref_max, ref, mix)
+    assert mix_rms < 3 * ref_rms + 1e-3, (mix_rms, ref_rms, ref, mix)
+    assert abs(alone[0][0]["obs"]["kT"] - im["obs"]["kT"]) < 3e-3
 
 
 def test_admission_respects_the_budget():

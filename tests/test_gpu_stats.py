@@ -85,7 +85,11 @@ def test_temperature_and_vacf_match_oracle(precision, oracle_vacf):
 # The run-to-run spread is large (oracle, 10 seeds: v2 6.1e-4 with sd 12 %,
 # speed 0.0126 with sd 8 %, rate 0.0041 with sd 8 %), so the test states
 # agreement of the GPU and oracle means within 3.5 standard errors of their
-# difference, the standard deviation pooled over both groups.
+# difference, the standard deviation pooled over both groups; twelve oracle
+# seeds and eight GPU seeds (with six each, one draw of six oracle seeds gave
+# v2 = 5.6e-4 and a pooled standard error a third of the one the spread
+# above implies).  v2 is also checked against equipartition, 3 kT / M with M
+# the swimmer's total mass (931 beads of mass 5: 6.4e-4), within 20 %.
 SWIM_WARM, SWIM_STEPS, SWIM_EVERY, SWIM_LAG = 200, 2000, 10, 5
 
 
@@ -121,7 +125,7 @@ def oracle_swimmer():
     from oracle import build_from_cfg
 
     runs = []
-    for seed in (11, 12, 13, 14, 15, 16):
+    for seed in range(11, 23):
         o = build_from_cfg(swimmer_cfg(), seed=seed, ststep=0.002)
         o.set_threads(8)
         runs.append(swimmer_observables(o.step, o.beads))
@@ -133,9 +137,11 @@ def test_swimmer_speed_and_rotation_match_oracle(precision, oracle_swimmer):
     import simcfg
 
     runs = []
-    for seed in (21, 22, 23, 24, 25, 26):
+    nbeads = 0
+    for seed in range(21, 29):
         s = cg.Sim(simcfg.dumps(swimmer_cfg()), precision=precision, ststep=0.002, seed=seed)
         runs.append(swimmer_observables(s.next_tstep, s.beads))
+        nbeads = s.nbeads
         s.close()
     g, o = np.array(runs), oracle_swimmer
     mg, mo = g.mean(axis=0), o.mean(axis=0)
@@ -145,3 +151,5 @@ def test_swimmer_speed_and_rotation_match_oracle(precision, oracle_swimmer):
     print("swimmer v2/speed/rate gpu", mg, "oracle", mo, "se", se)
     assert np.all(mo > 0) and np.all(mg > 0)
     assert np.all(np.abs(mg - mo) < 3.5 * se), (mg, mo, se)
+    equi = 3.0 / (nbeads * 5.0)
+    assert nbeads == 931 and abs(mg[0] / equi - 1.0) < 0.2 and abs(mo[0] / equi - 1.0) < 0.2, (mg[0], mo[0], equi)
