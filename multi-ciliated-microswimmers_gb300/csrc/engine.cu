@@ -49,6 +49,7 @@ struct mpcd_engine {
   unsigned* d_err = nullptr;
   double* d_diss = nullptr;
   double* d_obs = nullptr;
+  double* h_obs = nullptr;  // pinned: observables, dissipated energy and error bits of one read-back
   unsigned* d_bar = nullptr;
 
   FluidF64 f64, f64tmp;
@@ -221,23 +222,6 @@ int alloc_fluid(mpcd_engine* h, long n) {
   cudaFree(h->d_rank);
   CK(dalloc(&h->d_rank, n));
   return MPCD_OK;
-}
-
-// wrap an unwrapped coordinate into cell index + offset in [0,1)
-inline void wrap_coord(double x, int L, int& i, double& o) {
-  double xw = x - std::floor(x / L) * L;
-  if (xw >= L) xw -= L;
-  if (xw < 0) xw += L;
-  double fi = std::floor(xw);
-  i = (int)fi;
-  o = xw - fi;
-  if (i >= L) {
-    i -= L;
-  }
-  if (o >= 1.0) {
-    o = 0.0;
-    i = (i + 1) % L;
-  }
 }
 
 StepArgs step_args(mpcd_engine* h, const double* a_cur, const double* a_next, double t_move) {
@@ -623,6 +607,7 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
   if ((e = dalloc(&h->d_err, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_diss, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs, 16)) != cudaSuccess) return bail(e, "alloc");
+  if ((e = cudaMallocHost((void**)&h->h_obs, 16 * sizeof(double))) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_bar, 2)) != cudaSuccess) return bail(e, "alloc");
   cudaMemset(h->d_err, 0, sizeof(unsigned));
   cudaMemset(h->d_diss, 0, sizeof(double));
@@ -678,6 +663,7 @@ int mpcd_destroy(mpcd_engine* h) {
   cudaFree(h->d_err);
   cudaFree(h->d_diss);
   cudaFree(h->d_obs);
+  cudaFreeHost(h->h_obs);
   cudaFree(h->d_bar);
   cudaFree(h->flush_buf);
   for (auto& m : h->marks) {
@@ -700,63 +686,48 @@ long mpcd_fluid_count(const mpcd_engine* h) {
   return h->p.precision == MPCD_FP64 ? h->f64.n : h->f32.n;
 }
 
+// Device staging of the caller's N x 3 float64 arrays (pos, vel): 48 bytes per
+// particle, released when the transfer is done.
+struct Staging {
+  double* d = nullptr;
+  unsigned* flag = nullptr;
+  ~Staging() {
+    cudaFree(d);
+    cudaFree(flag);
+  }
+  cudaError_t alloc(long n) {
+    cudaError_t e = dalloc(&d, 6 * (size_t)(n > 0 ? n : 1));
+    if (e == cudaSuccess) e = dalloc(&flag, 1);
+    if (e == cudaSuccess) e = cudaMemset(flag, 0, sizeof(unsigned));
+    return e;
+  }
+};
+
 int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel) {
   if (!h || n < 0 || (n > 0 && (!pos || !vel))) return fail(h, MPCD_EINVAL, "set_fluid: bad arguments");
   if (n > 0x7fffffffL) return fail(h, MPCD_EINVAL, "set_fluid: more than 2^31 - 1 particles");
-  for (long i = 0; i < 3 * n; ++i)
-    if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || std::fabs(pos[i]) > 1e12)
-      return fail(h, MPCD_EINVAL, "set_fluid: non-finite or out-of-range position or velocity");
+  Staging st;
+  CK(st.alloc(n));
+  double* dpos = st.d;
+  double* dvel = st.d + 3 * (size_t)n;
+  if (n > 0) {
+    // the caller's arrays as they are; validation, wrapping into cell +
+    // offset and the split into the kernels' layout run on the device
+    CK(cudaMemcpyAsync(dpos, pos, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(dvel, vel, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    h->launches += launch_check_fluid(n, dpos, dvel, st.flag, h->stream);
+    unsigned bad = 0;
+    CK(cudaMemcpyAsync(&bad, st.flag, sizeof bad, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (bad) return fail(h, MPCD_EINVAL, "set_fluid: non-finite or out-of-range position or velocity");
+  }
   int rc = alloc_fluid(h, n);
   if (rc) return rc;
-  const int* L = h->box.L;
-  if (h->p.precision == MPCD_FP64) {
-    std::vector<uint32_t> cell(n);
-    std::vector<double> o[3], v[3];
-    for (int q = 0; q < 3; ++q) {
-      o[q].resize(n);
-      v[q].resize(n);
-    }
-    for (long i = 0; i < n; ++i) {
-      int c[3];
-      for (int q = 0; q < 3; ++q) {
-        wrap_coord(pos[3 * i + q], L[q], c[q], o[q][i]);
-        v[q][i] = vel[3 * i + q];
-      }
-      cell[i] = pack_cell(c[0], c[1], c[2]);
-    }
-    std::vector<uint32_t> ids(n);
-    for (long i = 0; i < n; ++i) ids[i] = (uint32_t)i;
-    CK(cudaMemcpy(h->f64.id, ids.data(), n * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f64.cell, cell.data(), n * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f64.ox, o[0].data(), n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f64.oy, o[1].data(), n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f64.oz, o[2].data(), n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f64.vx, v[0].data(), n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f64.vy, v[1].data(), n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f64.vz, v[2].data(), n * 8, cudaMemcpyHostToDevice));
-  } else {
-    std::vector<float4> P(n), V(n);
-    for (long i = 0; i < n; ++i) {
-      int c[3];
-      double o[3];
-      for (int q = 0; q < 3; ++q) wrap_coord(pos[3 * i + q], L[q], c[q], o[q]);
-      float f[3];
-      for (int q = 0; q < 3; ++q) {
-        f[q] = (float)o[q];
-        if (f[q] >= 1.0f) {  // rounding up to 1: move to the next cell
-          f[q] = 0.0f;
-          c[q] = (c[q] + 1) % L[q];
-        }
-      }
-      P[i] = make_float4(f[0], f[1], f[2], bits_to_float(pack_cell(c[0], c[1], c[2])));
-      V[i] = make_float4((float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f);
-    }
-    std::vector<uint32_t> ids(n);
-    for (long i = 0; i < n; ++i) ids[i] = (uint32_t)i;
-    CK(cudaMemcpy(h->f32.id, ids.data(), n * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f32.pos, P.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->f32.vel, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-  }
+  if (h->p.precision == MPCD_FP64)
+    h->launches += launch_load_fluid_f64(n, dpos, dvel, h->box, h->f64, h->stream);
+  else
+    h->launches += launch_load_fluid_f32(n, dpos, dvel, h->box, h->f32, h->stream);
+  CK(cudaStreamSynchronize(h->stream));  // the staging buffer is released on return
   h->prepared = false;
   return MPCD_OK;
 }
@@ -765,54 +736,22 @@ int mpcd_get_fluid(mpcd_engine* h, long n, double* pos, double* vel) {
   if (!h) return MPCD_EINVAL;
   const long have = mpcd_fluid_count(h);
   if (n != have) return fail(h, MPCD_EINVAL, "get_fluid: n does not match the fluid size");
+  if (n == 0) return device_error(h);
+  Staging st;
+  CK(st.alloc(n));
+  double* dpos = st.d;
+  double* dvel = st.d + 3 * (size_t)n;
+  // back into the caller's order (by particle id) and layout on the device
+  if (h->p.precision == MPCD_FP64)
+    h->launches += launch_store_fluid_f64(h->f64, dpos, dvel, st.flag, h->stream);
+  else
+    h->launches += launch_store_fluid_f32(h->f32, dpos, dvel, st.flag, h->stream);
+  unsigned bad = 0;
+  CK(cudaMemcpyAsync(&bad, st.flag, sizeof bad, cudaMemcpyDeviceToHost, h->stream));
+  if (pos) CK(cudaMemcpyAsync(pos, dpos, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (vel) CK(cudaMemcpyAsync(vel, dvel, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  if (h->p.precision == MPCD_FP64) {
-    std::vector<uint32_t> cell(n);
-    std::vector<double> o[3], v[3];
-    for (int q = 0; q < 3; ++q) {
-      o[q].resize(n);
-      v[q].resize(n);
-    }
-    CK(cudaMemcpy(cell.data(), h->f64.cell, n * 4, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(o[0].data(), h->f64.ox, n * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(o[1].data(), h->f64.oy, n * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(o[2].data(), h->f64.oz, n * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(v[0].data(), h->f64.vx, n * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(v[1].data(), h->f64.vy, n * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(v[2].data(), h->f64.vz, n * 8, cudaMemcpyDeviceToHost));
-    std::vector<uint32_t> ids(n);
-    CK(cudaMemcpy(ids.data(), h->f64.id, n * 4, cudaMemcpyDeviceToHost));
-    for (long i = 0; i < n; ++i) {
-      const long d = ids[i];
-      if (d < 0 || d >= n) return fail(h, MPCD_EDEVICE, "particle id out of range");
-      const int c[3] = {cell_x(cell[i]), cell_y(cell[i]), cell_z(cell[i])};
-      for (int q = 0; q < 3; ++q) {
-        if (pos) pos[3 * d + q] = c[q] + o[q][i];
-        if (vel) vel[3 * d + q] = v[q][i];
-      }
-    }
-  } else {
-    std::vector<float4> P(n), V(n);
-    CK(cudaMemcpy(P.data(), h->f32.pos, n * sizeof(float4), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(V.data(), h->f32.vel, n * sizeof(float4), cudaMemcpyDeviceToHost));
-    std::vector<uint32_t> ids(n);
-    CK(cudaMemcpy(ids.data(), h->f32.id, n * 4, cudaMemcpyDeviceToHost));
-    for (long i = 0; i < n; ++i) {
-      const long d = ids[i];
-      if (d < 0 || d >= n) return fail(h, MPCD_EDEVICE, "particle id out of range");
-      uint32_t cp = float_to_bits(P[i].w);
-      if (pos) {
-        pos[3 * d] = cell_x(cp) + (double)P[i].x;
-        pos[3 * d + 1] = cell_y(cp) + (double)P[i].y;
-        pos[3 * d + 2] = cell_z(cp) + (double)P[i].z;
-      }
-      if (vel) {
-        vel[3 * d] = V[i].x;
-        vel[3 * d + 1] = V[i].y;
-        vel[3 * d + 2] = V[i].z;
-      }
-    }
-  }
+  if (bad) return fail(h, MPCD_EDEVICE, "particle id out of range");
   return device_error(h);
 }
 
@@ -1113,10 +1052,15 @@ int mpcd_observables(mpcd_engine* h, mpcd_obs* out) {
     h->launches += launch_observables_f64(h->f64, h->md, h->p.bead_mass, h->d_obs, h->stream);
   else
     h->launches += launch_observables_f32(h->f32, h->md, h->p.bead_mass, h->d_obs, h->stream);
-  double o[8], diss = 0.0;
-  CK(cudaMemcpyAsync(o, h->d_obs, sizeof o, cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaMemcpyAsync(&diss, h->d_diss, sizeof diss, cudaMemcpyDeviceToHost, h->stream));
+  // one read-back into pinned memory: the sums, the dissipated energy, the error bits
+  double* o = h->h_obs;
+  CK(cudaMemcpyAsync(o, h->d_obs, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(o + 8, h->d_diss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(o + 9, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  const double diss = o[8];
+  unsigned err_bits;
+  std::memcpy(&err_bits, o + 9, sizeof err_bits);
   const double M = o[5] > 0 ? o[5] : 1.0, N = o[4] > 0 ? o[4] : 1.0;
   out->momentum[0] = o[0] / M;
   out->momentum[1] = o[1] / M;
@@ -1128,7 +1072,7 @@ int mpcd_observables(mpcd_engine* h, mpcd_obs* out) {
   out->diss_energy = diss;
   out->globalt = h->globalt;
   out->energy_fluid = 0.5 * o[6];
-  return device_error(h);
+  return err_bits ? device_error(h) : MPCD_OK;
 }
 
 int mpcd_timed_run(mpcd_engine* h, int nsteps, int flush_l2, double* step_ms) {

@@ -183,6 +183,14 @@ int launch_sort_f64(FluidF64& f, FluidF64& tmp, const Box& box, uint32_t* count,
                     uint32_t* rank, uint32_t* blocksums, cudaStream_t s);
 
 int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s);
+// caller arrays (float64, N x 3, staged in device memory) <-> fluid layout
+int launch_check_fluid(long n, const double* pos, const double* vel, unsigned* bad, cudaStream_t s);
+int launch_load_fluid_f64(long n, const double* pos, const double* vel, const Box& box, const FluidF64& f,
+                          cudaStream_t s);
+int launch_load_fluid_f32(long n, const double* pos, const double* vel, const Box& box, const FluidF32& f,
+                          cudaStream_t s);
+int launch_store_fluid_f64(const FluidF64& f, double* pos, double* vel, unsigned* bad, cudaStream_t s);
+int launch_store_fluid_f32(const FluidF32& f, double* pos, double* vel, unsigned* bad, cudaStream_t s);
 int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s, int per_sm = 4);
 int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s);
 int launch_bead_collide_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);

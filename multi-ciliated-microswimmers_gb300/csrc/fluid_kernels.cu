@@ -759,6 +759,115 @@ __global__ void k_observables_f32(FluidF32 f, MDState m, double bead_mass, doubl
   }
 }
 
+// ====================================================== host interchange ===
+// Fluid state to and from the caller's float64 arrays (positions N x 3,
+// unwrapped allowed; velocities N x 3), staged in device memory as they
+// are: the conversion to cell + offset, the split into the kernels' layout
+// and the return to input order by particle id run here, one thread per
+// particle, instead of in host loops.
+
+// 1 for a non-finite or out-of-range (|x| > 1e12) position or velocity
+__global__ void k_check_fluid(long n, const double* pos, const double* vel, unsigned* bad) {
+  unsigned b = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n; i += (long)gridDim.x * blockDim.x) {
+    const double x = pos[i], v = vel[i];
+    if (!(fabs(x) <= 1e12) || !isfinite(v)) b = 1u;
+  }
+  if (__syncthreads_or(b) && threadIdx.x == 0) atomicOr(bad, 1u);
+}
+
+// an unwrapped coordinate as cell index + offset in [0,1); explicit
+// roundings (no contraction into a fused multiply-add) so that the result is
+// the same as the host's plain float64 arithmetic
+__device__ __forceinline__ void wrap_coord_dev(double x, int L, int& i, double& o) {
+  const double dl = (double)L;
+  double xw = __dsub_rn(x, __dmul_rn(floor(__ddiv_rn(x, dl)), dl));
+  if (xw >= dl) xw = __dsub_rn(xw, dl);
+  if (xw < 0) xw = __dadd_rn(xw, dl);
+  const double fi = floor(xw);
+  i = (int)fi;
+  o = __dsub_rn(xw, fi);
+  if (i >= L) i -= L;
+  if (o >= 1.0) {
+    o = 0.0;
+    i = (i + 1) % L;
+  }
+}
+
+__global__ void k_load_fluid_f64(long n, const double* pos, const double* vel, Box box, FluidF64 f) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    int c[3];
+    double o[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) wrap_coord_dev(pos[3 * i + q], box.L[q], c[q], o[q]);
+    f.id[i] = (uint32_t)i;
+    f.cell[i] = pack_cell(c[0], c[1], c[2]);
+    f.ox[i] = o[0];
+    f.oy[i] = o[1];
+    f.oz[i] = o[2];
+    f.vx[i] = vel[3 * i];
+    f.vy[i] = vel[3 * i + 1];
+    f.vz[i] = vel[3 * i + 2];
+  }
+}
+
+__global__ void k_load_fluid_f32(long n, const double* pos, const double* vel, Box box, FluidF32 f) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    int c[3];
+    float o[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      double od;
+      wrap_coord_dev(pos[3 * i + q], box.L[q], c[q], od);
+      o[q] = __double2float_rn(od);
+      if (o[q] >= 1.0f) {  // rounding up to 1: move to the next cell
+        o[q] = 0.0f;
+        c[q] = (c[q] + 1) % box.L[q];
+      }
+    }
+    f.id[i] = (uint32_t)i;
+    f.pos[i] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell(c[0], c[1], c[2])));
+    f.vel[i] = make_float4(__double2float_rn(vel[3 * i]), __double2float_rn(vel[3 * i + 1]),
+                           __double2float_rn(vel[3 * i + 2]), 0.0f);
+  }
+}
+
+// back to input order: particle k of the caller is the one with id k
+__global__ void k_store_fluid_f64(FluidF64 f, double* pos, double* vel, unsigned* bad) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const long d = f.id[i];
+    if (d >= f.n) {
+      atomicOr(bad, 1u);
+      continue;
+    }
+    const uint32_t cp = f.cell[i];
+    pos[3 * d] = __dadd_rn((double)cell_x(cp), f.ox[i]);
+    pos[3 * d + 1] = __dadd_rn((double)cell_y(cp), f.oy[i]);
+    pos[3 * d + 2] = __dadd_rn((double)cell_z(cp), f.oz[i]);
+    vel[3 * d] = f.vx[i];
+    vel[3 * d + 1] = f.vy[i];
+    vel[3 * d + 2] = f.vz[i];
+  }
+}
+
+__global__ void k_store_fluid_f32(FluidF32 f, double* pos, double* vel, unsigned* bad) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const long d = f.id[i];
+    if (d >= f.n) {
+      atomicOr(bad, 1u);
+      continue;
+    }
+    const float4 p = f.pos[i], v = f.vel[i];
+    const uint32_t cp = __float_as_uint(p.w);
+    pos[3 * d] = __dadd_rn((double)cell_x(cp), (double)p.x);
+    pos[3 * d + 1] = __dadd_rn((double)cell_y(cp), (double)p.y);
+    pos[3 * d + 2] = __dadd_rn((double)cell_z(cp), (double)p.z);
+    vel[3 * d] = v.x;
+    vel[3 * d + 1] = v.y;
+    vel[3 * d + 2] = v.z;
+  }
+}
+
 }  // namespace
 
 // ============================================================ launchers ===
@@ -878,6 +987,34 @@ int launch_sort_f32(FluidF32& f, FluidF32& tmp, const Box& box, uint32_t* count,
   f = tmp;
   tmp = t;
   return k + 1;
+}
+
+int launch_check_fluid(long n, const double* pos, const double* vel, unsigned* bad, cudaStream_t s) {
+  if (n == 0) return 0;
+  k_check_fluid<<<grid_for(3 * n), kThreads, 0, s>>>(n, pos, vel, bad);
+  return 1;
+}
+int launch_load_fluid_f64(long n, const double* pos, const double* vel, const Box& box, const FluidF64& f,
+                          cudaStream_t s) {
+  if (n == 0) return 0;
+  k_load_fluid_f64<<<grid_for(n), kThreads, 0, s>>>(n, pos, vel, box, f);
+  return 1;
+}
+int launch_load_fluid_f32(long n, const double* pos, const double* vel, const Box& box, const FluidF32& f,
+                          cudaStream_t s) {
+  if (n == 0) return 0;
+  k_load_fluid_f32<<<grid_for(n), kThreads, 0, s>>>(n, pos, vel, box, f);
+  return 1;
+}
+int launch_store_fluid_f64(const FluidF64& f, double* pos, double* vel, unsigned* bad, cudaStream_t s) {
+  if (f.n == 0) return 0;
+  k_store_fluid_f64<<<grid_for(f.n), kThreads, 0, s>>>(f, pos, vel, bad);
+  return 1;
+}
+int launch_store_fluid_f32(const FluidF32& f, double* pos, double* vel, unsigned* bad, cudaStream_t s) {
+  if (f.n == 0) return 0;
+  k_store_fluid_f32<<<grid_for(f.n), kThreads, 0, s>>>(f, pos, vel, bad);
+  return 1;
 }
 
 }  // namespace mpcd
