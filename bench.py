@@ -50,7 +50,7 @@ METRIC = "MPCD particle-steps/s"
 # DRAM bytes (read + write) per fluid particle of one fluid_step launch, from
 # one ncu capture on swimmer64 (profiles/fluid_step_swimmer64.md); the traffic
 # grows in proportion to the particles, so it is scaled to the workload.
-TRAFFIC_B_PER_PARTICLE = {"fp64": 99.6, "fp32": 50.3}
+TRAFFIC_B_PER_PARTICLE = {"fp64": 98.6, "fp32": 48.7}
 UNIT = "particle-steps/s"
 
 
