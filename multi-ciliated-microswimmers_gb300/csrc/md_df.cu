@@ -363,6 +363,9 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     // consecutive slots, completing on the mbarrier; waited for before the
     // halo springs
     if (hn > 0) {
+      // the other tiles wrote the buffer through the generic proxy; order
+      // those writes (acquired at the barrier) before this thread's bulk reads
+      if (tid < nrun) asm volatile("fence.proxy.async.global;" ::: "memory");
       for (int r = tid; r < nrun; r += nthr) {
         const int4 run = s_runs[r];
         bulk_load(st + 2 * (T + run.y), m.q[b] + 2 * (size_t)run.x, 32u * (uint32_t)run.z, hbar);

@@ -159,8 +159,10 @@ MPCD_HD int cnt_beads(uint32_t w) { return (int)(w >> 16); }
 // Grid-wide barrier for cooperative launches: a monotonic arrival counter,
 // reset to zero by the host before every launch.  The k-th barrier of a
 // launch (k = 1, 2, ...) waits until the counter reaches k * nblocks.  Each
-// CTA publishes its writes with a gpu-scope fence and one relaxed atomic add,
-// then polls with acquire loads.  Every wait is bounded: on timeout the CTA
+// CTA publishes its writes with one gpu-scope release add (cumulative over
+// the CTA's writes, which __syncthreads made visible to the adding thread),
+// then polls with acquire loads, back to back (the wait is the critical path
+// of every MD substep).  Every wait is bounded: on timeout the CTA
 // sets kErrBarrier in *err and returns false, and the caller leaves the kernel
 // (the other CTAs then time out as well, so the launch always ends).
 struct GridBarrier {
@@ -179,16 +181,14 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned target,
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = 1;
-    __threadfence();
-    atomicAdd(b.count, 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(b.count) : "memory");
     unsigned long long spins = 0;
     while (ld_acquire(b.count) < target) {
-      if (++spins > (1ull << 22)) {  // bounded wait (a few seconds)
+      if (++spins > (1ull << 23)) {  // bounded wait (each poll is an L2 round trip: a few seconds)
         atomicOr(err, kErrBarrier);
         ok = 0;
         break;
       }
-      __nanosleep(20);
     }
   }
   __syncthreads();
