@@ -14,6 +14,8 @@
 // by its own seed, step counter and box-local cell index, exactly as for the
 // same box run alone (engine.cu), so its trajectory does not depend on the
 // company it keeps.
+#include <cstdlib>
+
 #include "batch_internal.h"
 #include "fluid_device.cuh"
 #include "tma.cuh"
@@ -207,6 +209,7 @@ __device__ __forceinline__ void fluid_particle(const FluidPage& P, const float4 
 // latency of the chain particle -> cell -> map).
 constexpr int kFluidBatchB = 2;
 
+template <int U>
 __global__ void __launch_bounds__(512, 2) k_batch_fluid_step(BatchTables t, BatchFluid f, BatchCells c) {
   for (long pg = blockIdx.x; pg < t.npart_pages; pg += gridDim.x) {
     const int r = t.part_page_rep[pg];
@@ -218,7 +221,6 @@ __global__ void __launch_bounds__(512, 2) k_batch_fluid_step(BatchTables t, Batc
     const FluidPage P = fluid_page(t, c, r);
     float ke_after = 0.0f;
     unsigned bad = 0;
-    constexpr int U = kFluidBatchB;
     const int np = (int)(i1 - i0);  // page-local indices: 32-bit
     float4* const pos = f.pos + i0;
     float4* const vel = f.vel + i0;
@@ -525,7 +527,15 @@ int launch_batch_fluid_step(const BatchTables& t, BatchFluid f, BatchCells c, in
     return 1;
   }
   if (blocks <= 0) blocks = page_grid(t.npart_pages);
-  k_batch_fluid_step<<<blocks, threads, 0, s>>>(t, f, c);
+  // particles per thread and round: kFluidBatchB unless MPCD_FLUID_BATCH is 1
+  static const int batch = [] {
+    const char* e = std::getenv("MPCD_FLUID_BATCH");
+    return e && std::atoi(e) == 1 ? 1 : kFluidBatchB;
+  }();
+  if (batch == 1)
+    k_batch_fluid_step<1><<<blocks, threads, 0, s>>>(t, f, c);
+  else
+    k_batch_fluid_step<kFluidBatchB><<<blocks, threads, 0, s>>>(t, f, c);
   return 1;
 }
 
