@@ -293,7 +293,11 @@ int build_md(mpcd_engine* h) {
   // MPCD_MD_NO_CLUSTER=1 keeps split arithmetic on the cooperative grid layout
   const char* no_cl = std::getenv("MPCD_MD_NO_CLUSTER");
   const bool allow_cluster = !(no_cl && std::atoi(no_cl) != 0);
-  const std::string why = plan_md(in, MDForce{}, allow_cluster, false, h->p.precision == MPCD_FP32 ? 1 : 0, pl);
+  // MPCD_MD_MIN_TILE: narrowest grid-layout tile (tests of the wide layouts on small bead sets)
+  const char* mt = std::getenv("MPCD_MD_MIN_TILE");
+  const int min_tile = mt ? std::max(0, std::min(256, std::atoi(mt))) : 0;
+  const std::string why =
+      plan_md(in, MDForce{}, allow_cluster, false, h->p.precision == MPCD_FP32 ? 1 : 0, pl, min_tile);
   if (!why.empty()) return fail(h, MPCD_EINVAL, why);
   if (pl.hstart.size() != (size_t)pl.ntiles + 1 || pl.halo.size() != (size_t)pl.hstart.back())
     return fail(h, MPCD_EINVAL, "MD plan: halo lists inconsistent with their offsets");

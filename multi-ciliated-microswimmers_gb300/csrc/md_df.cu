@@ -587,17 +587,20 @@ template <typename Bin>
 const void* df_kernel(const MDState& m, int lanes) {
   const bool fl = m.df == 2;
   if (lanes == 8) return fl ? (const void*)k_md_df<8, true, Bin> : (const void*)k_md_df<8, false, Bin>;
+  if (lanes == 2) return fl ? (const void*)k_md_df<2, true, Bin> : (const void*)k_md_df<2, false, Bin>;
   return fl ? (const void*)k_md_df<4, true, Bin> : (const void*)k_md_df<4, false, Bin>;
 }
 
 }  // namespace
 
-// eight lanes per slot when the tile allows it (more warps in flight), else four
+// eight lanes per slot when the tile allows it (more warps in flight), else
+// four, and two for the widest tiles (at most 512 threads per CTA)
 int md_df_lanes(int tile) {
   static const int forced = [] {
     const char* env = std::getenv("MPCD_MD_DF_LANES");  // 4 or 8
     return env ? std::atoi(env) : 0;
   }();
+  if (tile > 128) return 2;
   if (forced == 4 || (forced == 8 && tile <= 64)) return forced;
   return tile <= 64 ? 8 : 4;
 }

@@ -16,7 +16,7 @@
 namespace mpcd {
 
 std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster, bool no_react, int grid_f32cells,
-                    MDPlan& out) {
+                    MDPlan& out, int min_tile) {
   // springs per helper slot: the longest serial spring chain of any thread.
   // Odd, so that the helper slots' spring lists start in different
   // shared-memory banks.
@@ -231,7 +231,7 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
       // list (helper slots) instead of reactions
       bool any_hub = false;
       for (long b = 0; b < nb && !any_hub; ++b) any_hub = hub[b] != 0;
-      if (any_hub && !no_react) return plan_md(in, force, allow_cluster, true, grid_f32cells, out);
+      if (any_hub && !no_react) return plan_md(in, force, allow_cluster, true, grid_f32cells, out, min_tile);
       return "the MD bead set needs more than 16 tiles of the fixed layout";
     }
     tile = force.tile;
@@ -264,9 +264,10 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     std::fill(react.begin(), react.end(), 0);
     std::fill(dropped.begin(), dropped.end(), 0);
     maxw = widest();
-    tile = std::max(32, ((maxw + 15) / 16) * 16);
+    // the narrowest tile that holds the widest cilium (more CTAs, more lanes
+    // per slot), unless a wider one is asked for: the grid must be co-resident
+    tile = std::max(std::max(32, min_tile), ((maxw + 15) / 16) * 16);
     if (tile > 256) return "an MD group needs more than 256 slots";  // four threads per slot
-    if (tile > 128) out.df = 0;  // the double-float kernel runs at most 512 threads per CTA
     pack(tile);
   }
   // a hub and all its partners must share one tile, one hub per tile
@@ -282,7 +283,7 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     }
     for (long i = 0; i < nsp && !bad; ++i)
       if (react[i] && slot_of[in.sp_t[i]] / tile != slot_of[in.sp_o[i]] / tile) bad = true;
-    if (bad) return plan_md(in, force, allow_cluster, true, grid_f32cells, out);
+    if (bad) return plan_md(in, force, allow_cluster, true, grid_f32cells, out, min_tile);
   }
   out.tile = tile;
   out.ntiles = (int)fill.size();
@@ -517,11 +518,16 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     }
     if (!md_cluster_feasible(probe)) {
       if (forced) return "the fixed cluster layout does not fit on the device";
-      return plan_md(in, force, false, no_react, grid_f32cells, out);  // grid layout instead
+      return plan_md(in, force, false, no_react, grid_f32cells, out, min_tile);  // grid layout instead
     }
   } else {
     const int cap = md_max_coresident_blocks(probe, grid_f32cells);
-    if (out.ntiles > cap) return "MD tiles exceed the co-resident CTA limit of the device";
+    if (out.ntiles > cap) {
+      // a large bead set: wider tiles (fewer CTAs; the double-float kernel
+      // then runs four, then two lanes per slot)
+      if (tile < 256) return plan_md(in, force, allow_cluster, no_react, grid_f32cells, out, tile < 128 ? 128 : 256);
+      return "MD tiles exceed the co-resident CTA limit of the device";
+    }
   }
   // cilia
   out.cd.assign(ncil, CiliumDev{});

@@ -61,7 +61,9 @@ struct MDPlan {
 
 // Plans the layout.  Returns an empty string on success, else the reason.
 // `grid_f32cells` selects the co-resident limit checked for the grid layout.
+// `min_tile`: the narrowest grid-layout tile to consider (0: as narrow as the
+// widest cilium allows); a grid that is not co-resident is re-planned wider.
 std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster, bool no_react, int grid_f32cells,
-                    MDPlan& out);
+                    MDPlan& out, int min_tile = 0);
 
 }  // namespace mpcd

@@ -88,21 +88,29 @@ def test_swimmer_matches_reference_golden(case, arith):
     assert abs(e.time - g[f"step{int(steps)}_meta"][0]) < 1e-12
 
 
-@pytest.mark.parametrize("arith,bulk", [(cg.MD_DF, False), (cg.MD_DF, True), (cg.MD_F64, False)])
-def test_multi_tile_swimmer_matches_oracle(arith, bulk, monkeypatch):
+@pytest.mark.parametrize("arith,bulk,min_tile", [(cg.MD_DF, False, 0), (cg.MD_DF, True, 0), (cg.MD_F64, False, 0),
+                                                  (cg.MD_DF, False, 128), (cg.MD_DF, False, 256)])
+def test_multi_tile_swimmer_matches_oracle(arith, bulk, min_tile, monkeypatch):
     """A Clami whose cilia fill many MD tiles (halos between tiles, a sphere
     centre with helper slots) against the C oracle, injected randomness, 6 MPC
     steps of 50 substeps.  bulk: the double-float kernel copies halo runs of
     two or more slots by bulk asynchronous copies (TMA) instead of per-entry
-    cp.async."""
+    cp.async.  min_tile: the wide tiles that large swimmers get when the
+    narrow grid would not be co-resident (128 slots at four lanes per slot,
+    256 at two)."""
     if bulk:
         monkeypatch.setenv("MPCD_MD_LONG_RUN", "2")
+    if min_tile:
+        monkeypatch.setenv("MPCD_MD_MIN_TILE", str(min_tile))
     cfg = simcfg.swimmer_config(16, radius=4.0, n_cilia=24, rodlength=10, seed=3, ststep=0.002)
     o = build_from_cfg(cfg, seed=5, ststep=0.002)
     s = cg.Sim(simcfg.dumps(cfg), precision=cg.MPCD_FP64, ststep=0.002, create_fluid=False, md_arith=arith)
     e = s.engine
     lay = e.md_layout()
-    assert lay["arith"] == arith and lay["cluster"] == 0 and lay["ntiles"] > 4 and lay["hmax"] > 0
+    assert lay["arith"] == arith and lay["cluster"] == 0 and lay["hmax"] > 0
+    assert lay["ntiles"] > (4 if not min_tile else 2) and lay["tile"] >= min_tile
+    if min_tile:
+        assert lay["lanes"] == (4 if min_tile == 128 else 2)
     p0, v0 = o.fluid()
     e.set_fluid(p0, v0)
     e.shift = o.shift
@@ -119,7 +127,7 @@ def test_multi_tile_swimmer_matches_oracle(arith, bulk, monkeypatch):
     po, vo = o.fluid()
     errs = dict(bead_pos=np.abs(bp - op).max(), bead_vel=np.abs(bv - ov).max(),
                 fluid_pos=np.abs(periodic_diff(p, po, L)).max(), fluid_vel=np.abs(v - vo).max())
-    print("multi-tile", arith, bulk, errs)
+    print("multi-tile", arith, bulk, min_tile, errs)
     assert errs["bead_pos"] < POS_TOL and errs["bead_vel"] < 1e-8, errs
     assert errs["fluid_pos"] < POS_TOL and errs["fluid_vel"] < VEL_TOL, errs
     s.close()
