@@ -20,6 +20,9 @@ batched: the 64-replica mixed-size ensemble (box edges 16..48, 0-64 cilia)
          advanced together by the replica batch (float32 split, CUDA graphs,
          autotuned launch configuration), 1000 MPC steps timed, beside the
          same replicas run one at a time through the single-box engine.
+large_swimmer: the 128^3 box with a radius-16 Clami of 400 cilia (3 x 20
+         beads) in float32 split precision, beside the float64 plain path on
+         the same seed (observable differences after the same steps).
 
 --impl reference runs that CPU restatement alone (the reference's own
 sources are not available where this runs) and prints its line.
@@ -347,6 +350,45 @@ def run_serving(args, n=60, steps_range=(100, 2000), load=0.8, seed=21):
     }
 
 
+# ------------------------------------------------------- large swimmer (c2) --
+
+def run_large(args, steps=200, seed=2024):
+    """swimmer128 (128^3 cells x 10 fluid, Clami R=16 with 400 cilia of 3x20
+    beads) in float32 split precision, timed, beside the float64 plain path
+    on the same seed (same initial state and random draws): the difference of
+    the observables after the same steps states the float32 error (the float64
+    path is the one pinned to the oracle)."""
+    import cilia_gpu as cg
+
+    cfg = workload_cfg("swimmer128", seed=seed)
+    text = simcfg.dumps(cfg)
+    res = {}
+    for prec, key in ((cg.MPCD_FP32, "fp32"), (cg.MPCD_FP64, "fp64")):
+        sim = cg.Sim(text, precision=prec, seed=seed, device=args.device)
+        eng = sim.engine
+        nf = int(cfg["sizex"]) ** 3 * 10
+        nb = sim.nbeads
+        eng.run(3)
+        ms = eng.timed_run(steps, flush_l2=True)
+        obs = eng.observables()
+        bp, bv = sim.beads()
+        res[key] = dict(value=(nf + nb) * steps / (float(ms.sum()) / 1e3), ms_per_step=float(ms.mean()), kT=obs["kT"],
+                        fluid_T=obs["fluid_T"], x_cm=bp.mean(axis=0), v_cm=bv.mean(axis=0), nf=nf, nb=nb,
+                        md_lanes=eng.md_layout()["lanes"], md_tile=eng.md_layout()["tile"])
+        sim.close()
+    a, b = res["fp32"], res["fp64"]
+    return {
+        "workload": describe("swimmer128", a["nf"], a["nb"], "float32 split") + f"; {steps} timed MPC steps",
+        "metric": METRIC, "unit": UNIT, "value": a["value"], "ms_per_step": a["ms_per_step"],
+        "plain_fp64": {"value": b["value"], "ms_per_step": b["ms_per_step"]},
+        "md_layout": {"lanes": a["md_lanes"], "tile": a["md_tile"]},
+        "fp32_vs_fp64_same_seed": {"steps": steps + 3, "kT": [a["kT"], b["kT"]], "fluid_T": [a["fluid_T"], b["fluid_T"]],
+                                   "swimmer_x_cm_diff": float(np.linalg.norm(a["x_cm"] - b["x_cm"])),
+                                   "swimmer_v_cm": [float(np.linalg.norm(a["v_cm"])), float(np.linalg.norm(b["v_cm"]))],
+                                   "swimmer_v_cm_diff": float(np.linalg.norm(a["v_cm"] - b["v_cm"]))},
+    }
+
+
 # ------------------------------------------------------------------ CPU arm --
 
 def run_cpu(args, budget_s=None, threads=None):
@@ -392,6 +434,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-only", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-large", action="store_true", help="skip the 128^3 swimmer line")
     ap.add_argument("--serving-only", action="store_true")
     ap.add_argument("--serving-full", action="store_true", help="500 requests, steps 500..20000")
     args = ap.parse_args()
@@ -498,6 +541,8 @@ def main():
         line["batched"] = run_ensemble(args)
     if not args.no_serving and args.gpus == 1:
         line["serving"] = run_serving(args)
+    if not args.no_large and args.gpus == 1 and args.workload == "swimmer64":
+        line["large_swimmer"] = run_large(args)
     if not args.no_cpu:
         c = run_cpu(args)
         line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",
