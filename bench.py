@@ -54,6 +54,9 @@ METRIC = "MPCD particle-steps/s"
 # one ncu capture on swimmer64 (profiles/fluid_step_swimmer64.md); the traffic
 # grows in proportion to the particles, so it is scaled to the workload.
 TRAFFIC_B_PER_PARTICLE = {"fp64": 98.6, "fp32": 48.7}
+# FP64 pipe of the same captures (sm__pipe_fp64_cycles_active, of peak, active):
+# the float64 fluid step is bound by it, not by HBM
+FP64_PIPE_ACTIVE = {"fp64": 0.819, "fp32": 0.014}
 UNIT = "particle-steps/s"
 
 
@@ -517,6 +520,9 @@ def main():
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, swimmer64 capture, "
                                        "scaled by particles", "peak_kind": peak_kind,
                      "kernel": "fluid_step (collide + stream + bin)",
+                     "fp64_pipe_active": FP64_PIPE_ACTIVE[args.precision],
+                     "fp64_pipe_source": "ncu sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active, swimmer64 "
+                                         "capture (20 float64 operations per particle: the kernel's bound)",
                      "bytes_per_particle_step": bpp, "avg_launch_ms": avg_fluid_ms},
         "kernels_ms_per_step": {k: v[0] / max(g["prof_steps"], 1) for k, v in g["kernels"].items()},
         "gpu_launches": g["launches"],

@@ -225,6 +225,36 @@ def test_non_finite_input_rejected():
         e.set_fluid(pos, vel)
 
 
+@pytest.mark.parametrize("precision", [cg.MPCD_FP64, cg.MPCD_FP32])
+def test_fluid_upload_download_round_trip(precision):
+    """set_fluid wraps unwrapped positions into the box and splits them into
+    the device layout on the device; fluid() returns them in the caller's
+    order.  A rejected upload leaves the resident fluid as it was."""
+    L = (6, 5, 7)
+    rng = np.random.default_rng(3)
+    n = 5000
+    pos = rng.uniform(-20.0, 30.0, (n, 3))
+    vel = rng.normal(size=(n, 3))
+    e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=precision)
+    e.set_fluid(pos, vel)
+    p, v = e.fluid()
+    want = np.mod(pos, np.array(L, dtype=float))
+    f64 = precision == cg.MPCD_FP64
+    # float64: exact up to the wrap's rounding; float32: offsets in [0, 1) as float
+    assert np.abs(periodic_diff(p, want, L)).max() < (1e-12 if f64 else 1e-7)
+    assert np.all((p >= 0.0) & (p < np.array(L, dtype=float)))
+    if f64:
+        assert np.array_equal(v, vel)
+    else:
+        assert np.array_equal(v, vel.astype(np.float32).astype(np.float64))
+    bad = pos.copy()
+    bad[7, 2] = np.inf
+    with pytest.raises(cg.MpcdError, match="non-finite"):
+        e.set_fluid(bad, vel)
+    p2, v2 = e.fluid()
+    assert np.array_equal(p2, p) and np.array_equal(v2, v)
+
+
 def test_unstable_md_step_reports_error_without_fault():
     """A too-large MD step lets the beads diverge; the kernels report it."""
     import simcfg
