@@ -50,6 +50,8 @@ struct mpcd_engine {
   double* d_diss = nullptr;
   double* d_obs = nullptr;
   double* h_obs = nullptr;  // pinned: observables, dissipated energy and error bits of one read-back
+  double* d_obs_part = nullptr;     // per-block partials of the cell-sum observables
+  unsigned* d_obs_count = nullptr;  // blocks finished (reset by the last one)
   unsigned* d_bar = nullptr;
 
   FluidF64 f64, f64tmp;
@@ -612,6 +614,9 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
   if ((e = dalloc(&h->d_diss, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs, 16)) != cudaSuccess) return bail(e, "alloc");
   if ((e = cudaMallocHost((void**)&h->h_obs, 16 * sizeof(double))) != cudaSuccess) return bail(e, "alloc");
+  if ((e = dalloc(&h->d_obs_part, 7 * (size_t)kObsBlocks)) != cudaSuccess) return bail(e, "alloc");
+  if ((e = dalloc(&h->d_obs_count, 1)) != cudaSuccess) return bail(e, "alloc");
+  if ((e = cudaMemset(h->d_obs_count, 0, sizeof(unsigned))) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_bar, 2)) != cudaSuccess) return bail(e, "alloc");
   cudaMemset(h->d_err, 0, sizeof(unsigned));
   cudaMemset(h->d_diss, 0, sizeof(double));
@@ -668,6 +673,8 @@ int mpcd_destroy(mpcd_engine* h) {
   cudaFree(h->d_diss);
   cudaFree(h->d_obs);
   cudaFreeHost(h->h_obs);
+  cudaFree(h->d_obs_part);
+  cudaFree(h->d_obs_count);
   cudaFree(h->d_bar);
   cudaFree(h->flush_buf);
   for (auto& m : h->marks) {
@@ -1051,20 +1058,29 @@ int mpcd_observables(mpcd_engine* h, mpcd_obs* out) {
     int rc = build_md(h);
     if (rc) return rc;
   }
-  CK(cudaMemsetAsync(h->d_obs, 0, 8 * sizeof(double), h->stream));
-  if (h->p.precision == MPCD_FP64)
-    h->launches += launch_observables_f64(h->f64, h->md, h->p.bead_mass, h->d_obs, h->stream);
-  else
-    h->launches += launch_observables_f32(h->f32, h->md, h->p.bead_mass, h->d_obs, h->stream);
-  // one read-back into pinned memory: the sums, the dissipated energy, the error bits
-  double* o = h->h_obs;
-  CK(cudaMemcpyAsync(o, h->d_obs, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaMemcpyAsync(o + 8, h->d_diss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaMemcpyAsync(o + 9, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
+  double* o = h->h_obs;  // pinned: the sums, the dissipated energy, the error bits
+  unsigned err_bits = 0;
+  if (h->p.precision == MPCD_FP64 && h->prepared) {
+    // the cell sums of the last binning (the state has not changed since: every
+    // setter clears `prepared`) hold the totals; one kernel, one read-back
+    h->launches += launch_observables_cells_f64(h->c64, h->md, h->p.bead_mass, h->d_diss, h->d_err, h->d_obs_part,
+                                                h->d_obs_count, h->d_obs, h->stream);
+    CK(cudaMemcpyAsync(o, h->d_obs, 10 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    err_bits = (unsigned)o[9];
+  } else {
+    CK(cudaMemsetAsync(h->d_obs, 0, 8 * sizeof(double), h->stream));
+    if (h->p.precision == MPCD_FP64)
+      h->launches += launch_observables_f64(h->f64, h->md, h->p.bead_mass, h->d_obs, h->stream);
+    else
+      h->launches += launch_observables_f32(h->f32, h->md, h->p.bead_mass, h->d_obs, h->stream);
+    CK(cudaMemcpyAsync(o, h->d_obs, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(o + 8, h->d_diss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(o + 9, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    std::memcpy(&err_bits, o + 9, sizeof err_bits);
+  }
   const double diss = o[8];
-  unsigned err_bits;
-  std::memcpy(&err_bits, o + 9, sizeof err_bits);
   const double M = o[5] > 0 ? o[5] : 1.0, N = o[4] > 0 ? o[4] : 1.0;
   out->momentum[0] = o[0] / M;
   out->momentum[1] = o[1] / M;

@@ -191,6 +191,11 @@ int launch_load_fluid_f32(long n, const double* pos, const double* vel, const Bo
                           cudaStream_t s);
 int launch_store_fluid_f64(const FluidF64& f, double* pos, double* vel, unsigned* bad, cudaStream_t s);
 int launch_store_fluid_f32(const FluidF32& f, double* pos, double* vel, unsigned* bad, cudaStream_t s);
+// observables from the binned cell sums (float64 path; valid while the sums
+// are those of the last binning): out[10], part[7 * kObsBlocks], counter zeroed once
+constexpr int kObsBlocks = 512;
+int launch_observables_cells_f64(const CellsF64& c, const MDState& m, double bead_mass, const double* diss,
+                                 const unsigned* err, double* part, unsigned* counter, double* out, cudaStream_t s);
 int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s, int per_sm = 4);
 int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s);
 int launch_bead_collide_f32(const MDState& m, const CellsF32& c, const StepArgs& a, cudaStream_t s);

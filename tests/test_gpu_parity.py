@@ -255,6 +255,27 @@ def test_fluid_upload_download_round_trip(precision):
     assert np.array_equal(p2, p) and np.array_equal(v2, v)
 
 
+def test_observables_from_cell_sums_match_particle_sums():
+    """After a step the float64 engine reads its observables from the cell sums
+    binned at the end of the step (fluid and moving beads, m v and m v^2 once
+    each); they match the sums over the particles and beads themselves, which
+    the engine takes when a setter has invalidated the binning."""
+    import simcfg
+
+    cfg = simcfg.swimmer_config(16, radius=4.0, n_cilia=12, rodlength=8, seed=3, ststep=0.002)
+    s = cg.Sim(simcfg.dumps(cfg), precision=cg.MPCD_FP64, ststep=0.002, seed=4)
+    e = s.engine
+    e.run(3)
+    a = e.observables()
+    e.shift = e.shift  # the same shift: the binning is invalidated, the state unchanged
+    b = e.observables()
+    for k in ("kT", "fluid_T", "n", "mass", "diss_energy", "energy_fluid"):
+        assert a[k] == pytest.approx(b[k], rel=1e-12, abs=1e-12), k
+    assert np.abs(a["momentum"] - b["momentum"]).max() < 1e-12
+    assert 16 ** 3 * 10 < a["n"] <= 16 ** 3 * 10 + s.nbeads
+    s.close()
+
+
 def test_unstable_md_step_reports_error_without_fault():
     """A too-large MD step lets the beads diverge; the kernels report it."""
     import simcfg
