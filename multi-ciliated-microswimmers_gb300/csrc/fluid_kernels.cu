@@ -147,31 +147,33 @@ __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, c
     rx = (double)(st * cp);
     ry = (double)(st * sp);
     rz = (double)ct;
-    const double nrm = rsqrt(rx * rx + ry * ry + rz * rz);
-    rx *= nrm;
-    ry *= nrm;
-    rz *= nrm;
+    // |r|^2 = 1 + e with |e| of a few float roundings: two Newton steps for
+    // 1/sqrt from 1 (y1 = 1.5 - n2/2 is within 3e^2/8, y2 within float64
+    // rounding) on the FMA chain instead of the general reciprocal square root
+    const double n2 = fma(rx, rx, fma(ry, ry, rz * rz));
+    const double y1 = fma(-0.5, n2, 1.5);
+    const double y2 = y1 * fma(-0.5, (n2 * y1) * y1, 1.5);
+    rx *= y2;
+    ry *= y2;
+    rz *= y2;
   }
   const double ca = kCosAlpha, sa = kSinAlpha, oc = 1.0 - kCosAlpha;
-  // rotation about (rx, ry, rz) by alpha, entries as src/libcilia/mpcd.cpp:285-293
-  const double R00 = rx * rx + (1.0 - rx * rx) * ca;
-  const double R01 = rx * ry * oc - rz * sa;
-  const double R02 = rx * rz * oc + ry * sa;
-  const double R10 = rx * ry * oc + rz * sa;
-  const double R11 = ry * ry + (1.0 - ry * ry) * ca;
-  const double R12 = ry * rz * oc - rx * sa;
-  const double R20 = rx * rz * oc - ry * sa;
-  const double R21 = ry * rz * oc + rx * sa;
-  const double R22 = rz * rz + (1.0 - rz * rz) * ca;
-  A[0] = R00 * sc;
-  A[1] = R01 * sc;
-  A[2] = R02 * sc;
-  A[3] = R10 * sc;
-  A[4] = R11 * sc;
-  A[5] = R12 * sc;
-  A[6] = R20 * sc;
-  A[7] = R21 * sc;
-  A[8] = R22 * sc;
+  // A = sc R, R the rotation about (rx, ry, rz) by alpha with the entries of
+  // src/libcilia/mpcd.cpp:285-293 (R_ii = r_i^2 + (1 - r_i^2) ca,
+  // R_ij = r_i r_j (1 - ca) -+ r_k sa), the factor sc folded in:
+  // A_ii = (sc oc r_i) r_i + sc ca, A_ij = (sc oc r_i) r_j -+ sc sa r_k
+  const double sco = sc * oc, scc = sc * ca, scs = sc * sa;
+  const double tx = sco * rx, ty = sco * ry, tz = sco * rz;
+  const double qx = scs * rx, qy = scs * ry, qz = scs * rz;
+  A[0] = fma(tx, rx, scc);
+  A[1] = fma(tx, ry, -qz);
+  A[2] = fma(tx, rz, qy);
+  A[3] = fma(tx, ry, qz);
+  A[4] = fma(ty, ry, scc);
+  A[5] = fma(ty, rz, -qx);
+  A[6] = fma(tx, rz, -qy);
+  A[7] = fma(ty, rz, qx);
+  A[8] = fma(tz, rz, scc);
   b[0] = ux - (A[0] * ux + A[1] * uy + A[2] * uz);
   b[1] = uy - (A[3] * ux + A[4] * uy + A[5] * uz);
   b[2] = uz - (A[6] * ux + A[7] * uy + A[8] * uz);
