@@ -127,6 +127,7 @@ MD_ARITH_NAMES = {
     0: "float64",
     1: "split (float springs on hi/lo position pairs)",
     2: "double-float (pairs of floats, 48-bit significand; integer cell + offset coordinates)",
+    3: "float springs on double-float positions (split arithmetic; integer cell + offset coordinates)",
 }
 
 
@@ -375,16 +376,17 @@ def run_large(args, steps=200, seed=2024):
         ms = eng.timed_run(steps, flush_l2=True)
         obs = eng.observables()
         bp, bv = sim.beads()
+        lay = eng.md_layout()
         res[key] = dict(value=(nf + nb) * steps / (float(ms.sum()) / 1e3), ms_per_step=float(ms.mean()), kT=obs["kT"],
                         fluid_T=obs["fluid_T"], x_cm=bp.mean(axis=0), v_cm=bv.mean(axis=0), nf=nf, nb=nb,
-                        md_lanes=eng.md_layout()["lanes"], md_tile=eng.md_layout()["tile"])
+                        md_lanes=lay["lanes"], md_tile=lay["tile"], md_arith=MD_ARITH_NAMES[lay["arith"]])
         sim.close()
     a, b = res["fp32"], res["fp64"]
     return {
         "workload": describe("swimmer128", a["nf"], a["nb"], "float32 split") + f"; {steps} timed MPC steps",
         "metric": METRIC, "unit": UNIT, "value": a["value"], "ms_per_step": a["ms_per_step"],
         "plain_fp64": {"value": b["value"], "ms_per_step": b["ms_per_step"]},
-        "md_layout": {"lanes": a["md_lanes"], "tile": a["md_tile"]},
+        "md_layout": {"lanes": a["md_lanes"], "tile": a["md_tile"], "arith": a["md_arith"]},
         "fp32_vs_fp64_same_seed": {"steps": steps + 3, "kT": [a["kT"], b["kT"]], "fluid_T": [a["fluid_T"], b["fluid_T"]],
                                    "swimmer_x_cm_diff": float(np.linalg.norm(a["x_cm"] - b["x_cm"])),
                                    "swimmer_v_cm": [float(np.linalg.norm(a["v_cm"])), float(np.linalg.norm(b["v_cm"]))],

@@ -38,8 +38,10 @@ typedef struct {
   double gravity;          /* body force along x */
   double bead_mass;        /* collision mass of beads (0 = reference value 5) */
   int sort_interval;       /* 0 = default */
-  int md_arith;            /* MD arithmetic: 0 auto, else mpcd_params.md_split + 1 (1 float64,
-                              2 split, 3 double-float) */
+  int md_arith;            /* MD arithmetic: 0 auto (double-float for float64, float springs on
+                              double-float positions for float32), else mpcd_params.md_split + 1
+                              (1 float64, 2 split, 3 double-float, 4 float springs on the
+                              double-float layout) */
 } cilia_options;
 
 /* cfg is a file path, or libconfig text when is_text != 0 */

@@ -35,16 +35,16 @@ def test_fp32_fluid_tracks_reference_golden():
     assert np.mean(dv < 2e-4) > 0.995
 
 
-@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_SPLIT, cg.MD_FLOAT])
+@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_DF, cg.MD_SPLIT, cg.MD_FLOAT])
 def test_fp32_swimmer_tracks_reference_golden(arith):
-    """MD in double-float (the default), in split arithmetic on one
-    thread-block cluster (the replica batch's MD), and in split arithmetic on
-    the double-float kernel's grid layout."""
+    """MD in split arithmetic on the double-float kernel's grid layout (the
+    default of the float32 path), in double-float, and in split arithmetic on
+    one thread-block cluster (the replica batch's MD)."""
     g = golden("clami10")
     text = open(f"{GOLDEN}/cases/clami10.cfg").read()
     s = cg.Sim(text, precision=cg.MPCD_FP32, ststep=0.002, create_fluid=False, md_arith=arith)
     e = s.engine
-    assert e.md_layout()["arith"] == (cg.MD_DF if arith == cg.MD_AUTO else arith)
+    assert e.md_layout()["arith"] == (cg.MD_FLOAT if arith == cg.MD_AUTO else arith)
     e.set_fluid(g["step0_fluid_pos"], g["step0_fluid_vel"])
     e.shift = g["shift_0"]
     for k in range(1, 5):
