@@ -53,10 +53,10 @@ METRIC = "MPCD particle-steps/s"
 # DRAM bytes (read + write) per fluid particle of one fluid_step launch, from
 # one ncu capture on swimmer64 (profiles/fluid_step_swimmer64.md); the traffic
 # grows in proportion to the particles, so it is scaled to the workload.
-TRAFFIC_B_PER_PARTICLE = {"fp64": 98.6, "fp32": 48.7}
+TRAFFIC_B_PER_PARTICLE = {"fp64": 98.9, "fp32": 48.7}
 # FP64 pipe of the same captures (sm__pipe_fp64_cycles_active, of peak, active):
 # the float64 fluid step is bound by it, not by HBM
-FP64_PIPE_ACTIVE = {"fp64": 0.819, "fp32": 0.014}
+FP64_PIPE_ACTIVE = {"fp64": 0.824, "fp32": 0.014}
 UNIT = "particle-steps/s"
 
 

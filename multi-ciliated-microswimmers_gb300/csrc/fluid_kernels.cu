@@ -73,8 +73,28 @@ __device__ __forceinline__ int shifted(int i, double o, Thresh t, int L) {
 // pattern larger)
 __device__ __forceinline__ bool off_unit(double o) { return (uint32_t)__double2hiint(o) >= 0x3FF00000u; }
 
-// reduce an offset that left [0,1) back into the cell (rare path)
+// reduce an offset that left [0,1) back into the cell.  A streaming step
+// moves a particle by less than one cell almost always: 1 <= o < 2 and
+// -1 < o < 0 are told apart on the high word and corrected by one exact
+// float64 add (the same result as o - floor(o), without the FP64 floor and
+// compares); the general path takes the rest.
 __device__ __forceinline__ void rewrap(double& o, int& i, int L, unsigned& bad) {
+  const uint32_t hw = (uint32_t)__double2hiint(o);
+  if (hw < 0x3FF00000u) return;  // 0 <= o < 1
+  if (hw < 0x40000000u) {        // 1 <= o < 2: o - 1 is exact
+    o -= 1.0;
+    i = i + 1 == L ? 0 : i + 1;
+    return;
+  }
+  if (hw >= 0x80000000u && hw < 0xBFF00000u) {  // -1 < o < 0 (or -0)
+    o += 1.0;
+    if (__double2hiint(o) == 0x3FF00000 && __double2loint(o) == 0) {
+      o = 0.0;  // rounded up to 1: the particle stays in its cell at offset 0
+      return;
+    }
+    i = i == 0 ? L - 1 : i - 1;
+    return;
+  }
   if (off_unit(o)) {
     if (!(o > -1.0e9 && o < 1.0e9)) {  // non-finite: keep the particle in its cell and report
       o = 0.5;
