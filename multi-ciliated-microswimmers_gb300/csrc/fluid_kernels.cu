@@ -81,18 +81,17 @@ __device__ __forceinline__ bool off_unit(double o) { return (uint32_t)__double2h
 __device__ __forceinline__ void rewrap(double& o, int& i, int L, unsigned& bad) {
   const uint32_t hw = (uint32_t)__double2hiint(o);
   if (hw < 0x3FF00000u) return;  // 0 <= o < 1
-  if (hw < 0x40000000u) {        // 1 <= o < 2: o - 1 is exact
-    o -= 1.0;
-    i = i + 1 == L ? 0 : i + 1;
-    return;
-  }
-  if (hw >= 0x80000000u && hw < 0xBFF00000u) {  // -1 < o < 0 (or -0)
-    o += 1.0;
-    if (__double2hiint(o) == 0x3FF00000 && __double2loint(o) == 0) {
+  const bool up = hw < 0x40000000u;                       // 1 <= o < 2: o - 1 is exact
+  const bool down = hw >= 0x80000000u && hw < 0xBFF00000u;  // -1 < o < 0 (or -0)
+  if (up || down) {
+    o += up ? -1.0 : 1.0;  // one add for either case
+    if (up) {
+      i = i + 1 == L ? 0 : i + 1;
+    } else if (__double2hiint(o) == 0x3FF00000 && __double2loint(o) == 0) {
       o = 0.0;  // rounded up to 1: the particle stays in its cell at offset 0
-      return;
+    } else {
+      i = i == 0 ? L - 1 : i - 1;
     }
-    i = i == 0 ? L - 1 : i - 1;
     return;
   }
   if (off_unit(o)) {
