@@ -991,7 +991,13 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
     CK(cudaStreamWaitEvent(h->smd, h->ev_fork, 0));
   }
   if (md) {
-    {
+    // the double-float grid kernel applies the beads' collision itself (one
+    // launch less on the MD chain); the other MD kernels after the bead kernel
+    const bool folded = !h->md.cluster && h->md.df;
+    if (folded) {
+      ma.collide = 1;
+      ma.diss = h->d_diss;
+    } else {
       ProfScope ps(h, MPCD_K_BEAD, sm);
       h->launches += f64 ? launch_bead_collide_f64(h->md, h->c64, s, sm) : launch_bead_collide_f32(h->md, h->c32, s, sm);
     }

@@ -160,6 +160,10 @@ struct MDStepArgs {
   double a_cur[3], a_next[3];
   double bead_mass;
   unsigned* err;
+  // 1: the MD launch first applies the beads' collision (their cells' maps,
+  // as the separate bead kernel would) and subtracts their m v'^2 from *diss
+  int collide = 0;
+  double* diss = nullptr;
 };
 
 // ------------------------------------------------------------ launchers ---

@@ -142,6 +142,19 @@ __device__ __forceinline__ void cell_map_f32(const float4 s0, const uint32_t w, 
   ldiss += s.w;
 }
 
+// v' = A v + b with the float64 map of one cell (A row-major, then b)
+__device__ __forceinline__ void apply_map_f64(const double* par, double& vx, double& vy, double& vz) {
+  const double2* p = reinterpret_cast<const double2*>(par);
+  const double2 p0 = __ldg(p + 0), p1 = __ldg(p + 1), p2 = __ldg(p + 2);
+  const double2 p3 = __ldg(p + 3), p4 = __ldg(p + 4), p5 = __ldg(p + 5);
+  const double nx = fma(p0.x, vx, fma(p0.y, vy, fma(p1.x, vz, p4.y)));
+  const double ny = fma(p1.y, vx, fma(p2.x, vy, fma(p2.y, vz, p5.x)));
+  const double nz = fma(p3.x, vx, fma(p3.y, vy, fma(p4.x, vz, p5.y)));
+  vx = nx;
+  vy = ny;
+  vz = nz;
+}
+
 // v' = u + sc R (v - u) with the map k = {rx, ry, rz, sc}, u = {ux, uy, uz, 0}
 __device__ __forceinline__ void apply_map_f32(const float4 k, const float4 u, float& vx, float& vy, float& vz) {
   const float ca = (float)kCosAlpha, sa = (float)kSinAlpha, oc = 1.0f - (float)kCosAlpha;

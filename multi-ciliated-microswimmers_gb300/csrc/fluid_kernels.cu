@@ -232,18 +232,6 @@ __global__ void k_cell_params_f64(CellsF64 c, StepArgs a) {
   if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
 }
 
-__device__ __forceinline__ void apply_map_f64(const double* par, double& vx, double& vy, double& vz) {
-  const double2* p = reinterpret_cast<const double2*>(par);
-  const double2 p0 = __ldg(p + 0), p1 = __ldg(p + 1), p2 = __ldg(p + 2);
-  const double2 p3 = __ldg(p + 3), p4 = __ldg(p + 4), p5 = __ldg(p + 5);
-  const double nx = fma(p0.x, vx, fma(p0.y, vy, fma(p1.x, vz, p4.y)));
-  const double ny = fma(p1.y, vx, fma(p2.x, vy, fma(p2.y, vz, p5.x)));
-  const double nz = fma(p3.x, vx, fma(p3.y, vy, fma(p4.x, vz, p5.y)));
-  vx = nx;
-  vy = ny;
-  vz = nz;
-}
-
 // Walls along z (NOSLIP / SLIP, src/libcilia/mpcd.cpp:346-376): the channel is
 // 0 <= z <= Lz - 1; a particle that crossed a wall during the streaming step
 // is reflected.  Returns the (possibly changed) unwrapped z.

@@ -4,6 +4,7 @@
 // shared memory, and the binning of beads into the next collision's cells.
 #pragma once
 #include "engine_internal.h"
+#include "fluid_device.cuh"
 
 namespace mpcd {
 
@@ -147,6 +148,17 @@ struct BinF64 {
   using Cells = CellsF64;
   CellsF64 c;
   const MDStepArgs* a;
+  // a moving bead in the collision (its cell's map, MPCD::next_tstep,
+  // src/libcilia/mpcd.cpp:140-247): the new velocity and its m v'^2, as k_bead_collide_f64
+  __device__ double collide(double x, double y, double z, double& vx, double& vy, double& vz) const {
+    const long cid = unwrapped_cell(a->box, a->a_cur, x, y, z);
+    if (cid < 0) {
+      atomicOr(a->err, kErrCellRange);
+      return 0.0;
+    }
+    apply_map_f64(c.par + 12 * cid, vx, vy, vz);
+    return a->bead_mass * (vx * vx + vy * vy + vz * vz);
+  }
   __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
     const long cid = unwrapped_cell(a->box, a->a_next, x, y, z);
     if (cid < 0) {
@@ -167,6 +179,20 @@ struct BinF32 {
   using Cells = CellsF32;
   CellsF32 c;
   const MDStepArgs* a;
+  // as k_bead_collide_f32: the map applied in float to the rounded velocity
+  __device__ double collide(double x, double y, double z, double& vx, double& vy, double& vz) const {
+    const long cid = unwrapped_cell(a->box, a->a_cur, x, y, z);
+    if (cid < 0) {
+      atomicOr(a->err, kErrCellRange);
+      return 0.0;
+    }
+    float fx = (float)vx, fy = (float)vy, fz = (float)vz;
+    apply_map_f32(c.par + 2 * cid, fx, fy, fz);
+    vx = fx;
+    vy = fy;
+    vz = fz;
+    return a->bead_mass * ((double)fx * fx + (double)fy * fy + (double)fz * fz);
+  }
   __device__ void operator()(double x, double y, double z, double vx, double vy, double vz) const {
     const long cid = unwrapped_cell(a->box, a->a_next, x, y, z);
     if (cid < 0) {

@@ -333,13 +333,21 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
   BeadCoord x{0, {0.f, 0.f}}, y{0, {0.f, 0.f}}, z{0, {0.f, 0.f}};
   dfloat vx{0.f, 0.f}, vy{0.f, 0.f}, vz{0.f, 0.f};
   dfloat fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
+  double ke_coll = 0.0;
   if (oprim) {
-    x = coord_from_double(m.x[0][oslot]);
-    y = coord_from_double(m.y[0][oslot]);
-    z = coord_from_double(m.z[0][oslot]);
-    vx = df_from_double(m.vx[oslot]);
-    vy = df_from_double(m.vy[oslot]);
-    vz = df_from_double(m.vz[oslot]);
+    const double X = m.x[0][oslot], Y = m.y[0][oslot], Z = m.z[0][oslot];
+    double VX = m.vx[oslot], VY = m.vy[oslot], VZ = m.vz[oslot];
+    if (a.collide && omoves) ke_coll = bin.collide(X, Y, Z, VX, VY, VZ);  // the beads' collision, folded in
+    x = coord_from_double(X);
+    y = coord_from_double(Y);
+    z = coord_from_double(Z);
+    vx = df_from_double(VX);
+    vy = df_from_double(VY);
+    vz = df_from_double(VZ);
+  }
+  if (a.collide) {  // the dissipated-energy bookkeeping of the collided beads
+    const double tot = block_sum_f64(ke_coll);
+    if (tid == 0 && tot != 0.0) atomicAdd(a.diss, -tot);
   }
   const unsigned nblocks = gridDim.x;
   unsigned barriers = 0;
