@@ -79,7 +79,6 @@ __device__ __forceinline__ void cell_map_f32(const float4 s0, const uint32_t w, 
                                              const double* inj_axis, float4* par_out, float& ldiss, unsigned& errbits,
                                              bool& gfail, const bool wall_cell = false,
                                              const double* inj_virt = nullptr) {
-  const float ca = (float)kCosAlpha, sa = (float)kSinAlpha, oc = 1.0f - (float)kCosAlpha;
   const int nf = cnt_fluid(w), nb = cnt_beads(w);
   int num = nf + nb;
   float M = (float)nf + (float)nb * mb;
