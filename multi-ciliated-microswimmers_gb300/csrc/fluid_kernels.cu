@@ -112,6 +112,19 @@ __device__ __forceinline__ void rewrap(double& o, int& i, int L, unsigned& bad) 
   }
 }
 
+// 1/n for the particle counts of bead-free cells, rounded once as the IEEE
+// division rounds it (the same bits as 1.0 / n at run time), so that the
+// common cell needs no float64 division on GB300's small FP64 pipe
+struct InvTable {
+  double v[256];
+};
+constexpr InvTable make_inv_table() {
+  InvTable t{};
+  for (int i = 1; i < 256; ++i) t.v[i] = 1.0 / i;
+  return t;
+}
+__device__ const InvTable g_inv_n = make_inv_table();
+
 __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, const StepArgs& a, double* A,
                                               double* b, double& ldiss, unsigned& errbits, bool& gfail) {
   const int nf = cnt_fluid(w), nb = cnt_beads(w);
@@ -134,7 +147,7 @@ __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, c
     M += dm;
     num += dm;
   }
-  const double inv = 1.0 / M;
+  const double inv = (nb == 0 && num < 256) ? __ldg(g_inv_n.v + num) : 1.0 / M;  // M = num without beads
   const double ux = s.x * inv, uy = s.y * inv, uz = s.z * inv;
   const double erel = s.w - (ux * s.x + uy * s.y + uz * s.z);  // K - M u^2
   double sc = 1.0;
