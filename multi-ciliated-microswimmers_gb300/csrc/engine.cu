@@ -42,7 +42,7 @@ struct mpcd_engine {
   // launch shape of the fluid pass beside the MD launch: > 0 persistent with that
   // many CTAs per SM, <= 0 short-lived CTAs of -fluid_per_sm (at least 1)
   // particles per thread
-  int fluid_per_sm = -2;
+  int fluid_per_sm = -1;
   std::string error;
   long long launches = 0;
 
@@ -1013,11 +1013,11 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
                          : launch_md_f32cells(h->md, h->c32, ma, sm, &coop);
   }
   {
-    // beside the MD launch the fluid pass runs as many short-lived CTAs (two
-    // particles per thread): as they retire, the higher-priority MD CTAs take
-    // their place, and the fluid CTAs fill what the MD leaves of every SM
-    // (swimmer64 float64: 0.366 ms per step against 0.455 with a persistent
-    // grid of 3 CTAs per SM and 0.480 with the two run one after the other)
+    // beside the MD launch the fluid pass runs as many short-lived CTAs (one
+    // round of particles per thread): as they retire, the higher-priority MD
+    // CTAs take their place, and the fluid CTAs fill what the MD leaves of
+    // every SM (swimmer64 float64: 0.336 ms per step against 0.405 with a
+    // persistent grid of 3 CTAs per SM)
     ProfScope ps(h, MPCD_K_FLUID);
     const int per_sm = fork ? h->fluid_per_sm : 4;
     h->launches += f64 ? launch_fluid_step_f64(h->f64, h->c64, s, h->stream, per_sm)
