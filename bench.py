@@ -54,6 +54,8 @@ METRIC = "MPCD particle-steps/s"
 # one ncu capture on swimmer64 (profiles/fluid_step_swimmer64.md); the traffic
 # grows in proportion to the particles, so it is scaled to the workload.
 TRAFFIC_B_PER_PARTICLE = {"fp64": 98.9, "fp32": 48.7}
+# the replica batch's fluid pass on the 64-replica ensemble (profiles/batch_fluid_ensemble64.md)
+BATCH_TRAFFIC_B_PER_PARTICLE = 69.7
 # FP64 pipe of the same captures (sm__pipe_fp64_cycles_active, of peak, active):
 # the float64 fluid step is bound by it, not by HBM
 FP64_PIPE_ACTIVE = {"fp64": 0.824, "fp32": 0.014}
@@ -273,6 +275,10 @@ def run_ensemble(args, n=64, steps=1000):
                              "how": "each replica alone through the single-box engine, 5 timed steps, L2 flushed"},
         "speedup_vs_plain_fp64": value / plain64, "speedup_vs_single_fp32": value / plain32,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": BATCH_TRAFFIC_B_PER_PARTICLE * nf_tot,
+                     "traffic_frac": BATCH_TRAFFIC_B_PER_PARTICLE * nf_tot / (stage["fluid"] * 1e-3) / 1e9 / hbm,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same ensemble, "
+                                       "scaled by particles (cell maps and sums beside the particle state)",
                      "peak_kind": peak_kind, "kernel": "batch fluid_step (collide + stream + bin), stages serialised",
                      "bytes_per_particle_step": 64, "avg_launch_ms": stage["fluid"]},
         "stage_ms_per_step": stage, "tuning": tuning, "clocks": clk.summary(),
