@@ -40,10 +40,15 @@ inline int sm_count() {
 inline int grid_for(long n, int threads = kThreads, int per_sm = 4) {
   long g = (n + threads - 1) / threads;
   if (g < 1) g = 1;
-  if (per_sm <= 0) {  // not persistent: -per_sm items per thread, short-lived CTAs
+  if (per_sm <= 0) {
+    // not persistent: -per_sm items per thread, short-lived CTAs, at most
+    // kMaxShortCTAs of them (more rounds per thread beyond that: every CTA
+    // ends with one float64 atomic into the same dissipated-energy word;
+    // 128^3 boxes measured best at about 10 k CTAs, like 64^3 ones)
+    constexpr long kMaxShortCTAs = 10240;
     const long per = (long)threads * (per_sm < 0 ? -per_sm : 1);
     g = (n + per - 1) / per;
-    return (int)(g < 1 ? 1 : (g > 0x7fffffffL ? 0x7fffffffL : g));
+    return (int)(g < 1 ? 1 : (g > kMaxShortCTAs ? kMaxShortCTAs : g));
   }
   const long cap = (long)sm_count() * per_sm;
   return (int)(g < cap ? g : cap);
