@@ -424,6 +424,21 @@ def run_cpu(args, budget_s=None, threads=None):
     return dict(value=(nf + nb) * n / el, steps=n, seconds=el, threads=threads, nf=nf, nb=nb)
 
 
+def max_over_ranks(t_rank, dist, device):
+    """The slowest rank's ms per step (replicas: every rank runs its own box)."""
+    import torch
+
+    t = torch.tensor([t_rank], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank, world, t_max_ms):
+    """Whole-job particle-steps/s: the units every rank advanced per step, over
+    the slowest rank's step time."""
+    return units_per_rank * world / (t_max_ms / 1e3)
+
+
 def clock_ok(c):
     bad = {"hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown"}
     return not (set(c.get("reasons", [])) & bad)
@@ -496,12 +511,8 @@ def main():
     value_rank = g["value"]
     t_rank = g["ms_per_step"]
     if dist is not None:
-        import torch
-
-        t = torch.tensor([t_rank], device=f"cuda:{args.device}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-        value = (g["nf"] + g["nb"]) * world / (t_max / 1e3)
+        t_max = max_over_ranks(t_rank, dist, f"cuda:{args.device}")
+        value = job_value(g["nf"] + g["nb"], world, t_max)
         dist.barrier()
     else:
         t_max = t_rank
