@@ -67,7 +67,7 @@ typedef struct {
   double bead_mass;      /* collision mass of MD beads (MDObject::partmass = 5) */
   unsigned long long seed; /* counter-based generator seed for free-running steps */
   int device;            /* CUDA device ordinal */
-  int sort_interval;     /* reorder particles by cell every this many steps (0 = auto) */
+  int sort_interval;     /* reorder particles by cell every this many steps (0 = auto: 50) */
   int md_split;          /* MD arithmetic: -1 auto (2 for MPCD_FP64, 3 for MPCD_FP32),
                             0 float64, 1 split (float springs on hi/lo position pairs; state
                             stays float64), 2 double-float (pairs of floats, about 48

@@ -586,7 +586,9 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
   mpcd_engine* h = new (std::nothrow) mpcd_engine();
   if (!h) return MPCD_ENOMEM;
   h->p = p;
-  if (h->p.sort_interval <= 0) h->p.sort_interval = 25;
+  // auto: every 50 steps (swimmer64 ms per step, float64 / float32: every 10
+  // steps 0.343 / 0.251, 25 0.334 / 0.246, 50 0.331 / 0.244, 100 0.331 / 0.244)
+  if (h->p.sort_interval <= 0) h->p.sort_interval = 50;
   for (int q = 0; q < 3; ++q) h->box.L[q] = p.sizes[q];
   h->ncell = (long)p.sizes[0] * p.sizes[1] * p.sizes[2];
   h->nsub = (int)((p.tstep + 0.00000001) / p.ststep);

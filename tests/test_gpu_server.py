@@ -19,7 +19,8 @@ collision partners), so:
     the three pairwise differences among three runs alone, and the mixed
     result's difference is the median over those three runs; it must stay
     within 3x (+1e-3) of the reference, both in the largest and in the RMS
-    bead deviation; kT agrees within 3e-3.
+    bead deviation; kT agrees with the runs alone within 3x their spread
+    (at least 2e-3).
 """
 import numpy as np
 import pytest
@@ -122,7 +123,11 @@ def test_long_run_mix_within_the_run_to_run_spread():
     mix_max, mix_rms = float(np.median([m[0] for m in mix])), float(np.median([m[1] for m in mix]))
     assert mix_max < 3 * ref_max + 1e-3, (mix_max, ref_max, ref, mix)
     assert mix_rms < 3 * ref_rms + 1e-3, (mix_rms, ref_rms, ref, mix)
-    assert abs(alone[0][0]["obs"]["kT"] - im["obs"]["kT"]) < 3e-3
+    # kT of diverged trajectories of a 16^3 box differs by its thermal spread
+    # (relative 1/sqrt(3N/2), about 0.005 here): against the runs alone
+    kts = [info["obs"]["kT"] for info, _, _ in alone]
+    kt_spread = max(abs(a - b) for a in kts for b in kts)
+    assert abs(im["obs"]["kT"] - float(np.median(kts))) < 3 * max(kt_spread, 2e-3), (im["obs"]["kT"], kts)
 
 
 def test_admission_respects_the_budget():
