@@ -56,6 +56,16 @@ def test_executable_runs_and_resumes(tmp_path):
     assert "T=" + str(g1)[:3] in r.stdout or "T=" in r.stdout
     san = np.loadtxt(tmp_path / "mpcd.san", ndmin=2)
     assert len(san) >= 2 and np.all(np.abs(san[:, 7] - 1.0) < 0.1)  # kT column of both runs
+    # the swimmer's <name>.san (Clami::writedata) read by the analysis restatement
+    import analysis
+
+    swim = [f for f in os.listdir(tmp_path) if f.endswith(".san") and f not in ("mpcd.san", "temp.san")]
+    assert swim, os.listdir(tmp_path)
+    d = analysis.load_san(tmp_path / swim[0])
+    assert len(d["time"]) >= 2 and np.all(np.diff(d["time"]) > 0)
+    N, B, P = analysis.orientation(d)
+    assert np.allclose(np.linalg.norm(N, axis=1), 1.0) and np.allclose(np.linalg.norm(P, axis=1), 1.0)
+    assert np.all(np.isfinite(d["vx"])) and np.all(np.isfinite(d["power"]))
 
 
 def _state(s):
