@@ -13,9 +13,11 @@ median deviation below 1e-5: the order of the float additions into the cell
 sums varies from run to run, and a particle within rounding of a cell face
 can then take the other cell under a later shift and collide with other
 partners, which spreads to its neighbours (measured: in about one run in
-three some 5 % of the particles differ by step 5, else 0.14 %); the kinetic temperature of a free run with walls sits above 1
-in the reference's own arithmetic (about 1.05 - 1.07 for an 8 x 8 x 12
-channel), so it is compared with the oracle's within 0.03; Poiseuille
+three some 5 % of the particles differ by step 5, else 0.14 %).
+
+The kinetic temperature of a free run with walls sits above 1 in the
+reference's own arithmetic (about 1.05 - 1.07 for an 8 x 8 x 12 channel),
+so it is compared with the oracle's within 0.03; Poiseuille
 viscosity (fit of the velocity profile averaged over 1000 samples 5 steps
 apart) within 8 % of the oracle's, the statistical error of each being about
 3 %.
