@@ -7,25 +7,38 @@ substeps per MPC step, the plain float64 method.  One step = one full MPC
 step: collision, all MD substeps, grid shift, streaming and binning.
 
 value  : (fluid + beads) x steps / device time of the timed steps (CUDA events
-         on the engine's stream; the L2 is flushed between steps).
-e2e    : the same metric through the C ABI with host buffers: the fluid and
-         the swimmer are uploaded from host memory, every step reads the
-         observables back, the final state is downloaded; wall clock.
+         on the engine's stream; the L2 is flushed between steps).  The MD
+         substeps run in double-float arithmetic (the float64 path's default,
+         `md_arith`); `ieee_fp64` is the same workload with IEEE float64 MD.
+e2e    : the same metric through the C ABI with host buffers over a fixed
+         window of 200 steps: the fluid and swimmer uploaded from host memory,
+         every step followed by an observables read-back, the final state
+         downloaded (wall clock).  The one-time upload / download and the
+         steady per-step rate are reported beside it.
 roofline: the fluid collide+stream kernel against the measured HBM copy
          bandwidth; algorithmic bytes per particle-step = read + write of the
-         particle state (float64: 6 x 8 B each way = 96 B; float32 split: 64 B).
+         reference's particle state (float64: 3 position + 4 velocity/mass
+         doubles = 56 B each way, 112 B; float32 split: 2 float4 = 64 B); the
+         96 B this build's float64 state moves (no mass column) beside it.
 cpu_baseline: the C restatement of the reference (oracle/) with OpenMP on the
          host cores, on a bounded sample of the same workload.
+plain_fluid: the 32^3 periodic fluid (327,680 particles, no swimmer).
 batched: the 64-replica mixed-size ensemble (box edges 16..48, 0-64 cilia)
          advanced together by the replica batch (float32 split, CUDA graphs,
          autotuned launch configuration), 1000 MPC steps timed, beside the
          same replicas run one at a time through the single-box engine.
+serving: 500 swimmer-run requests (box edges 16..64, 0-200 cilia, steps
+         log-uniform in 500..20000) arriving as a Poisson process, served by
+         continuous batching: p50 / p99 completion latency and throughput.
 large_swimmer: the 128^3 box with a radius-16 Clami of 400 cilia (3 x 20
-         beads) in float32 split precision, beside the float64 plain path on
-         the same seed (observable differences after the same steps).
+         beads) in float32 split precision, beside the float64 plain path, and
+         its observables against the float64 oracle run on the same initial
+         state and the same random draws.
 
 --impl reference runs that CPU restatement alone (the reference's own
 sources are not available where this runs) and prints its line.
+--ensemble-only --no-plain runs only the replica batch (the command of the
+batch fluid pass's ncu profile).
 Multi-GPU: replicas only - every rank advances its own independent box.
 """
 from __future__ import annotations
@@ -54,12 +67,19 @@ METRIC = "MPCD particle-steps/s"
 # one ncu capture on swimmer64 (profiles/fluid_step_swimmer64.md); the traffic
 # grows in proportion to the particles, so it is scaled to the workload.
 TRAFFIC_B_PER_PARTICLE = {"fp64": 98.9, "fp32": 48.7}
-# the replica batch's fluid pass on the 64-replica ensemble (profiles/batch_fluid_ensemble64.md)
-BATCH_TRAFFIC_B_PER_PARTICLE = 69.7
+# the replica batch's fluid pass on the 64-replica ensemble
+# (profiles/batch_fluid_ensemble64.md: 2,389.7 MB for 34,273,280 particles)
+BATCH_TRAFFIC_B_PER_PARTICLE = 2389.7e6 / 34273280
 # FP64 pipe of the same captures (sm__pipe_fp64_cycles_active, of peak, active):
 # the float64 fluid step is bound by it, not by HBM
 FP64_PIPE_ACTIVE = {"fp64": 0.824, "fp32": 0.014}
+# algorithmic bytes per particle-step: read + write of the reference's state
+# (float64: 3 position + 4 velocity/mass doubles; float32 split: two float4)
+BYTES_PER_PARTICLE = {"fp64": 112, "fp32": 64}
+# what this build's float64 layout moves (no mass column: 3 offsets + 3 velocities)
+STATE_BYTES_PER_PARTICLE = {"fp64": 96, "fp32": 64}
 UNIT = "particle-steps/s"
+E2E_STEPS = 200
 
 
 def peaks():
@@ -90,6 +110,7 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            time.sleep(0.3)  # the first sample lands before the timed region starts
         except FileNotFoundError:
             self.proc = None
         return self
@@ -102,6 +123,7 @@ class ClockSampler:
 
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.1)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -143,13 +165,23 @@ def describe(name, nf, nb, precision):
     return f"{name}: {geo}; {nf} fluid + {nb} beads; {precision}"
 
 
+def arm_config(args, nf, nb):
+    """The `config` both arms print for the same workload."""
+    prec = "float64 plain" if args.precision == "fp64" else "float32 split"
+    return {"workload": describe(args.workload, nf, nb, prec),
+            "l2": "flushed between timed steps (256 MB write, outside the timed events)",
+            "parallelism": f"replicas{args.gpus}"}
+
+
 # ------------------------------------------------------------------ GPU arm --
 
-def run_gpu(args, rank=0, md_arith=None, steps=None):
+def run_gpu(args, rank=0, md_arith=None, steps=None, workload=None, precision=None):
     import cilia_gpu as cg
 
-    prec = cg.MPCD_FP64 if args.precision == "fp64" else cg.MPCD_FP32
-    cfg = workload_cfg(args.workload, seed=1000 + rank)
+    precision = precision or args.precision
+    workload = workload or args.workload
+    prec = cg.MPCD_FP64 if precision == "fp64" else cg.MPCD_FP32
+    cfg = workload_cfg(workload, seed=1000 + rank)
     text = simcfg.dumps(cfg)
     sim = cg.Sim(text, precision=prec, seed=1000 + rank, device=args.device,
                  md_arith=cg.MD_AUTO if md_arith is None else md_arith)
@@ -181,9 +213,29 @@ def run_gpu(args, rank=0, md_arith=None, steps=None):
                 md_arith=md_arith)
 
 
+def roofline(nf, kernels, precision):
+    """The fluid collide + stream + bin kernel against the measured HBM copy bandwidth."""
+    hbm, peak_kind = peaks()
+    fl_ms, fl_n = kernels["fluid"]
+    avg_ms = fl_ms / max(fl_n, 1)
+    bpp = BYTES_PER_PARTICLE[precision]
+    achieved = nf * bpp / (avg_ms * 1e-3) / 1e9
+    state = nf * STATE_BYTES_PER_PARTICLE[precision] / (avg_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": TRAFFIC_B_PER_PARTICLE[precision] * nf,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, swimmer64 capture, scaled by "
+                              "particles", "peak_kind": peak_kind, "kernel": "fluid_step (collide + stream + bin)",
+            "bytes_per_particle_step": bpp, "avg_launch_ms": avg_ms,
+            "state_bytes_per_particle_step": STATE_BYTES_PER_PARTICLE[precision], "frac_state_bytes": state / hbm,
+            "fp64_pipe_active": FP64_PIPE_ACTIVE[precision],
+            "fp64_pipe_source": "ncu sm__pipe_fp64_cycles_active, swimmer64 capture (the float64 kernel's bound)"}
+
+
 def run_e2e(args):
-    """Through the C ABI with host buffers: upload, K steps with an observables
-    read-back each, final download."""
+    """Through the C ABI with host buffers, over a fixed window of E2E_STEPS
+    steps: upload of the fluid (the swimmer is built on the host and uploaded
+    with the Sim), every step followed by an observables read-back, final
+    download of fluid and beads; wall clock."""
     import cilia_gpu as cg
 
     prec = cg.MPCD_FP64 if args.precision == "fp64" else cg.MPCD_FP32
@@ -200,25 +252,47 @@ def run_e2e(args):
     bpos, bvel = sim.beads()
     t0 = time.perf_counter()
     eng.set_fluid(pos, vel)
-    for _ in range(args.steps):
+    t1 = time.perf_counter()
+    for _ in range(E2E_STEPS):
         eng.step()
         eng.observables()
+    t2 = time.perf_counter()
     p, v = eng.fluid()
     bp, bv = sim.beads()
-    wall = time.perf_counter() - t0
+    t3 = time.perf_counter()
     sim.close()
-    h2d = (pos.nbytes + vel.nbytes) / args.steps
-    d2h = (p.nbytes + v.nbytes + bp.nbytes + bv.nbytes) / args.steps + 64
-    return dict(value=(nf + nb) * args.steps / wall, h2d=h2d, d2h=d2h)
+    up = pos.nbytes + vel.nbytes + bpos.nbytes + bvel.nbytes
+    down = p.nbytes + v.nbytes + bp.nbytes + bv.nbytes
+    obs_bytes = 80
+    ntot = nf + nb
+    return dict(value=ntot * E2E_STEPS / (t3 - t0), h2d=up / E2E_STEPS, d2h=down / E2E_STEPS + obs_bytes,
+                steady=ntot * E2E_STEPS / (t2 - t1), upload_s=t1 - t0, download_s=t3 - t2, up=up, down=down,
+                step_ms=1e3 * (t2 - t1) / E2E_STEPS)
+
+
+def run_plain(args):
+    """The 32^3 periodic fluid (the plain-fluid workload), float64 and float32 split."""
+    out = {}
+    for prec in ("fp64", "fp32"):
+        g = run_gpu(args, workload="plain32", precision=prec, steps=max(20, min(args.steps, 200)))
+        rf = roofline(g["nf"], g["kernels"], prec)
+        out[prec] = {"value": g["value"], "ms_per_step": g["ms_per_step"], "kT": g["kT"],
+                     "fluid_kernel_ms": rf["avg_launch_ms"], "roofline_frac": rf["frac"],
+                     "bytes_per_particle_step": rf["bytes_per_particle_step"]}
+    out["workload"] = "plain32: 32^3 cells x 10 fluid (327680 particles), h = 0.1, no swimmer, L2 flushed"
+    return out
 
 
 # --------------------------------------------------------- batched ensemble --
 
-def run_ensemble(args, n=64, steps=1000):
+def run_ensemble(args, n=64, steps=1000, plain=True, stage_steps=20):
     """64 uneven replicas (box edge in {16..48}, sphere radius edge/8, 0-64
     cilia of rodlength 10-15) advanced together by the replica batch, FP32
-    split, `steps` MPC steps timed; beside it the same replicas run one at a
-    time through the single-box engine (the plain path), FP64 and FP32."""
+    split, `steps` MPC steps timed; beside it (plain=True) the same replicas
+    run one at a time through the single-box engine (the plain path), FP64
+    and FP32.  With plain=False and steps=0 only the stage timer runs
+    (`stage_steps` serialised steps): the command the batch fluid pass is
+    profiled with."""
     import cilia_gpu as cg
 
     specs = simcfg.ensemble_specs(n, seed=11)
@@ -229,12 +303,15 @@ def run_ensemble(args, n=64, steps=1000):
         text = simcfg.dumps(simcfg.swimmer_config(sp["L"], radius=sp["radius"], n_cilia=sp["n_cilia"],
                                                   rodlength=sp["rodlength"], seed=sp["seed"]))
         for prec, key in ((cg.MPCD_FP64, "fp64"), (cg.MPCD_FP32, "fp32")):
+            if key == "fp64" and not plain:
+                continue
             s = cg.Sim(text, precision=prec, ststep=0.002, seed=sp["seed"], device=args.device)
             npart = 10 * sp["L"] ** 3 + s.nbeads
-            s.engine.run(3)
-            ms = s.engine.timed_run(5, flush_l2=True)
-            single[key][0] += npart * 5
-            single[key][1] += float(ms.sum())
+            if plain:
+                s.engine.run(3)
+                ms = s.engine.timed_run(5, flush_l2=True)
+                single[key][0] += npart * 5
+                single[key][1] += float(ms.sum())
             if key == "fp32":
                 r = b.add_engine(s.engine)
                 b.admit(r)
@@ -243,8 +320,14 @@ def run_ensemble(args, n=64, steps=1000):
             s.close()
     for r in ids:
         b.set_steps(r, 10 ** 9)
+    if steps == 0:
+        b.set_md_layout(1, 512)
+        b.set_tuning(fluid_threads=256, fluid_blocks=0, cell_threads=256, cell_blocks=0, sort_interval=100)
+        stage = b.stage_times(stage_steps)
+        b.close()
+        return {"stage_ms_per_step": stage, "particles": parts, "replicas": len(ids)}
     tuning = b.autotune(trial_steps=50)
-    stage = b.stage_times(20)
+    stage = b.stage_times(stage_steps)
     for r in ids:
         b.set_steps(r, steps)
     l0 = b.launch_count()
@@ -264,6 +347,7 @@ def run_ensemble(args, n=64, steps=1000):
     achieved = nf_tot * 64 / (stage["fluid"] * 1e-3) / 1e9
     plain64 = single["fp64"][0] / (single["fp64"][1] / 1e3)
     plain32 = single["fp32"][0] / (single["fp32"][1] / 1e3)
+    step_bytes = value / parts * nf_tot * 64 / 1e9  # fluid state bytes per second of the whole timed step
     b.close()
     return {
         "workload": f"ensemble{n}: {n} replicas, box edge uniform in {{16,24,32,40,48}} x 10 fluid/cell, "
@@ -274,11 +358,12 @@ def run_ensemble(args, n=64, steps=1000):
         "plain_single_run": {"fp64": plain64, "fp32": plain32,
                              "how": "each replica alone through the single-box engine, 5 timed steps, L2 flushed"},
         "speedup_vs_plain_fp64": value / plain64, "speedup_vs_single_fp32": value / plain32,
+        "step_hbm_frac": step_bytes / hbm,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": BATCH_TRAFFIC_B_PER_PARTICLE * nf_tot,
                      "traffic_frac": BATCH_TRAFFIC_B_PER_PARTICLE * nf_tot / (stage["fluid"] * 1e-3) / 1e9 / hbm,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same ensemble, "
-                                       "scaled by particles (cell maps and sums beside the particle state)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same ensemble "
+                                       "(profiles/batch_fluid_ensemble64.md), scaled by particles",
                      "peak_kind": peak_kind, "kernel": "batch fluid_step (collide + stream + bin), stages serialised",
                      "bytes_per_particle_step": 64, "avg_launch_ms": stage["fluid"]},
         "stage_ms_per_step": stage, "tuning": tuning, "clocks": clk.summary(),
@@ -289,7 +374,7 @@ def run_ensemble(args, n=64, steps=1000):
 
 # ----------------------------------------------------------------- serving --
 
-def run_serving(args, n=60, steps_range=(100, 2000), load=0.8, seed=21):
+def run_serving(args, n=500, steps_range=(500, 20000), load=0.8, seed=21):
     """Continuous batching of swimmer runs: Poisson arrivals of requests with
     box edge uniform in 16..64 (10 fluid per cell), 0-200 cilia of rodlength
     15 on a sphere of radius min(8, edge/4) (a radius-edge/8 sphere carrying
@@ -346,9 +431,9 @@ def run_serving(args, n=60, steps_range=(100, 2000), load=0.8, seed=21):
     srv.close()
     done = [i for i in infos if i["state"] == cg.REQ_DONE]
     return {
-        "workload": f"serving: {n} swimmer runs, Poisson arrivals at {rate:.1f}/s, box edge uniform 16..64 x 10 "
-                    f"fluid/cell, sphere radius min(8, edge/4) with 0-200 cilia of 3x15 beads, steps log-uniform {steps_range[0]}..{steps_range[1]}, "
-                    f"float32 split",
+        "workload": f"serving: {n} swimmer runs, Poisson arrivals at {rate:.2f}/s, box edge uniform 16..64 x 10 "
+                    f"fluid/cell, sphere radius min(8, edge/4) with 0-200 cilia of 3x15 beads, steps log-uniform "
+                    f"{steps_range[0]}..{steps_range[1]}, float32 split",
         "metric": METRIC, "value": st["throughput"], "unit": UNIT, "p50_s": st["p50_s"], "p99_s": st["p99_s"],
         "mean_s": st["mean_s"], "max_s": st["max_s"], "completed": st["completed"], "failed": st["failed"],
         "wall_s": wall, "busy_s": st["busy_s"], "particle_steps": st["particle_steps"],
@@ -362,13 +447,28 @@ def run_serving(args, n=60, steps_range=(100, 2000), load=0.8, seed=21):
 
 # ------------------------------------------------------- large swimmer (c2) --
 
-def run_large(args, steps=200, seed=2024):
+def body_axis(bp):
+    """The swimmer's body axis n = sphere bead 1 - bead 0 (Clami::writedata), normalised."""
+    n = bp[1] - bp[0]
+    return n / np.linalg.norm(n)
+
+
+def vacf(v0, v):
+    """Normalised fluid velocity autocorrelation <v(0).v(t)> / <v(0).v(0)>."""
+    return float(np.einsum("ij,ij->", v0, v) / np.einsum("ij,ij->", v0, v0))
+
+
+def run_large(args, steps=200, seed=2024, oracle_steps=20):
     """swimmer128 (128^3 cells x 10 fluid, Clami R=16 with 400 cilia of 3x20
-    beads) in float32 split precision, timed, beside the float64 plain path
-    on the same seed (same initial state and random draws): the difference of
-    the observables after the same steps states the float32 error (the float64
-    path is the one pinned to the oracle)."""
+    beads) in float32 split precision, timed, beside the float64 plain path.
+    Then the precision statement: the float32 path run on the float64
+    oracle's recorded draws (grid shift, Gamma variates, rotation axes) from
+    the oracle's own initial state for `oracle_steps` steps, its observables
+    against the oracle's: fluid temperature, the fluid velocity
+    autocorrelation, the swimmer's centre-of-mass velocity and speed, and the
+    rotation rate of its body axis."""
     import cilia_gpu as cg
+    from oracle import build_from_cfg
 
     cfg = workload_cfg("swimmer128", seed=seed)
     text = simcfg.dumps(cfg)
@@ -380,29 +480,69 @@ def run_large(args, steps=200, seed=2024):
         nb = sim.nbeads
         eng.run(3)
         ms = eng.timed_run(steps, flush_l2=True)
-        obs = eng.observables()
-        bp, bv = sim.beads()
         lay = eng.md_layout()
-        res[key] = dict(value=(nf + nb) * steps / (float(ms.sum()) / 1e3), ms_per_step=float(ms.mean()), kT=obs["kT"],
-                        fluid_T=obs["fluid_T"], x_cm=bp.mean(axis=0), v_cm=bv.mean(axis=0), nf=nf, nb=nb,
-                        md_lanes=lay["lanes"], md_tile=lay["tile"], md_arith=MD_ARITH_NAMES[lay["arith"]])
+        res[key] = dict(value=(nf + nb) * steps / (float(ms.sum()) / 1e3), ms_per_step=float(ms.mean()), nf=nf,
+                        nb=nb, md_lanes=lay["lanes"], md_tile=lay["tile"], md_arith=MD_ARITH_NAMES[lay["arith"]])
         sim.close()
+    # float32 split on the oracle's draws against the float64 oracle
+    t0 = time.perf_counter()
+    o = build_from_cfg(cfg, seed=seed, ststep=0.002)
+    o.set_threads(os.cpu_count() or 1)
+    sim = cg.Sim(text, precision=cg.MPCD_FP32, seed=seed, create_fluid=False, device=args.device)
+    eng = sim.engine
+    p0, v0 = o.fluid()
+    eng.set_fluid(p0, v0)
+    eng.shift = o.shift
+    ob0, _ = o.beads()
+    gb0, _ = sim.beads()
+    dt = oracle_steps * float(cfg["tstep"])
+    for _ in range(oracle_steps):
+        rs, rg, ra, _ = o.step(record=True)
+        # a particle within float rounding of a cell face can fill a cell the
+        # float64 oracle left with one particle: no Gamma variate was drawn
+        # there; such a cell takes the mean of a two-particle cell's Gamma law
+        rg = np.where(rg < 0.0, 1.5, rg)
+        sim.next_tstep(rs, rg, ra)
+    _, vg = eng.fluid()
+    _, vo = o.fluid()
+    gb, gv = sim.beads()
+    ob, ov = o.beads()
+    sim.close()
+    ang = {}
+    for k, (b0, b1) in (("fp32", (gb0, gb)), ("oracle", (ob0, ob))):
+        c = float(np.clip(np.dot(body_axis(b0), body_axis(b1)), -1.0, 1.0))
+        ang[k] = math.acos(c) / dt
+    vc_g, vc_o = gv.mean(axis=0), ov.mean(axis=0)
+    stats = {
+        "steps": oracle_steps, "oracle_s": time.perf_counter() - t0,
+        "fluid_T": [float((vg ** 2).sum() / (3 * len(vg))), float((vo ** 2).sum() / (3 * len(vo)))],
+        "vacf": [vacf(v0, vg), vacf(v0, vo)],
+        "swimmer_v_cm": [vc_g.tolist(), vc_o.tolist()],
+        "swimmer_v_cm_err": float(np.linalg.norm(vc_g - vc_o)),
+        "swimmer_speed": [float(np.linalg.norm(vc_g)), float(np.linalg.norm(vc_o))],
+        "rotation_rate": [ang["fp32"], ang["oracle"]],
+        "rotation_rate_err": abs(ang["fp32"] - ang["oracle"]),
+        "bead_pos_err_max": float(np.abs(gb - ob).max()),
+        "how": "float32 split GPU run on the float64 oracle's recorded grid shifts, Gamma variates and rotation "
+               "axes from the oracle's initial state; pairs are [float32 GPU, float64 oracle]",
+    }
+    stats["fluid_T_err"] = abs(stats["fluid_T"][0] - stats["fluid_T"][1])
+    stats["vacf_err"] = abs(stats["vacf"][0] - stats["vacf"][1])
     a, b = res["fp32"], res["fp64"]
     return {
         "workload": describe("swimmer128", a["nf"], a["nb"], "float32 split") + f"; {steps} timed MPC steps",
         "metric": METRIC, "unit": UNIT, "value": a["value"], "ms_per_step": a["ms_per_step"],
         "plain_fp64": {"value": b["value"], "ms_per_step": b["ms_per_step"]},
         "md_layout": {"lanes": a["md_lanes"], "tile": a["md_tile"], "arith": a["md_arith"]},
-        "fp32_vs_fp64_same_seed": {"steps": steps + 3, "kT": [a["kT"], b["kT"]], "fluid_T": [a["fluid_T"], b["fluid_T"]],
-                                   "swimmer_x_cm_diff": float(np.linalg.norm(a["x_cm"] - b["x_cm"])),
-                                   "swimmer_v_cm": [float(np.linalg.norm(a["v_cm"])), float(np.linalg.norm(b["v_cm"]))],
-                                   "swimmer_v_cm_diff": float(np.linalg.norm(a["v_cm"] - b["v_cm"]))},
+        "fp32_vs_fp64_oracle": stats,
     }
 
 
 # ------------------------------------------------------------------ CPU arm --
 
-def run_cpu(args, budget_s=None, threads=None):
+def run_cpu(args, budget_s=None, threads=None, warmup=1, steps=None):
+    """The C restatement on the host cores: `warmup` untimed steps, then
+    `steps` timed steps (stopping early once the time budget is spent)."""
     from oracle import build_from_cfg
 
     cfg = workload_cfg(args.workload, seed=3)
@@ -412,15 +552,18 @@ def run_cpu(args, budget_s=None, threads=None):
     nf = s.fluid()[0].shape[0]
     nb = s.bead_count()
     budget = budget_s if budget_s is not None else args.cpu_budget
-    s.step()  # warm-up
+    steps = steps if steps is not None else args.steps
+    for _ in range(max(warmup, 0)):
+        s.step()
     n = 0
     t0 = time.perf_counter()
-    while True:
+    while n < steps:
         s.step()
         n += 1
         el = time.perf_counter() - t0
-        if (el >= budget and n >= 2) or n >= args.steps:
+        if el >= budget and n >= 2:
             break
+    el = time.perf_counter() - t0
     return dict(value=(nf + nb) * n / el, steps=n, seconds=el, threads=threads, nf=nf, nb=nb)
 
 
@@ -459,10 +602,12 @@ def main():
     ap.add_argument("--verify-counts", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ensemble-only", action="store_true")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="with --ensemble-only: skip the one-at-a-time runs and the timed run (stage timer only)")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-large", action="store_true", help="skip the 128^3 swimmer line")
     ap.add_argument("--serving-only", action="store_true")
-    ap.add_argument("--serving-full", action="store_true", help="500 requests, steps 500..20000")
+    ap.add_argument("--serving-quick", action="store_true", help="60 requests, steps 100..2000")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -471,6 +616,37 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.device is None:
         args.device = local
+    serving_kw = dict(n=60, steps_range=(100, 2000)) if args.serving_quick else {}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # 300 s at most for the timed steps (the full --steps when they fit)
+        r = run_cpu(args, budget_s=max(args.cpu_budget, 300.0), warmup=args.warmup, steps=args.steps)
+        line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic",
+                "config": arm_config(args, r["nf"], r["nb"]),
+                "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["threads"], "kind": "port",
+                                 "sample": f"{r['steps']} MPC steps of the full workload after {args.warmup} "
+                                           f"warm-up steps, {r['seconds']:.1f} s, C restatement of the reference "
+                                           f"(float64 throughout), OpenMP on {r['threads']} host threads"},
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if args.ensemble_only:
+        if rank == 0:
+            if args.no_plain:
+                print(json.dumps(run_ensemble(args, plain=False, steps=0, stage_steps=args.steps)))
+            else:
+                print(json.dumps(run_ensemble(args)))
+        return
+    if args.serving_only:
+        if rank == 0:
+            print(json.dumps(run_serving(args, **serving_kw)))
+        return
     dist = None
     if world > 1:
         import torch
@@ -478,32 +654,6 @@ def main():
 
         torch.cuda.set_device(args.device)
         dist.init_process_group("nccl")
-
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        r = run_cpu(args, budget_s=args.cpu_budget)
-        line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
-                "steps": r["steps"], "warmup": 1, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": describe(args.workload, r["nf"], r["nb"], "float64 CPU"),
-                                                "parallelism": f"openmp{r['threads']}"},
-                "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["threads"], "kind": "port",
-                                 "sample": f"{r['steps']} MPC steps of the full workload in {r['seconds']:.1f} s"},
-                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return
-
-    if args.ensemble_only:
-        if rank == 0:
-            print(json.dumps(run_ensemble(args)))
-        return
-    if args.serving_only or args.serving_full:
-        if rank == 0:
-            kw = dict(n=500, steps_range=(500, 20000)) if args.serving_full else {}
-            print(json.dumps(run_serving(args, **kw)))
-        return
-    if dist is not None:
         dist.barrier()
     g = run_gpu(args, rank)
     if not clock_ok(g["clocks"]):  # throttled: measure once more
@@ -519,60 +669,51 @@ def main():
         value = value_rank
     if rank != 0:
         return
-    hbm, peak_kind = peaks()
-    bpp = 96 if args.precision == "fp64" else 64
-    fl_ms, fl_n = g["kernels"]["fluid"]
-    avg_fluid_ms = fl_ms / max(fl_n, 1)
-    achieved = g["nf"] * bpp / (avg_fluid_ms * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
         "data": "synthetic",
-        "config": {"workload": describe(args.workload, g["nf"], g["nb"],
-                                        "float64 plain" if args.precision == "fp64" else "float32 split"),
-                   "l2": "flushed between timed steps (256 MB write, outside the timed events)",
-                   "parallelism": f"replicas{args.gpus}"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm,
-                     "traffic": TRAFFIC_B_PER_PARTICLE[args.precision] * g["nf"],
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, swimmer64 capture, "
-                                       "scaled by particles", "peak_kind": peak_kind,
-                     "kernel": "fluid_step (collide + stream + bin)",
-                     "fp64_pipe_active": FP64_PIPE_ACTIVE[args.precision],
-                     "fp64_pipe_source": "ncu sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active, swimmer64 "
-                                         "capture (20 float64 operations per particle: the kernel's bound)",
-                     "bytes_per_particle_step": bpp, "avg_launch_ms": avg_fluid_ms},
+        "config": arm_config(args, g["nf"], g["nb"]),
         "kernels_ms_per_step": {k: v[0] / max(g["prof_steps"], 1) for k, v in g["kernels"].items()},
-        "gpu_launches": g["launches"],
-        "clocks": g["clocks"],
         "kT": g["kT"],
     }
     if g["md_arith"] is not None:
-        line["config"]["md_arith"] = MD_ARITH_NAMES[g["md_arith"]]
+        line["md_arith"] = MD_ARITH_NAMES[g["md_arith"]]
+    # the long nested records first, the short headline figures last (the end
+    # of the line is what a truncated log keeps)
+    if not args.no_ensemble and args.gpus == 1:
+        line["batched"] = run_ensemble(args)
+    if not args.no_serving and args.gpus == 1:
+        line["serving"] = run_serving(args, **serving_kw)
+    if not args.no_large and args.gpus == 1 and args.workload == "swimmer64":
+        line["large_swimmer"] = run_large(args)
+    if not args.no_extra and args.gpus == 1:
+        line["plain_fluid"] = run_plain(args)
     if args.precision == "fp64" and g["nb"] and not args.no_extra:
         # the same workload with the MD substeps in IEEE float64 arithmetic
         import cilia_gpu as cg
 
-        f = run_gpu(args, rank, md_arith=cg.MD_F64, steps=min(args.steps, 30))
-        line["plain_md_float64"] = {"value": f["value"], "unit": UNIT, "ms_per_step": f["ms_per_step"],
-                                    "md_ms_per_step": f["kernels"]["md"][0] / max(f["prof_steps"], 1),
-                                    "steps": min(args.steps, 30), "md_arith": MD_ARITH_NAMES[0]}
-    if not args.no_extra:
-        e = run_e2e(args)
-        line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
-                       "d2h_bytes_per_step": e["d2h"]}
-    if not args.no_ensemble and args.gpus == 1:
-        line["batched"] = run_ensemble(args)
-    if not args.no_serving and args.gpus == 1:
-        line["serving"] = run_serving(args)
-    if not args.no_large and args.gpus == 1 and args.workload == "swimmer64":
-        line["large_swimmer"] = run_large(args)
+        k = max(3, min(args.steps, 100))
+        f = run_gpu(args, rank, md_arith=cg.MD_F64, steps=k)
+        line["ieee_fp64"] = {"value": f["value"], "ms_per_step": f["ms_per_step"],
+                             "md_ms_per_step": f["kernels"]["md"][0] / max(f["prof_steps"], 1), "steps": k,
+                             "md_arith": MD_ARITH_NAMES[0]}
+    line["roofline"] = roofline(g["nf"], g["kernels"], args.precision)
     if not args.no_cpu:
         c = run_cpu(args)
         line["cpu_baseline"] = {"value": c["value"], "unit": UNIT, "cores": c["threads"], "kind": "port",
                                 "sample": f"{c['steps']} MPC steps of {args.workload} ({c['nf']} fluid + "
                                           f"{c['nb']} beads) in {c['seconds']:.1f} s, C restatement, OpenMP"}
+    if not args.no_extra:
+        e = run_e2e(args)
+        line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                       "d2h_bytes_per_step": e["d2h"], "steps": E2E_STEPS,
+                       "steady_value": e["steady"], "steady_ms_per_step": e["step_ms"],
+                       "upload_s": e["upload_s"], "download_s": e["download_s"],
+                       "upload_bytes": e["up"], "download_bytes": e["down"]}
+    line["gpu_launches"] = g["launches"]
+    line["clocks"] = g["clocks"]
     print(json.dumps(line))
 
 

@@ -87,6 +87,14 @@ int mpcd_batch_admit(mpcd_batch* b, int r);
 int mpcd_batch_set_steps(mpcd_batch* b, int r, long long nsteps);
 /* nsteps MPC steps of every replica with steps left */
 int mpcd_batch_run(mpcd_batch* b, int nsteps);
+/* One MPC step of every replica with steps left, in which replica r takes
+ * the grid shift, Gamma variates and rotation axes of `inj` (mpcd_inject of
+ * mpcd_gpu.h, indexed by r's own cells; virt must be NULL) instead of its
+ * generator's: the replica-batch counterpart of mpcd_step(h, inj), used to
+ * run a replica against the reference's recorded randomness.  Launched
+ * without graphs; waits for the step.  MPCD_EDEVICE when an injected Gamma is
+ * missing for a thermostatted cell. */
+int mpcd_batch_step_inject(mpcd_batch* b, int r, const mpcd_inject* inj);
 /* like run, timed with CUDA events on the batch's stream: total device ms */
 int mpcd_batch_timed_run(mpcd_batch* b, int nsteps, double* total_ms);
 int mpcd_batch_sync(mpcd_batch* b);

@@ -199,6 +199,55 @@ int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* la
 int mpcd_md_layout(mpcd_engine* h, int* info);
 
 /* ----------------------------------------------------------------------------
+ * Rigid spheres with no-slip bounce-back.  The reference's bounce-back
+ * surfaces are the planar walls of -DNOSLIP (streaming reflection,
+ * src/libcilia/mpcd.cpp:346-376; virtual particles in the wall layers,
+ * mpcd.cpp:175-198); these calls extend the same two rules to spheres, an
+ * addition with no counterpart in the reference's object model (its Sphere is
+ * a bead-spring mesh coupled through the collision only):
+ *   - streaming: a fluid particle that reaches a sphere's surface during the
+ *     step leaves the contact point with v' = 2 u_s - v, u_s the surface
+ *     velocity V + W x r_c, for the rest of the step;
+ *   - collision: a cell the surface cuts that holds n < 10 particles gets
+ *     10 - n virtual particles moving with u_s at the cell centre plus
+ *     thermal noise at kT = 1 (or the injected mpcd_inject.virt);
+ *   - both exchanges are summed per sphere in float64 (impulse and angular
+ *     impulse); a free sphere (mass > 0, solid: I = 2/5 m r^2) takes them into
+ *     its velocity and angular velocity after every step and moves with its
+ *     velocity; a held sphere (mass <= 0) keeps its velocity and angular
+ *     velocity (0 for a fixed obstacle).
+ * Spheres smaller than half the box have periodic images; larger ones (a
+ * sphere of very large radius stands for a curved wall) have none.  Fluid
+ * should be placed outside the spheres: a particle found inside at the start
+ * of a step is put on the surface and reflected there.  At most
+ * MPCD_MAX_RIGID_SPHERES; n = 0 removes them.  The getter returns the state
+ * and, in force_torque[n][6] (may be NULL), the mean force and torque the
+ * fluid exerted since the spheres were set or the sums reset.
+ * -------------------------------------------------------------------------- */
+#define MPCD_MAX_RIGID_SPHERES 4
+typedef struct {
+  double center[3];
+  double velocity[3];
+  double omega[3];
+  double radius;
+  double mass; /* > 0 free, <= 0 held */
+} mpcd_rigid_sphere;
+int mpcd_set_rigid_spheres(mpcd_engine* h, int n, const mpcd_rigid_sphere* spheres);
+int mpcd_get_rigid_spheres(mpcd_engine* h, int n, mpcd_rigid_sphere* spheres, double* force_torque);
+int mpcd_reset_rigid_sphere_forces(mpcd_engine* h);
+
+/* The counter-based generator's collision draws, for checking them against
+ * the reference's samplers: for cells k = 0 .. n-1 of step `step` under
+ * `seed`, gamma[k] is the Gamma(3(nc-1)/2, 1) variate a free-running step
+ * gives a cell of nc particles (rgamma, src/libcilia/mpcd.cpp:13-43) and
+ * axis[3k..3k+2] the float64 path's unit rotation axis
+ * (generate_collision_matrix, src/libcilia/mpcd.cpp:269-284).  Host arrays;
+ * either may be NULL.  Runs on `device` (allocates and frees its own device
+ * buffers).  MPCD_EDEVICE when a Gamma draw hit the sampler's iteration cap. */
+int mpcd_collision_draws(int nc, unsigned long long seed, unsigned long long step, long n, double* gamma,
+                         double* axis, int device);
+
+/* ----------------------------------------------------------------------------
  * mpcd_fluid_step_noalloc -- one split-precision MPC step of a plain fluid
  * (collision, streaming, binning; no beads, no walls) that allocates no device
  * memory.  It has no counterpart in the reference: it exists for callers that
@@ -222,9 +271,13 @@ int mpcd_md_layout(mpcd_engine* h, int* info);
  * MPCD_NOALLOC_MAX_CELLS cells (about 3.4 MB), held by every GPU that loads the
  * library until the process exits.  Larger boxes are rejected with
  * MPCD_EINVAL.  The first call on a device looks the array's address up
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race, and the array keeps the last call's contents.
+ * (cudaGetSymbolAddress) with that device current.  Every call synchronizes
+ * `stream` (it reads the layout check, the error word and the dissipated
+ * energy back), so it must not be called on a stream that is being captured.
+ * All calls share the array: calls that overlap on the GPU race, and the
+ * array keeps the last call's contents.  Particles that break the layout
+ * above (a cell index at or beyond its box edge, an offset outside [0,1)) are
+ * rejected with MPCD_EDEVICE before anything is changed.
  * Returns MPCD_OK, MPCD_EINVAL, MPCD_ECUDA, or MPCD_EDEVICE (a device-side check failed).
  * -------------------------------------------------------------------------- */
 #define MPCD_NOALLOC_MAX_CELLS 65536

@@ -97,6 +97,11 @@ class MpcdServerStats(ctypes.Structure):
 REQ_QUEUED, REQ_RESIDENT, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
+class MpcdRigidSphere(ctypes.Structure):
+    _fields_ = [("center", ctypes.c_double * 3), ("velocity", ctypes.c_double * 3), ("omega", ctypes.c_double * 3),
+                ("radius", ctypes.c_double), ("mass", ctypes.c_double)]
+
+
 class MpcdError(RuntimeError):
     pass
 
@@ -142,6 +147,12 @@ def lib():
             "mpcd_md_layout": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
             "mpcd_fluid_step_noalloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.c_long, P, P, _D, _DP, _DP,
                                                        ctypes.c_ulonglong, ctypes.c_ulonglong, _DP, P]),
+            "mpcd_set_rigid_spheres": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdRigidSphere)]),
+            "mpcd_get_rigid_spheres": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdRigidSphere), _DP]),
+            "mpcd_reset_rigid_sphere_forces": (ctypes.c_int, [P]),
+            "mpcd_collision_draws": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_long,
+                                                    _DP, _DP, ctypes.c_int]),
+            "mpcd_batch_step_inject": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdInject)]),
             "mpcd_batch_create": (ctypes.c_int, [ctypes.POINTER(MpcdBatchParams), ctypes.POINTER(P)]),
             "mpcd_batch_destroy": (ctypes.c_int, [P]),
             "mpcd_batch_last_error": (ctypes.c_char_p, [P]),
@@ -211,6 +222,17 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def collision_draws(nc, n, *, seed=1, step=1, device=0, gamma=True, axis=True):
+    """The device generator's per-cell draws of one step (mpcd_collision_draws):
+    Gamma(3(nc-1)/2) variates and float64-path rotation axes of cells 0..n-1."""
+    g = np.zeros(n) if gamma else None
+    a = np.zeros((n, 3)) if axis else None
+    rc = lib().mpcd_collision_draws(int(nc), int(seed), int(step), int(n), _dp(g), _dp(a), int(device))
+    if rc:
+        raise MpcdError(f"mpcd_collision_draws failed ({rc})")
+    return g, a
 
 
 def _dp(a):
@@ -355,6 +377,32 @@ class Engine:
         n = ctypes.c_longlong()
         self._ck(lib().mpcd_kernel_time(self._h, int(kernel), ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
         return ms.value, n.value
+
+    def set_rigid_spheres(self, spheres):
+        """Rigid no-slip spheres: dicts with center, radius and optional velocity,
+        omega, mass (> 0 free, <= 0 or absent held)."""
+        arr = (MpcdRigidSphere * max(len(spheres), 1))()
+        for k, sp in enumerate(spheres):
+            arr[k].center[:] = [float(x) for x in sp["center"]]
+            arr[k].velocity[:] = [float(x) for x in sp.get("velocity", (0.0, 0.0, 0.0))]
+            arr[k].omega[:] = [float(x) for x in sp.get("omega", (0.0, 0.0, 0.0))]
+            arr[k].radius = float(sp["radius"])
+            arr[k].mass = float(sp.get("mass", 0.0))
+        self._ck(lib().mpcd_set_rigid_spheres(self._h, len(spheres), arr), "set_rigid_spheres")
+        self._nsph = len(spheres)
+
+    def rigid_spheres(self):
+        """(list of sphere dicts, mean force and torque [n, 6] since the last reset)."""
+        n = getattr(self, "_nsph", 0)
+        arr = (MpcdRigidSphere * max(n, 1))()
+        ft = np.zeros((max(n, 1), 6))
+        self._ck(lib().mpcd_get_rigid_spheres(self._h, n, arr, _dp(ft)), "get_rigid_spheres")
+        out = [dict(center=np.array(arr[k].center[:]), velocity=np.array(arr[k].velocity[:]),
+                    omega=np.array(arr[k].omega[:]), radius=arr[k].radius, mass=arr[k].mass) for k in range(n)]
+        return out, ft[:n]
+
+    def reset_sphere_forces(self):
+        self._ck(lib().mpcd_reset_rigid_sphere_forces(self._h), "reset_rigid_sphere_forces")
 
     def md_layout(self):
         """The MD kernels' layout: cluster or cooperative grid, threads per slot, tile, tiles, slots, springs."""
@@ -528,6 +576,12 @@ class Batch:
 
     def run(self, nsteps):
         self._ck(lib().mpcd_batch_run(self._h, int(nsteps)), "batch_run")
+
+    def step_inject(self, r, shift_next=None, gamma=None, axis=None):
+        """One step in which replica r takes injected randomness (mpcd_batch_step_inject)."""
+        keep = [_f64(shift_next), _f64(gamma), _f64(axis)]
+        inj = MpcdInject(_dp(keep[0]), _dp(keep[1]), _dp(keep[2]), None)
+        self._ck(lib().mpcd_batch_step_inject(self._h, r, ctypes.byref(inj)), "step_inject")
 
     def timed_run(self, nsteps):
         ms = ctypes.c_double()

@@ -334,8 +334,7 @@ int plan_launches(mpcd_batch* b) {
 }
 
 // enqueue one step (prologue, cell maps, fluid | MD) on s0 with MD forked off
-int enqueue_step(mpcd_batch* b, int par) {
-  const BatchTables t = tables(b);
+int enqueue_step(mpcd_batch* b, int par, const BatchTables& t) {
   int n = 0;
   n += launch_batch_prologue(t, b->s0);
   n += launch_batch_cell_params(t, b->cells, b->tune.cell_threads, b->tune.cell_blocks, b->s0);
@@ -377,7 +376,7 @@ int capture(mpcd_batch* b, int par, int nsteps, bool sorts, cudaGraphExec_t* out
   int rc = MPCD_OK;
   int p = par;
   for (int k = 0; k < nsteps && rc == MPCD_OK; ++k) {
-    rc = enqueue_step(b, p);
+    rc = enqueue_step(b, p, tables(b));
     if (rc == MPCD_OK && sorts && (k + 1) % b->tune.sort_interval == 0) {
       rc = enqueue_sort(b, p);
       p ^= 1;
@@ -1111,6 +1110,55 @@ int mpcd_batch_timed_run(mpcd_batch* b, int nsteps, double* total_ms) {
   cudaEventDestroy(e1);
   if (total_ms) *total_ms = ms;
   return rc;
+}
+
+int mpcd_batch_step_inject(mpcd_batch* b, int r, const mpcd_inject* inj) {
+  Replica* R = get_rep(b, r);
+  if (!R || !R->admitted || !inj) return fail(b, MPCD_EINVAL, "step_inject: bad arguments");
+  if (inj->virt) return fail(b, MPCD_EINVAL, "step_inject: a batch replica has no walls");
+  if (inj->shift_next)
+    for (int q = 0; q < 3; ++q)
+      if (!(inj->shift_next[q] >= 0.0 && inj->shift_next[q] < 1.0))
+        return fail(b, MPCD_EINVAL, "step_inject: injected shift outside [0,1)");
+  int rc = rebuild_graphs(b);  // plans the MD launches
+  if (rc) return rc;
+  const long nc = R->ncell;
+  double* d = nullptr;  // shift [3] | gamma [nc] | axis [3 nc]
+  BK(dalloc(&d, 3 + 4 * (size_t)nc));
+  BatchTables t = tables(b);
+  t.inj_rep = r;
+  cudaError_t e = cudaSuccess;
+  if (inj->shift_next && e == cudaSuccess) {
+    e = cudaMemcpyAsync(d, inj->shift_next, 3 * sizeof(double), cudaMemcpyHostToDevice, b->s0);
+    t.inj_shift = d;
+  }
+  if (inj->gamma && e == cudaSuccess) {
+    e = cudaMemcpyAsync(d + 3, inj->gamma, nc * sizeof(double), cudaMemcpyHostToDevice, b->s0);
+    t.inj_gamma = d + 3;
+  }
+  if (inj->axis && e == cudaSuccess) {
+    e = cudaMemcpyAsync(d + 3 + nc, inj->axis, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, b->s0);
+    t.inj_axis = d + 3 + nc;
+  }
+  if (e == cudaSuccess) {
+    rc = enqueue_step(b, b->cur, t);  // every replica with steps left advances; r with these draws
+    b->launches_total += b->kernels_per_step;
+    if (rc == MPCD_OK && ++b->since_sort >= b->tune.sort_interval) {
+      enqueue_sort(b, b->cur);
+      b->launches_total += b->kernels_per_sort;
+      b->cur ^= 1;
+      b->since_sort = 0;
+    }
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->s0);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(b, e, "step_inject");
+  if (rc) return rc;
+  BatchState S;
+  BK(cudaMemcpy(&S, b->d_state + r, sizeof S, cudaMemcpyDeviceToHost));
+  if (S.err & kErrGammaMissing) return fail(b, MPCD_EDEVICE, "step_inject: injected gamma missing for a thermostatted cell");
+  return MPCD_OK;
 }
 
 int mpcd_batch_sync(mpcd_batch* b) {

@@ -75,6 +75,13 @@ struct BatchTables {
   const int* cell_page_rep;  // [ncell_pages]
   long npart_pages, ncell_pages;
   int nrep;                  // replica slots
+  // values that replace the generator for replica inj_rep in this step (as
+  // mpcd_inject for one engine); inj_rep = -1: none.  Device arrays indexed by
+  // the replica's own cells.
+  int inj_rep = -1;
+  const double* inj_shift = nullptr;  // [3]
+  const double* inj_gamma = nullptr;  // [ncell]
+  const double* inj_axis = nullptr;   // [ncell][3]
 };
 
 // ------------------------------------------------------------ launchers ---

@@ -38,7 +38,11 @@ __global__ void k_batch_prologue(BatchTables t) {
   const uint64_t step = st.steps + 1;
   S.step = step;
   double an[3];
-  {
+  if (r == t.inj_rep && t.inj_shift) {
+    an[0] = t.inj_shift[0];
+    an[1] = t.inj_shift[1];
+    an[2] = t.inj_shift[2];
+  } else {
     const u32x4 q = draw4(R.seed, step, kStreamShift, 0u, 0u);  // shift_from_counter (engine.cu)
     an[0] = u01_dbl(q.x);
     an[1] = u01_dbl(q.y);
@@ -97,6 +101,9 @@ __global__ void k_batch_cell_params(BatchTables t, BatchCells c) {
     const uint64_t seed = R.seed, step = S.step;
     const float mb = S.fbead_mass;
     const long cell0 = R.cell0;
+    const bool inj = r == t.inj_rep;
+    const double* inj_gamma = inj ? t.inj_gamma : nullptr;
+    const double* inj_axis = inj ? t.inj_axis : nullptr;
     float ldiss = 0.0f;
     unsigned errbits = 0;
     bool gfail = false;
@@ -123,8 +130,8 @@ __global__ void k_batch_cell_params(BatchTables t, BatchCells c) {
         const long cid = cb + u * stride;
         c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
         c.cnt[cid] = 0u;
-        cell_map_f32(sm[u], w[u], (uint32_t)(cid - cell0), seed, step, mb, nullptr, nullptr, c.par + 2 * cid, ldiss,
-                     errbits, gfail);
+        cell_map_f32(sm[u], w[u], (uint32_t)(cid - cell0), seed, step, mb, inj_gamma, inj_axis, c.par + 2 * cid,
+                     ldiss, errbits, gfail);
       }
     }
     if (gfail) errbits |= kErrGammaLoop;

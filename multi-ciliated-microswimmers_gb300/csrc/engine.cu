@@ -87,6 +87,14 @@ struct mpcd_engine {
   long long prof_n[8] = {0};
   void* flush_buf = nullptr;
 
+  // rigid spheres (mpcd_set_rigid_spheres): device state, this step's
+  // impulses, running force / torque sums and the steps they cover
+  int nsph = 0;
+  RigidSphereDev* d_sph = nullptr;
+  double* d_sph_acc = nullptr;
+  double* d_sph_fsum = nullptr;
+  long long sph_steps = 0;
+
   long steps = 0;
   double globalt = 0.0;
   double a[3] = {0.5, 0.5, 0.5};
@@ -250,6 +258,11 @@ StepArgs step_args(mpcd_engine* h, const double* a_cur, const double* a_next, do
   s.fh = (float)s.h;
   s.fgkick = (float)s.gkick;
   s.fbead_mass = (float)s.bead_mass;
+  if (h->nsph > 0) {
+    s.sph.n = h->nsph;
+    s.sph.s = h->d_sph;
+    s.sph.acc = h->d_sph_acc;
+  }
   return s;
 }
 
@@ -681,6 +694,9 @@ int mpcd_destroy(mpcd_engine* h) {
   cudaFree(h->d_obs_part);
   cudaFree(h->d_obs_count);
   cudaFree(h->d_bar);
+  cudaFree(h->d_sph);
+  cudaFree(h->d_sph_acc);
+  cudaFree(h->d_sph_fsum);
   cudaFree(h->flush_buf);
   for (auto& m : h->marks) {
     cudaEventDestroy(m.a);
@@ -1025,6 +1041,10 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
     h->launches += f64 ? launch_fluid_step_f64(h->f64, h->c64, s, h->stream, per_sm)
                        : launch_fluid_step_f32(h->f32, h->c32, s, h->stream, per_sm);
   }
+  if (h->nsph > 0) {
+    h->launches += launch_spheres_update(h->d_sph, h->nsph, h->d_sph_acc, h->d_sph_fsum, h->p.tstep, h->box, h->stream);
+    h->sph_steps++;
+  }
   if (fork) {
     CK(cudaEventRecord(h->ev_join, h->smd));
     CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
@@ -1151,6 +1171,104 @@ int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* la
   if (total_ms) *total_ms = h->prof_ms[kernel];
   if (launches) *launches = h->prof_n[kernel];
   return MPCD_OK;
+}
+
+int mpcd_set_rigid_spheres(mpcd_engine* h, int n, const mpcd_rigid_sphere* spheres) {
+  if (!h || n < 0 || n > MPCD_MAX_RIGID_SPHERES || (n > 0 && !spheres))
+    return fail(h, MPCD_EINVAL, "set_rigid_spheres: bad arguments");
+  std::vector<RigidSphereDev> dev(kMaxSpheres);
+  for (int k = 0; k < n; ++k) {
+    const mpcd_rigid_sphere& q = spheres[k];
+    RigidSphereDev& d = dev[k];
+    if (!(q.radius > 0.0) || !std::isfinite(q.radius) || !std::isfinite(q.mass))
+      return fail(h, MPCD_EINVAL, "set_rigid_spheres: radius must be positive and finite");
+    for (int j = 0; j < 3; ++j) {
+      if (!std::isfinite(q.center[j]) || !std::isfinite(q.velocity[j]) || !std::isfinite(q.omega[j]))
+        return fail(h, MPCD_EINVAL, "set_rigid_spheres: non-finite centre, velocity or angular velocity");
+      double c = q.center[j];
+      const double L = h->box.L[j];
+      if (q.radius < 0.5 * L) c -= std::floor(c / L) * L;  // spheres with periodic images: into [0, L)
+      if (c >= L && q.radius < 0.5 * L) c = 0.0;
+      d.c[j] = c;
+      d.v[j] = q.velocity[j];
+      d.w[j] = q.omega[j];
+    }
+    d.r = q.radius;
+    d.mass = q.mass;
+    d.inertia = q.mass > 0.0 ? 0.4 * q.mass * q.radius * q.radius : 0.0;
+  }
+  if (!h->d_sph) {
+    CK(dalloc(&h->d_sph, kMaxSpheres));
+    CK(dalloc(&h->d_sph_acc, 6 * kMaxSpheres));
+    CK(dalloc(&h->d_sph_fsum, 6 * kMaxSpheres));
+  }
+  CK(cudaMemcpyAsync(h->d_sph, dev.data(), kMaxSpheres * sizeof(RigidSphereDev), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemsetAsync(h->d_sph_acc, 0, 6 * kMaxSpheres * sizeof(double), h->stream));
+  CK(cudaMemsetAsync(h->d_sph_fsum, 0, 6 * kMaxSpheres * sizeof(double), h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->nsph = n;
+  h->sph_steps = 0;
+  return MPCD_OK;
+}
+
+int mpcd_get_rigid_spheres(mpcd_engine* h, int n, mpcd_rigid_sphere* spheres, double* force_torque) {
+  if (!h || n != h->nsph || (n > 0 && !spheres && !force_torque))
+    return fail(h, MPCD_EINVAL, "get_rigid_spheres: n does not match the sphere count");
+  if (n == 0) return MPCD_OK;
+  std::vector<RigidSphereDev> dev(n);
+  std::vector<double> fs(6 * (size_t)n);
+  CK(cudaMemcpyAsync(dev.data(), h->d_sph, n * sizeof(RigidSphereDev), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(fs.data(), h->d_sph_fsum, 6 * n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < n; ++k) {
+    if (spheres) {
+      for (int j = 0; j < 3; ++j) {
+        spheres[k].center[j] = dev[k].c[j];
+        spheres[k].velocity[j] = dev[k].v[j];
+        spheres[k].omega[j] = dev[k].w[j];
+      }
+      spheres[k].radius = dev[k].r;
+      spheres[k].mass = dev[k].mass;
+    }
+    if (force_torque)
+      for (int j = 0; j < 6; ++j) force_torque[6 * k + j] = h->sph_steps > 0 ? fs[6 * k + j] / h->sph_steps : 0.0;
+  }
+  return device_error(h);
+}
+
+int mpcd_reset_rigid_sphere_forces(mpcd_engine* h) {
+  if (!h) return MPCD_EINVAL;
+  if (h->d_sph_fsum) CK(cudaMemsetAsync(h->d_sph_fsum, 0, 6 * kMaxSpheres * sizeof(double), h->stream));
+  h->sph_steps = 0;
+  return MPCD_OK;
+}
+
+int mpcd_collision_draws(int nc, unsigned long long seed, unsigned long long step, long n, double* gamma,
+                         double* axis, int device) {
+  if (nc < 2 || nc > 0xffff || n < 0 || n > 0xffffffffL || (!gamma && !axis)) return MPCD_EINVAL;
+  if (n == 0) return MPCD_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return MPCD_ECUDA;
+  double *dg = nullptr, *da = nullptr;
+  unsigned* derr = nullptr;
+  int rc = MPCD_OK;
+  auto ok = [&](cudaError_t e) {
+    if (e != cudaSuccess && rc == MPCD_OK) rc = e == cudaErrorMemoryAllocation ? MPCD_ENOMEM : MPCD_ECUDA;
+    return rc == MPCD_OK;
+  };
+  unsigned err = 0;
+  if (ok(dalloc(&derr, 1)) && ok(cudaMemset(derr, 0, sizeof(unsigned))) && (!gamma || ok(dalloc(&dg, n))) &&
+      (!axis || ok(dalloc(&da, 3 * n)))) {
+    launch_collision_draws(nc, seed, step, n, dg, da, derr, nullptr);
+    if (ok(cudaGetLastError()) && ok(cudaDeviceSynchronize()) &&
+        (!gamma || ok(cudaMemcpy(gamma, dg, n * sizeof(double), cudaMemcpyDeviceToHost))) &&
+        (!axis || ok(cudaMemcpy(axis, da, 3 * n * sizeof(double), cudaMemcpyDeviceToHost))))
+      ok(cudaMemcpy(&err, derr, sizeof err, cudaMemcpyDeviceToHost));
+  }
+  cudaFree(dg);
+  cudaFree(da);
+  cudaFree(derr);
+  if (rc == MPCD_OK && err) rc = MPCD_EDEVICE;
+  return rc;
 }
 
 int mpcd_md_layout(mpcd_engine* h, int* info) {

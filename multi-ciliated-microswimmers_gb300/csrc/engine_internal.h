@@ -44,6 +44,24 @@ struct CellsF32 {
   float4* par = nullptr;  // 2 float4 per cell: (axis, thermostat factor), (mean velocity, 0)
 };
 
+// Rigid spheres the fluid bounces off (no-slip), with virtual particles in
+// the cells their surface cuts.  State on the device, advanced by
+// k_spheres_update after every step unless held.
+constexpr int kMaxSpheres = 4;
+struct RigidSphereDev {
+  double c[3];  // centre, in [0, L)
+  double v[3];  // velocity
+  double w[3];  // angular velocity
+  double r;     // radius
+  double mass;  // > 0 free; <= 0 held (v, w kept)
+  double inertia;
+};
+struct SphereSet {
+  int n = 0;
+  const RigidSphereDev* s = nullptr;  // device [n]
+  double* acc = nullptr;              // device [n][6]: impulse and angular impulse received this step
+};
+
 // Per-step scalars for the fluid kernels.
 struct StepArgs {
   Box box;
@@ -64,6 +82,7 @@ struct StepArgs {
   double* diss;       // accumulated dissipated energy (float64)
   // float copies for the split-precision kernels (no conversions per thread)
   float fta_cur[3], fta_next[3], fh, fgkick, fbead_mass;
+  SphereSet sph;      // rigid spheres (n = 0: none)
 };
 
 // ------------------------------------------------------------------- MD ---
@@ -212,5 +231,12 @@ int launch_md_cluster_f32cells(const MDState& m, const CellsF32& c, const MDStep
 int launch_observables_f32(const FluidF32& f, const MDState& m, double bead_mass, double* out, cudaStream_t s);
 int launch_sort_f32(FluidF32& f, FluidF32& tmp, const Box& box, uint32_t* count, uint32_t* start,
                     uint32_t* rank, uint32_t* blocksums, cudaStream_t s);
+// the generator's Gamma variates (cells of nc particles) and float64 rotation
+// axes of cells 0 .. n-1 in step `step` (either output may be null)
+int launch_collision_draws(int nc, uint64_t seed, uint64_t step, long n, double* gamma, double* axis, unsigned* err,
+                           cudaStream_t s);
+// rigid spheres after a step: force sums, motion, impulses cleared (one CTA)
+int launch_spheres_update(RigidSphereDev* sph, int n, double* acc, double* fsum, double h, const Box& box,
+                          cudaStream_t s);
 
 }  // namespace mpcd

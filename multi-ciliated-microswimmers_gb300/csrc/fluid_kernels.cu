@@ -130,11 +130,55 @@ constexpr InvTable make_inv_table() {
 }
 __device__ const InvTable g_inv_n = make_inv_table();
 
+// Free-running rotation axis of the float64 path: the direction drawn in
+// float (cos theta = 2u - 1, phi = 2 pi u', as generate_collision_matrix,
+// src/libcilia/mpcd.cpp:269-284), normalised in float64 so that the rotation
+// is orthogonal to float64 precision.  |r|^2 = 1 + e with |e| of a few float
+// roundings: two Newton steps for 1/sqrt from 1 (y1 = 1.5 - n2/2 is within
+// 3e^2/8, y2 within float64 rounding) on the FMA chain instead of the general
+// reciprocal square root.
+__device__ __forceinline__ void draw_axis_f64(uint64_t seed, uint64_t step, uint32_t cid, double& rx, double& ry,
+                                              double& rz) {
+  const u32x4 r = draw4(seed, step, kStreamCell, cid, 0u);
+  const float ct = 2.0f * u01_flt(r.y) - 1.0f;
+  const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+  float sp, cp;
+  sincospif(2.0f * u01_flt(r.x), &sp, &cp);
+  rx = (double)(st * cp);
+  ry = (double)(st * sp);
+  rz = (double)ct;
+  const double n2 = fma(rx, rx, fma(ry, ry, rz * rz));
+  const double y1 = fma(-0.5, n2, 1.5);
+  const double y2 = y1 * fma(-0.5, (n2 * y1) * y1, 1.5);
+  rx *= y2;
+  ry *= y2;
+  rz *= y2;
+}
+
 __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, const StepArgs& a, double* A,
                                               double* b, double& ldiss, unsigned& errbits, bool& gfail) {
   const int nf = cnt_fluid(w), nb = cnt_beads(w);
   int num = nf + nb;
   double M = (double)nf + (double)nb * a.bead_mass;
+  const double preal[3] = {s.x, s.y, s.z}, mreal = M;  // the real particles' momentum and mass
+  int sk = -1;  // rigid sphere whose surface cuts the cell
+  double rel[3];
+  if (a.sph.n && num < 10 && !(a.walls && wall_layer_cell(a.box, cid))) {
+    const int L0 = a.box.L[0], L1 = a.box.L[1];
+    sk = sphere_cut_cell(a.sph, a.box, a.a_cur, (int)(cid % L0), (int)((cid / L0) % L1), (int)(cid / ((long)L0 * L1)),
+                         rel);
+    if (sk >= 0) {  // virtual particles up to rho = 10, moving with the surface
+      const int dm = 10 - num;
+      double pv[3];
+      sphere_virtual(a.sph.s[sk], rel, dm, a.seed, a.step, (uint32_t)cid, a.inj_virt, pv);
+      s.x += pv[0];
+      s.y += pv[1];
+      s.z += pv[2];
+      s.w += (pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2]) / dm;
+      M += dm;
+      num += dm;
+    }
+  }
   if (a.walls && num < 10 && wall_layer_cell(a.box, cid)) {  // virtual particles up to rho = 10
     const int dm = 10 - num;
     double pv[3];
@@ -175,24 +219,7 @@ __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, c
     ry = a.inj_axis[3 * cid + 1];
     rz = a.inj_axis[3 * cid + 2];
   } else {
-    // direction drawn in float, normalised in float64 so that R is orthogonal to float64 precision
-    const u32x4 r = draw4(a.seed, a.step, kStreamCell, (uint32_t)cid, 0u);
-    const float ct = 2.0f * u01_flt(r.y) - 1.0f;
-    const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-    float sp, cp;
-    sincospif(2.0f * u01_flt(r.x), &sp, &cp);
-    rx = (double)(st * cp);
-    ry = (double)(st * sp);
-    rz = (double)ct;
-    // |r|^2 = 1 + e with |e| of a few float roundings: two Newton steps for
-    // 1/sqrt from 1 (y1 = 1.5 - n2/2 is within 3e^2/8, y2 within float64
-    // rounding) on the FMA chain instead of the general reciprocal square root
-    const double n2 = fma(rx, rx, fma(ry, ry, rz * rz));
-    const double y1 = fma(-0.5, n2, 1.5);
-    const double y2 = y1 * fma(-0.5, (n2 * y1) * y1, 1.5);
-    rx *= y2;
-    ry *= y2;
-    rz *= y2;
+    draw_axis_f64(a.seed, a.step, (uint32_t)cid, rx, ry, rz);
   }
   const double ca = kCosAlpha, sa = kSinAlpha, oc = 1.0 - kCosAlpha;
   // A = sc R, R the rotation about (rx, ry, rz) by alpha with the entries of
@@ -214,6 +241,15 @@ __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, c
   b[0] = ux - (A[0] * ux + A[1] * uy + A[2] * uz);
   b[1] = uy - (A[3] * ux + A[4] * uy + A[5] * uz);
   b[2] = uz - (A[6] * ux + A[7] * uy + A[8] * uz);
+  if (sk >= 0) {
+    // the real particles' momentum after the collision is A P + M b; what
+    // they gained came from the virtual particles, i.e. from the sphere
+    double J[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      J[q] = preal[q] - (A[3 * q] * preal[0] + A[3 * q + 1] * preal[1] + A[3 * q + 2] * preal[2] + mreal * b[q]);
+    add_impulse(a.sph.acc + 6 * sk, rel, J);
+  }
   // dissipated energy (src/libcilia/mpcd.cpp:166-168, 232-234, 243-246): every
   // cell adds sum m v^2 before the collision here, and every particle
   // subtracts its m v'^2 after it (fluid_step, bead_collide), so the total
@@ -288,7 +324,8 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
   const Thresh tcx = thresh(a.ta_cur[0]), tcy = thresh(a.ta_cur[1]), tcz = thresh(a.ta_cur[2]);
   const Thresh tnx = thresh(a.ta_next[0]), tny = thresh(a.ta_next[1]), tnz = thresh(a.ta_next[2]);
   const double h = a.h, gk = a.gkick;
-  const bool kick = gk != 0.0, walls = a.walls != 0;
+  // walls or rigid spheres: streaming in unwrapped coordinates with bounce-back
+  const bool kick = gk != 0.0, walls = a.walls != 0 || a.sph.n > 0;
   const I n = (I)f.n;
   double ke_after = 0.0;
   unsigned bad = 0;
@@ -310,10 +347,20 @@ __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF6
       oz = fma(vz, h, oz);
     } else {
       double x = ix + ox, y = iy + oy, z = iz + oz;
-      x += vx * h;
-      y += vy * h;
-      z += vz * h;
-      wall_bounce(a.walls, (double)(Lz - 1), x, y, z, vx, vy, vz);
+      double X[3] = {x, y, z}, V[3] = {vx, vy, vz};
+      if (a.sph.n && sphere_bounce(a.sph, a.box, h, X, V)) {
+        x = X[0];
+        y = X[1];
+        z = X[2];
+        vx = V[0];
+        vy = V[1];
+        vz = V[2];
+      } else {
+        x += vx * h;
+        y += vy * h;
+        z += vz * h;
+      }
+      if (a.walls) wall_bounce(a.walls, (double)(Lz - 1), x, y, z, vx, vy, vz);
       double fx = floor(x), fy = floor(y), fz = floor(z);
       ox = x - fx;
       oy = y - fy;
@@ -663,7 +710,7 @@ __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
       c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
       c.cnt[cid] = 0u;
       cell_map_f32(sm[u], w[u], (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 2 * cid,
-                   ldiss, errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt);
+                   ldiss, errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt, &a);
     }
   }
   if (gfail) errbits |= kErrGammaLoop;
@@ -684,11 +731,26 @@ template <int U>
 struct FluidMinBlocks {
   static constexpr int value = U >= 4 ? 2 : 4;
 };
+// default options of the split-precision fluid pass (kOptPrefetch | kOptAggregate bits)
+constexpr int kFluidOpt = 0;
+
+// Options of the split-precision fluid pass (bits of kOpt):
+//   kOptPrefetch  one thread per CTA and round sends the particle state of the
+//                 chunk `pf_dist` particles ahead (the chunk a later round or
+//                 a later CTA takes) from HBM into L2 by a bulk prefetch, so
+//                 that the dependent chain particle -> cell -> map starts
+//                 from L2
+//   kOptAggregate the warp's particles binned into the same next cell are
+//                 summed in registers (peer_sum) and added by one vector
+//                 reduction and one count add per cell and warp
+constexpr int kOptPrefetch = 1;
+constexpr int kOptAggregate = 2;
 
 // kWalls: the bounce-back path (its float64 temporaries would otherwise
 // crowd the registers of the batched loads).
-template <int U, bool kWalls, typename I>
-__global__ void __launch_bounds__(kThreads, FluidMinBlocks<U>::value) k_fluid_step_f32(FluidF32 f, CellsF32 c, StepArgs a) {
+template <int U, bool kWalls, typename I, int kOpt>
+__global__ void __launch_bounds__(kThreads, FluidMinBlocks<U>::value)
+    k_fluid_step_f32(FluidF32 f, CellsF32 c, StepArgs a, long pf_dist) {
   const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
   const float tcx = a.fta_cur[0], tcy = a.fta_cur[1], tcz = a.fta_cur[2];
   const float tnx = a.fta_next[0], tny = a.fta_next[1], tnz = a.fta_next[2];
@@ -696,8 +758,19 @@ __global__ void __launch_bounds__(kThreads, FluidMinBlocks<U>::value) k_fluid_st
   float ke_after = 0.0f;
   unsigned bad = 0;
   const I n = (I)f.n;
-  // each block takes U x blockDim consecutive particles per round
-  for (I base = (I)blockIdx.x * U * blockDim.x + threadIdx.x; base < n; base += (I)gridDim.x * U * blockDim.x) {
+  const I lane = (I)(threadIdx.x & 31);
+  // each block takes U x blockDim consecutive particles per round; the loop
+  // runs while the warp's first particle exists, so that every lane of a
+  // warp takes part in the warp-wide operations of each round
+  for (I base = (I)blockIdx.x * U * blockDim.x + threadIdx.x; base - lane < n; base += (I)gridDim.x * U * blockDim.x) {
+    if ((kOpt & kOptPrefetch) && threadIdx.x == 0) {
+      const long s = (long)base + pf_dist;
+      if (s < (long)n) {
+        const long cnt = min((long)U * blockDim.x, (long)n - s);
+        prefetch_l2(f.pos + s, (uint32_t)(cnt * sizeof(float4)));
+        prefetch_l2(f.vel + s, (uint32_t)(cnt * sizeof(float4)));
+      }
+    }
     float4 p[U], v[U], mk[U], mu[U];
 #pragma unroll
     for (int q = 0; q < U; ++q) {
@@ -723,7 +796,13 @@ __global__ void __launch_bounds__(kThreads, FluidMinBlocks<U>::value) k_fluid_st
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       const I i = base + (I)q * blockDim.x;
-      if (i >= n) continue;
+      if (kOpt & kOptAggregate) {
+        if (base + (I)q * blockDim.x - lane >= n) continue;  // warp-uniform: no particle of this warp
+      } else if (i >= n) {
+        continue;
+      }
+      const bool valid = i < n;
+      if (!valid) p[q] = v[q] = mk[q] = mu[q] = make_float4(0.f, 0.f, 0.f, 0.f);
       const uint32_t cp = __float_as_uint(p[q].w);
       int ix = cell_x(cp), iy = cell_y(cp), iz = cell_z(cp);
       float ox = p[q].x, oy = p[q].y, oz = p[q].z, vx = v[q].x, vy = v[q].y, vz = v[q].z;
@@ -736,10 +815,20 @@ __global__ void __launch_bounds__(kThreads, FluidMinBlocks<U>::value) k_fluid_st
       } else {
         double x = ix + (double)ox, y = iy + (double)oy, z = iz + (double)oz;
         double dvx = vx, dvy = vy, dvz = vz;
-        x += dvx * a.h;
-        y += dvy * a.h;
-        z += dvz * a.h;
-        wall_bounce(a.walls, (double)(Lz - 1), x, y, z, dvx, dvy, dvz);
+        double X[3] = {x, y, z}, V[3] = {dvx, dvy, dvz};
+        if (a.sph.n && sphere_bounce(a.sph, a.box, a.h, X, V)) {
+          x = X[0];
+          y = X[1];
+          z = X[2];
+          dvx = V[0];
+          dvy = V[1];
+          dvz = V[2];
+        } else {
+          x += dvx * a.h;
+          y += dvy * a.h;
+          z += dvz * a.h;
+        }
+        if (a.walls) wall_bounce(a.walls, (double)(Lz - 1), x, y, z, dvx, dvy, dvz);
         double fx = floor(x), fy = floor(y), fz = floor(z);
         ox = (float)(x - fx);
         oy = (float)(y - fy);
@@ -757,10 +846,23 @@ __global__ void __launch_bounds__(kThreads, FluidMinBlocks<U>::value) k_fluid_st
       if (gk != 0.0f) vx += gk;
       const uint32_t cn = (uint32_t)shifted_f(ix, ox, tnx, Lx) +
                           (uint32_t)Lx * ((uint32_t)shifted_f(iy, oy, tny, Ly) + (uint32_t)Ly * (uint32_t)shifted_f(iz, oz, tnz, Lz));
-      red_add_v4(c.sum + cn, make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz));
-      atomicAdd(c.cnt + cn, 1u);
-      __stcs(f.pos + i, make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz))));
-      __stcs(f.vel + i, make_float4(vx, vy, vz, 0.f));
+      const float4 contrib = make_float4(vx, vy, vz, vx * vx + vy * vy + vz * vz);
+      if (kOpt & kOptAggregate) {
+        const uint32_t key = valid ? cn : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const float4 tot = peer_sum(peers, valid ? contrib : make_float4(0.f, 0.f, 0.f, 0.f));
+        if (valid && (unsigned)(__ffs(peers) - 1) == (unsigned)lane) {
+          red_add_v4(c.sum + cn, tot);
+          atomicAdd(c.cnt + cn, (uint32_t)__popc(peers));
+        }
+      } else {
+        red_add_v4(c.sum + cn, contrib);
+        atomicAdd(c.cnt + cn, 1u);
+      }
+      if (valid) {  // (a lane past the end carried a zero particle: nothing to store, nothing added to ke_after)
+        __stcs(f.pos + i, make_float4(ox, oy, oz, __uint_as_float(pack_cell(ix, iy, iz))));
+        __stcs(f.vel + i, make_float4(vx, vy, vz, 0.f));
+      }
     }
   }
   if (bad) atomicOr(a.err, bad);
@@ -959,9 +1061,64 @@ __global__ void k_store_fluid_f32(FluidF32 f, double* pos, double* vel, unsigned
   }
 }
 
+// Rigid spheres after a step: the impulse and angular impulse the fluid gave
+// them this step are added to the running force and torque sums (divided by
+// h) and cleared; every sphere moves with the velocity it had during the
+// step; a free sphere (mass > 0) then takes the impulses into its velocity
+// and angular velocity (solid sphere, I = 2/5 m r^2).  Float64 throughout.
+__global__ void k_spheres_update(RigidSphereDev* s, int n, double* acc, double* fsum, double h, Box box) {
+  const int k = threadIdx.x;
+  if (k >= n) return;
+  RigidSphereDev S = s[k];
+  double* A = acc + 6 * k;
+  for (int j = 0; j < 6; ++j) fsum[6 * k + j] += A[j] / h;
+  for (int q = 0; q < 3; ++q) {
+    S.c[q] += S.v[q] * h;
+    if (S.r < 0.5 * box.L[q]) {  // spheres with periodic images stay in [0, L)
+      if (S.c[q] >= box.L[q]) S.c[q] -= box.L[q];
+      if (S.c[q] < 0.0) S.c[q] += box.L[q];
+    }
+  }
+  if (S.mass > 0.0) {
+    for (int q = 0; q < 3; ++q) {
+      S.v[q] += A[q] / S.mass;
+      S.w[q] += A[3 + q] / S.inertia;
+    }
+  }
+  for (int j = 0; j < 6; ++j) A[j] = 0.0;
+  s[k] = S;
+}
+
+// The generator's per-cell draws, as the collision kernels take them: cell k
+// of step `step` gets the Gamma(3(nc-1)/2) variate of gamma_mt and the
+// float64 path's rotation axis.  Used to check the samplers' distributions.
+__global__ void k_collision_draws(int nc, uint64_t seed, uint64_t step, long n, double* gamma, double* axis,
+                                  unsigned* err) {
+  bool gfail = false;
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    if (gamma) gamma[k] = (double)gamma_mt(nc, seed, step, (uint32_t)k, &gfail);
+    if (axis) draw_axis_f64(seed, step, (uint32_t)k, axis[3 * k], axis[3 * k + 1], axis[3 * k + 2]);
+  }
+  if (gfail) atomicOr(err, kErrGammaLoop);
+}
+
 }  // namespace
 
 // ============================================================ launchers ===
+
+int launch_spheres_update(RigidSphereDev* sph, int n, double* acc, double* fsum, double h, const Box& box,
+                          cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_spheres_update<<<1, 32, 0, s>>>(sph, n, acc, fsum, h, box);
+  return 1;
+}
+
+int launch_collision_draws(int nc, uint64_t seed, uint64_t step, long n, double* gamma, double* axis, unsigned* err,
+                           cudaStream_t s) {
+  if (n == 0) return 0;
+  k_collision_draws<<<grid_for(n), kThreads, 0, s>>>(nc, seed, step, n, gamma, axis, err);
+  return 1;
+}
 
 int launch_cell_params_f64(const CellsF64& c, const StepArgs& a, cudaStream_t s) {
   k_cell_params_f64<<<grid_for(c.ncell), kThreads, 0, s>>>(c, a);
@@ -1025,32 +1182,60 @@ int launch_cell_params_f32(const CellsF32& c, const StepArgs& a, cudaStream_t s)
   k_cell_params_f32<<<grid_for(c.ncell), kThreads, 0, s>>>(c, a);
   return 1;
 }
+template <int U, int kOpt>
+void launch_fluid_f32_opt(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s, int per_sm) {
+  const int ps = per_sm <= 0 ? per_sm : std::min(per_sm, FluidMinBlocks<U>::value);
+  const int gb = grid_for((f.n + U - 1) / U, kThreads, ps);
+  const bool i32 = f.n + 4L * gb * kThreads < (1L << 32);
+  long pf = 0;
+  if (kOpt & kOptPrefetch) {
+    // the chunk the CTA starting after the current wave (or this CTA's next
+    // round, for a grid of at most one wave) will take
+    static int resident = 0;
+    if (resident == 0) {
+      int per = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fluid_step_f32<U, false, uint32_t, kOpt>, kThreads, 0);
+      resident = std::max(1, per) * sm_count();
+    }
+    pf = (long)std::min(gb, resident) * U * kThreads;
+  }
+  if (i32)
+    k_fluid_step_f32<U, false, uint32_t, kOpt><<<gb, kThreads, 0, s>>>(f, c, a, pf);
+  else
+    k_fluid_step_f32<U, false, long, kOpt><<<gb, kThreads, 0, s>>>(f, c, a, pf);
+}
+
 int launch_fluid_step_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s, int per_sm) {
   if (f.n == 0) return 0;
-  const int g1 = grid_for(f.n, kThreads, per_sm);
-  const bool i32 = f.n + 4L * g1 * kThreads < (1L << 32);
-  if (a.walls != 0) {
-    i32 ? k_fluid_step_f32<1, true, uint32_t><<<g1, kThreads, 0, s>>>(f, c, a)
-        : k_fluid_step_f32<1, true, long><<<g1, kThreads, 0, s>>>(f, c, a);
+  if (a.walls != 0 || a.sph.n > 0) {
+    const int g1 = grid_for(f.n, kThreads, per_sm);
+    const bool i32 = f.n + 4L * g1 * kThreads < (1L << 32);
+    i32 ? k_fluid_step_f32<1, true, uint32_t, 0><<<g1, kThreads, 0, s>>>(f, c, a, 0)
+        : k_fluid_step_f32<1, true, long, 0><<<g1, kThreads, 0, s>>>(f, c, a, 0);
     return 1;
   }
-  // particles per thread and round: kFluidBatch unless MPCD_FLUID_BATCH (1, 2, 4) says otherwise
+  // particles per thread and round: kFluidBatch unless MPCD_FLUID_BATCH (1, 2) says otherwise;
+  // options: kFluidOpt unless MPCD_FLUID_OPT (0..3: bit 0 prefetch, bit 1 aggregation) says otherwise
   static const int batch = [] {
     const char* e = std::getenv("MPCD_FLUID_BATCH");
     const int b = e ? std::atoi(e) : kFluidBatch;
-    return b == 1 || b == 4 ? b : 2;
+    return b == 1 ? 1 : 2;
   }();
-  const int ps = per_sm <= 0 ? per_sm : std::min(per_sm, batch == 4 ? FluidMinBlocks<4>::value : FluidMinBlocks<2>::value);
-  const int gb = grid_for((f.n + batch - 1) / batch, kThreads, ps);
-  if (batch == 4)
-    i32 ? k_fluid_step_f32<4, false, uint32_t><<<gb, kThreads, 0, s>>>(f, c, a)
-        : k_fluid_step_f32<4, false, long><<<gb, kThreads, 0, s>>>(f, c, a);
-  else if (batch == 2)
-    i32 ? k_fluid_step_f32<2, false, uint32_t><<<gb, kThreads, 0, s>>>(f, c, a)
-        : k_fluid_step_f32<2, false, long><<<gb, kThreads, 0, s>>>(f, c, a);
-  else
-    i32 ? k_fluid_step_f32<1, false, uint32_t><<<gb, kThreads, 0, s>>>(f, c, a)
-        : k_fluid_step_f32<1, false, long><<<gb, kThreads, 0, s>>>(f, c, a);
+  static const int opt = [] {
+    const char* e = std::getenv("MPCD_FLUID_OPT");
+    const int o = e ? std::atoi(e) : kFluidOpt;
+    return o & 3;
+  }();
+  switch (batch * 4 + opt) {
+    case 4: launch_fluid_f32_opt<1, 0>(f, c, a, s, per_sm); break;
+    case 5: launch_fluid_f32_opt<1, 1>(f, c, a, s, per_sm); break;
+    case 6: launch_fluid_f32_opt<1, 2>(f, c, a, s, per_sm); break;
+    case 7: launch_fluid_f32_opt<1, 3>(f, c, a, s, per_sm); break;
+    case 8: launch_fluid_f32_opt<2, 0>(f, c, a, s, per_sm); break;
+    case 9: launch_fluid_f32_opt<2, 1>(f, c, a, s, per_sm); break;
+    case 10: launch_fluid_f32_opt<2, 2>(f, c, a, s, per_sm); break;
+    default: launch_fluid_f32_opt<2, 3>(f, c, a, s, per_sm); break;
+  }
   return 1;
 }
 int launch_bin_fluid_f32(const FluidF32& f, const CellsF32& c, const StepArgs& a, cudaStream_t s) {

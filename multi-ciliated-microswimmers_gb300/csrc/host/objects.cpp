@@ -711,6 +711,26 @@ Simulation::Simulation(const libconfig::Setting& root, const SimOptions& o) : op
     if (!(opt.read_files && load_fluid("fluid_n.dat"))) create_fluid();
   }
   upload_md();
+  // rigid no-slip spheres (an addition to the reference's cfg schema):
+  //   rigid_spheres = ( { position = [x, y, z]; radius = r; mass = m; velocity = [..]; omega = [..]; } );
+  // mass > 0 free, absent or <= 0 held (mpcd_set_rigid_spheres)
+  if (root.exists("rigid_spheres") && !opt.host_only) {
+    const libconfig::Setting& rs = root["rigid_spheres"];
+    std::vector<mpcd_rigid_sphere> sp(rs.getLength());
+    for (int i = 0; i < rs.getLength(); ++i) {
+      const libconfig::Setting& c = rs[i];
+      mpcd_rigid_sphere& q = sp[i];
+      q = mpcd_rigid_sphere{};
+      for (int j = 0; j < 3; ++j) q.center[j] = (double)c["position"][j];
+      q.radius = (double)c["radius"];
+      c.lookupValue("mass", q.mass);
+      if (c.exists("velocity"))
+        for (int j = 0; j < 3; ++j) q.velocity[j] = (double)c["velocity"][j];
+      if (c.exists("omega"))
+        for (int j = 0; j < 3; ++j) q.omega[j] = (double)c["omega"][j];
+    }
+    check(mpcd_set_rigid_spheres(eng, (int)sp.size(), sp.data()), eng, "mpcd_set_rigid_spheres");
+  }
 }
 
 Simulation::~Simulation() {

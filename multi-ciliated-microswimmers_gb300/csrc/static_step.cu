@@ -9,7 +9,10 @@
 // loads the library holds that array until the process exits; every call
 // shares it, so calls that overlap on the GPU (different streams or threads)
 // race, and the array keeps the last call's contents (the sums are cleared at
-// the start of each call).
+// the start of each call).  Particles that break the layout (a cell index
+// beyond the box, an offset outside [0,1)) are rejected before any kernel
+// touches the scratch.
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -53,6 +56,21 @@ cudaError_t scratch_for_device(int dev, unsigned char** out) {
   return cudaSuccess;
 }
 
+// Caller-packed particles are checked before any kernel indexes the scratch
+// with them: every axis' cell index below the box edge and every offset in
+// [0,1) (NaN fails).  A bad particle sets kErrCellRange in *err.
+__global__ void k_check_split_f32(FluidF32 f, Box box, unsigned* err) {
+  unsigned bad = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < f.n; i += (long)gridDim.x * blockDim.x) {
+    const float4 p = f.pos[i];
+    const uint32_t cp = __float_as_uint(p.w);
+    const bool ok = (cp >> 30) == 0u && cell_x(cp) < box.L[0] && cell_y(cp) < box.L[1] && cell_z(cp) < box.L[2] &&
+                    p.x >= 0.0f && p.x < 1.0f && p.y >= 0.0f && p.y < 1.0f && p.z >= 0.0f && p.z < 1.0f;
+    if (!ok) bad = 1u;
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(err, kErrCellRange);
+}
+
 }  // namespace
 
 extern "C" int mpcd_fluid_step_noalloc(const int* sizes, long n, void* pos, void* vel, double tstep,
@@ -87,6 +105,18 @@ extern "C" int mpcd_fluid_step_noalloc(const int* sizes, long n, void* pos, void
   if (cudaMemsetAsync(cells.sum, 0, sizeof(float4) * ncell, s) != cudaSuccess) return MPCD_ECUDA;
   if (cudaMemsetAsync(cells.cnt, 0, sizeof(uint32_t) * ncell, s) != cudaSuccess) return MPCD_ECUDA;
   if (cudaMemsetAsync(d_diss, 0, sizeof(double) + sizeof(unsigned), s) != cudaSuccess) return MPCD_ECUDA;
+  unsigned err_h = 0;
+  if (n > 0) {
+    // the caller's layout is checked first: a cell index beyond the box would
+    // send the binning's atomics past the scratch array
+    Box box{{sizes[0], sizes[1], sizes[2]}};
+    const long g = std::min<long>((n + 255) / 256, 4096);
+    k_check_split_f32<<<(int)g, 256, 0, s>>>(f, box, d_err);
+    if (cudaGetLastError() != cudaSuccess) return MPCD_ECUDA;
+    if (cudaMemcpyAsync(&err_h, d_err, sizeof err_h, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPCD_ECUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return MPCD_ECUDA;
+    if (err_h) return MPCD_EDEVICE;  // nothing was changed
+  }
   StepArgs a{};
   for (int q = 0; q < 3; ++q) {
     a.box.L[q] = sizes[q];
@@ -110,7 +140,6 @@ extern "C" int mpcd_fluid_step_noalloc(const int* sizes, long n, void* pos, void
   launch_fluid_step_f32(f, cells, a, s);    // collide, stream, bin with the next shift
   if (cudaGetLastError() != cudaSuccess) return MPCD_ECUDA;
   double diss_h = 0.0;
-  unsigned err_h = 0;
   if (cudaMemcpyAsync(&diss_h, d_diss, sizeof diss_h, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPCD_ECUDA;
   if (cudaMemcpyAsync(&err_h, d_err, sizeof err_h, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPCD_ECUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return MPCD_ECUDA;

@@ -248,3 +248,72 @@ def test_shared_memory_staged_fluid_pass_matches_the_direct_pass():
     for (p1, v1), (p2, v2), sp in zip(out[0], out[1], specs):
         ok, worst = fluid_close(p1, v1, p2, v2, sp["L"])
         assert ok, worst
+
+
+def ref_bead_pos(g, tag):
+    P = [g[f"{tag}_obj{k}_pos"].reshape(-1, 3) for k in range(64) if f"{tag}_obj{k}_pos" in g]
+    return np.concatenate(P)
+
+
+def test_replica_with_injected_randomness_tracks_reference_fluid():
+    """One replica of the batch run on the reference's recorded randomness
+    (mpcd_batch_step_inject) against the reference's own trajectory
+    (tests/golden/fluid8.npz), beside an uninjected replica that keeps
+    running on its generator: split-precision tolerances of test_gpu_fp32."""
+    from conftest import golden
+
+    g = golden("fluid8")
+    L = 8
+    b = make_batch([dict(L=L, n_cilia=0, rodlength=10), dict(L=16, n_cilia=0, rodlength=10)])
+    other = b.add(16, seed=5)
+    rng = np.random.default_rng(2)
+    po = rng.uniform(0, 16, (16 ** 3 * 10, 3))
+    vo = rng.normal(size=po.shape)
+    b.set_fluid(other, po, vo)
+    b.admit(other)
+    b.set_steps(other, 10)
+    r = b.add(L, seed=1)
+    b.set_fluid(r, g["step0_fluid_pos"], g["step0_fluid_vel"])
+    b.set_shift(r, g["shift_0"])
+    b.admit(r)
+    b.set_steps(r, 3)
+    for k in range(1, 4):
+        b.step_inject(r, g[f"shift_{k}"], g[f"gamma_{k}"], g[f"axis_{k}"])
+        assert np.array_equal(b.shift(r), g[f"shift_{k}"])
+    p, v = b.fluid(r, g["step3_fluid_pos"].shape[0])
+    dp = np.abs(periodic_diff(p, g["step3_fluid_pos"], L)).max(axis=1)
+    dv = np.abs(v - g["step3_fluid_vel"]).max(axis=1)
+    assert np.mean(dp < 2e-4) > 0.999, np.sort(dp)[-3:]
+    assert np.mean(dv < 2e-4) > 0.995, np.sort(dv)[-3:]
+    assert b.status(r)["steps"] == 3 and b.status(other)["steps"] == 3
+    # a missing Gamma variate for a thermostatted cell is reported
+    b.set_steps(r, 1)
+    with pytest.raises(cg.MpcdError, match="gamma"):
+        b.step_inject(r, g["shift_1"], np.full_like(g["gamma_1"], -1.0), g["axis_1"])
+    b.close()
+
+
+def test_swimmer_replica_with_injected_randomness_tracks_reference():
+    """A Clami replica (the batch's split-arithmetic cluster MD) on the
+    reference's recorded randomness against its trajectory
+    (tests/golden/clami10.npz): beads within 1e-3 after 4 MPC steps of 50
+    substeps, as the single-box split-arithmetic MD."""
+    from conftest import GOLDEN, golden
+
+    g = golden("clami10")
+    text = open(f"{GOLDEN}/cases/clami10.cfg").read()
+    b = make_batch([dict(L=10, n_cilia=4, rodlength=6)])
+    r = b.add_cfg(text, seed=3, ststep=0.002, create_fluid=False)
+    b.set_fluid(r, g["step0_fluid_pos"], g["step0_fluid_vel"])
+    b.set_shift(r, g["shift_0"])
+    b.admit(r)
+    b.set_steps(r, 4)
+    for k in range(1, 5):
+        b.step_inject(r, g[f"shift_{k}"], g[f"gamma_{k}"], g[f"axis_{k}"])
+    rp = ref_bead_pos(g, "step4")
+    bp, _ = b.beads(r, rp.shape[0])
+    assert np.abs(bp - rp).max() < 1e-3, np.abs(bp - rp).max()
+    p, v = b.fluid(r, g["step4_fluid_pos"].shape[0])
+    dp = np.abs(periodic_diff(p, g["step4_fluid_pos"], 10)).max(axis=1)
+    assert np.mean(dp < 2e-4) > 0.999, np.sort(dp)[-3:]
+    b.close()
