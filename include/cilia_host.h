@@ -58,6 +58,14 @@ long cilia_sim_bead_count(const cilia_sim* s);
 int cilia_sim_next_tstep(cilia_sim* s, const mpcd_inject* inj);
 int cilia_sim_run(cilia_sim* s);
 int cilia_sim_save(cilia_sim* s);
+/* The writes of Simulation::run after a measure interval (src/simulation.cpp:
+ * 103-107), in the working directory: flags bit 0, every object's writedata
+ * (Clami::writedata, src/clami.cpp:208-284: <name>.xyz frame and <name>.san
+ * row; the dissipated energy is cleared afterwards); bit 1, MPCD::debug's row
+ * of mpcd.san (src/libcilia/mpcd.cpp:404-467). */
+#define CILIA_WRITE_OBJECTS 1
+#define CILIA_WRITE_DEBUG 2
+int cilia_sim_writedata(cilia_sim* s, int flags);
 /* Builds the system a sim.cfg describes on the host only (objects, springs,
  * cilia, the fluid of Fluid::create or fluid_n.dat, the grid shift) and adds
  * it to a replica batch as a new replica, not yet admitted (mpcd_batch_admit).

@@ -198,6 +198,21 @@ int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* la
  * 3 float springs on the double-float layout). */
 int mpcd_md_layout(mpcd_engine* h, int* info);
 
+/* Lossless snapshots of a handle's whole state, for checkpoints that keep
+ * every bit (the reference's own checkpoint files, which `cilia` writes and
+ * reads as well, round the fluid to 7 digits: src/libcilia/fluid.cpp:100-108)
+ * and for moving a run between handles: fluid in the engine's own layout,
+ * beads, springs, cilia and their beat state, grid shift, time, step counter
+ * and generator seed, dissipated energy, rigid spheres.  mpcd_snapshot_size
+ * gives the bytes; mpcd_snapshot fills a host buffer of at least that size;
+ * mpcd_restore loads one into a handle created with the same box, precision,
+ * tstep and ststep (MPCD_EINVAL otherwise) and replaces its state.  The first
+ * step after a restore bins the particles again, so a restored run continues
+ * the original one to the order of floating-point additions into cell sums. */
+int mpcd_snapshot_size(mpcd_engine* h, long long* bytes);
+int mpcd_snapshot(mpcd_engine* h, void* buf, long long bytes);
+int mpcd_restore(mpcd_engine* h, const void* buf, long long bytes);
+
 /* ----------------------------------------------------------------------------
  * Rigid spheres with no-slip bounce-back.  The reference's bounce-back
  * surfaces are the planar walls of -DNOSLIP (streaming reflection,
@@ -235,6 +250,7 @@ typedef struct {
 int mpcd_set_rigid_spheres(mpcd_engine* h, int n, const mpcd_rigid_sphere* spheres);
 int mpcd_get_rigid_spheres(mpcd_engine* h, int n, mpcd_rigid_sphere* spheres, double* force_torque);
 int mpcd_reset_rigid_sphere_forces(mpcd_engine* h);
+int mpcd_rigid_sphere_count(const mpcd_engine* h);
 
 /* The counter-based generator's collision draws, for checking them against
  * the reference's samplers: for cells k = 0 .. n-1 of step `step` under

@@ -147,9 +147,13 @@ def lib():
             "mpcd_md_layout": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
             "mpcd_fluid_step_noalloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.c_long, P, P, _D, _DP, _DP,
                                                        ctypes.c_ulonglong, ctypes.c_ulonglong, _DP, P]),
+            "mpcd_snapshot_size": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
+            "mpcd_snapshot": (ctypes.c_int, [P, ctypes.c_void_p, ctypes.c_longlong]),
+            "mpcd_restore": (ctypes.c_int, [P, ctypes.c_void_p, ctypes.c_longlong]),
             "mpcd_set_rigid_spheres": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdRigidSphere)]),
             "mpcd_get_rigid_spheres": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdRigidSphere), _DP]),
             "mpcd_reset_rigid_sphere_forces": (ctypes.c_int, [P]),
+            "mpcd_rigid_sphere_count": (ctypes.c_int, [P]),
             "mpcd_collision_draws": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_long,
                                                     _DP, _DP, ctypes.c_int]),
             "mpcd_batch_step_inject": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdInject)]),
@@ -214,6 +218,7 @@ def lib():
             "cilia_sim_next_tstep": (ctypes.c_int, [P, ctypes.POINTER(MpcdInject)]),
             "cilia_sim_run": (ctypes.c_int, [P]),
             "cilia_sim_save": (ctypes.c_int, [P]),
+            "cilia_sim_writedata": (ctypes.c_int, [P, ctypes.c_int]),
             "cilia_sim_write_cfg": (ctypes.c_int, [P, ctypes.c_char_p]),
         }
         for name, (res, args) in sig.items():
@@ -378,6 +383,19 @@ class Engine:
         self._ck(lib().mpcd_kernel_time(self._h, int(kernel), ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
         return ms.value, n.value
 
+    def snapshot(self):
+        """The handle's whole state as bytes (mpcd_snapshot)."""
+        n = ctypes.c_longlong()
+        self._ck(lib().mpcd_snapshot_size(self._h, ctypes.byref(n)), "snapshot_size")
+        buf = ctypes.create_string_buffer(n.value)
+        self._ck(lib().mpcd_snapshot(self._h, buf, n.value), "snapshot")
+        return buf.raw
+
+    def restore(self, data):
+        """Replace the handle's state by a snapshot (mpcd_restore)."""
+        buf = ctypes.create_string_buffer(bytes(data), len(data))
+        self._ck(lib().mpcd_restore(self._h, buf, len(data)), "restore")
+
     def set_rigid_spheres(self, spheres):
         """Rigid no-slip spheres: dicts with center, radius and optional velocity,
         omega, mass (> 0 free, <= 0 or absent held)."""
@@ -389,11 +407,10 @@ class Engine:
             arr[k].radius = float(sp["radius"])
             arr[k].mass = float(sp.get("mass", 0.0))
         self._ck(lib().mpcd_set_rigid_spheres(self._h, len(spheres), arr), "set_rigid_spheres")
-        self._nsph = len(spheres)
 
     def rigid_spheres(self):
         """(list of sphere dicts, mean force and torque [n, 6] since the last reset)."""
-        n = getattr(self, "_nsph", 0)
+        n = lib().mpcd_rigid_sphere_count(self._h)
         arr = (MpcdRigidSphere * max(n, 1))()
         ft = np.zeros((max(n, 1), 6))
         self._ck(lib().mpcd_get_rigid_spheres(self._h, n, arr, _dp(ft)), "get_rigid_spheres")
@@ -472,6 +489,10 @@ class Sim:
 
     def save(self):
         self._ck(lib().cilia_sim_save(self._h), "save")
+
+    def writedata(self, objects=True, debug=False):
+        """The writes of a measure interval (cilia_sim_writedata) in the working directory."""
+        self._ck(lib().cilia_sim_writedata(self._h, int(objects) | (2 if debug else 0)), "writedata")
 
     def write_cfg(self, path):
         self._ck(lib().cilia_sim_write_cfg(self._h, path.encode()), "write_cfg")

@@ -83,6 +83,9 @@ struct StepArgs {
   // float copies for the split-precision kernels (no conversions per thread)
   float fta_cur[3], fta_next[3], fh, fgkick, fbead_mass;
   SphereSet sph;      // rigid spheres (n = 0: none)
+  // 1: the maps of the cells holding beads were made by launch_bead_maps
+  // this step; the cell-map kernel only clears those cells' sums
+  int premapped = 0;
 };
 
 // ------------------------------------------------------------------- MD ---
@@ -183,6 +186,13 @@ struct MDStepArgs {
   // as the separate bead kernel would) and subtracts their m v'^2 from *diss
   int collide = 0;
   double* diss = nullptr;
+  // 1: the beads' final binning goes to bcell / bsum per slot (the cell and
+  // its m v, m v^2), added to the cell sums by launch_bead_add after the
+  // launch, instead of straight into the cell sums (which the cell-map kernel
+  // may still be reading and clearing while the MD runs)
+  int deferred = 0;
+  uint32_t* bcell = nullptr;
+  void* bsum = nullptr;  // double4 per slot (float64 cells) or float4 (split)
 };
 
 // ------------------------------------------------------------ launchers ---
@@ -235,6 +245,17 @@ int launch_sort_f32(FluidF32& f, FluidF32& tmp, const Box& box, uint32_t* count,
 // axes of cells 0 .. n-1 in step `step` (either output may be null)
 int launch_collision_draws(int nc, uint64_t seed, uint64_t step, long n, double* gamma, double* axis, unsigned* err,
                            cudaStream_t s);
+// Bead-first ordering of a step (the MD launch starts before the cell maps of
+// the fluid): the collision maps of the cells that hold moving beads, each
+// made once (claim[cid] takes this step's tag), ahead of the cell-map kernel
+// (StepArgs::premapped); and after the MD launch the beads' deferred binning
+// (MDStepArgs::deferred) added into the cell sums.
+int launch_bead_maps_f64(const MDState& m, const CellsF64& c, const StepArgs& a, uint32_t* claim, uint32_t tag,
+                         cudaStream_t s);
+int launch_bead_maps_f32(const MDState& m, const CellsF32& c, const StepArgs& a, uint32_t* claim, uint32_t tag,
+                         cudaStream_t s);
+int launch_bead_add_f64(const MDState& m, const CellsF64& c, const uint32_t* bcell, const void* bsum, cudaStream_t s);
+int launch_bead_add_f32(const MDState& m, const CellsF32& c, const uint32_t* bcell, const void* bsum, cudaStream_t s);
 // rigid spheres after a step: force sums, motion, impulses cleared (one CTA)
 int launch_spheres_update(RigidSphereDev* sph, int n, double* acc, double* fsum, double h, const Box& box,
                           cudaStream_t s);

@@ -270,6 +270,7 @@ __global__ void k_cell_params_f64(CellsF64 c, StepArgs a) {
     const double4 s = c.sum[cid];
     c.sum[cid] = make_double4(0.0, 0.0, 0.0, 0.0);
     c.cnt[cid] = 0u;
+    if (a.premapped && cnt_beads(w) > 0) continue;  // mapped by k_bead_maps_f64
     double A[9], b[3];
     collision_map(s, w, cid, a, A, b, ldiss, errbits, gfail);
     double2* p = reinterpret_cast<double2*>(c.par + 12 * cid);
@@ -317,15 +318,18 @@ __device__ __forceinline__ void wall_bounce(int walls, double ztop, double& x, d
 }
 
 // I: particle index type (32-bit whenever the particle count allows, so that
-// no 64-bit integer work competes with the float64 arithmetic)
-template <typename I>
+// no 64-bit integer work competes with the float64 arithmetic).
+// kBoundary: walls or rigid spheres, streaming in unwrapped coordinates with
+// bounce-back; a separate instantiation, so that the common periodic pass
+// keeps the registers (about 60) that let its CTAs share the SMs with the MD
+// launch (the sphere bounce-back alone takes the kernel to over 100).
+template <typename I, bool kBoundary>
 __global__ void __launch_bounds__(kThreads) k_fluid_step_f64(FluidF64 f, CellsF64 c, StepArgs a) {
   const int Lx = a.box.L[0], Ly = a.box.L[1], Lz = a.box.L[2];
   const Thresh tcx = thresh(a.ta_cur[0]), tcy = thresh(a.ta_cur[1]), tcz = thresh(a.ta_cur[2]);
   const Thresh tnx = thresh(a.ta_next[0]), tny = thresh(a.ta_next[1]), tnz = thresh(a.ta_next[2]);
   const double h = a.h, gk = a.gkick;
-  // walls or rigid spheres: streaming in unwrapped coordinates with bounce-back
-  const bool kick = gk != 0.0, walls = a.walls != 0 || a.sph.n > 0;
+  const bool kick = gk != 0.0, walls = kBoundary;
   const I n = (I)f.n;
   double ke_after = 0.0;
   unsigned bad = 0;
@@ -709,6 +713,7 @@ __global__ void k_cell_params_f32(CellsF32 c, StepArgs a) {
       const long cid = cb + u * stride;
       c.sum[cid] = make_float4(0.f, 0.f, 0.f, 0.f);
       c.cnt[cid] = 0u;
+      if (a.premapped && cnt_beads(w[u]) > 0) continue;  // mapped by k_bead_maps_f32
       cell_map_f32(sm[u], w[u], (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 2 * cid,
                    ldiss, errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt, &a);
     }
@@ -731,8 +736,11 @@ template <int U>
 struct FluidMinBlocks {
   static constexpr int value = U >= 4 ? 2 : 4;
 };
-// default options of the split-precision fluid pass (kOptPrefetch | kOptAggregate bits)
-constexpr int kFluidOpt = 0;
+// default options of the split-precision fluid pass (kOptPrefetch | kOptAggregate
+// bits): both (2.62 M particles, persistent grid: 45.8 us against 49.2 us
+// without either, 50.4 with the prefetch alone, 49.1 with the aggregation
+// alone; the same order with one particle per thread)
+constexpr int kFluidOpt = 3;
 
 // Options of the split-precision fluid pass (bits of kOpt):
 //   kOptPrefetch  one thread per CTA and round sends the particle state of the
@@ -1061,6 +1069,90 @@ __global__ void k_store_fluid_f32(FluidF32 f, double* pos, double* vel, unsigned
   }
 }
 
+// The collision maps of the cells holding moving beads (the same map
+// k_cell_params_* would make from the same sums and generator keys), one
+// thread per bead slot; the first bead of a cell to take the cell's claim
+// word with this step's tag makes it.  The sums are left for the cell-map
+// kernel to clear.
+__global__ void k_bead_maps_f64(MDState m, CellsF64 c, StepArgs a, uint32_t* claim, uint32_t tag) {
+  double ldiss = 0.0;
+  unsigned errbits = 0;
+  bool gfail = false;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const long cid = unwrapped_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    if (cid < 0) {
+      errbits |= kErrCellRange;
+      continue;
+    }
+    if (atomicExch(claim + cid, tag) == tag) continue;  // another bead of the cell makes it
+    const uint32_t w = c.cnt[cid];
+    if (w == 0) continue;
+    double A[9], b[3];
+    collision_map(c.sum[cid], w, cid, a, A, b, ldiss, errbits, gfail);
+    double2* p = reinterpret_cast<double2*>(c.par + 12 * cid);
+    p[0] = make_double2(A[0], A[1]);
+    p[1] = make_double2(A[2], A[3]);
+    p[2] = make_double2(A[4], A[5]);
+    p[3] = make_double2(A[6], A[7]);
+    p[4] = make_double2(A[8], b[0]);
+    p[5] = make_double2(b[1], b[2]);
+  }
+  if (gfail) errbits |= kErrGammaLoop;
+  if (errbits) atomicOr(a.err, errbits);
+  const double tot = block_sum_f64(ldiss);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
+}
+
+__global__ void k_bead_maps_f32(MDState m, CellsF32 c, StepArgs a, uint32_t* claim, uint32_t tag) {
+  float ldiss = 0.0f;
+  unsigned errbits = 0;
+  bool gfail = false;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const long cid = unwrapped_cell(a.box, a.a_cur, m.x[0][s], m.y[0][s], m.z[0][s]);
+    if (cid < 0) {
+      errbits |= kErrCellRange;
+      continue;
+    }
+    if (atomicExch(claim + cid, tag) == tag) continue;
+    const uint32_t w = c.cnt[cid];
+    if (w == 0) continue;
+    cell_map_f32(c.sum[cid], w, (uint32_t)cid, a.seed, a.step, a.fbead_mass, a.inj_gamma, a.inj_axis, c.par + 2 * cid,
+                 ldiss, errbits, gfail, a.walls != 0 && wall_layer_cell(a.box, cid), a.inj_virt, &a);
+  }
+  if (gfail) errbits |= kErrGammaLoop;
+  if (errbits) atomicOr(a.err, errbits);
+  const double tot = block_sum_f32(ldiss);
+  if (threadIdx.x == 0 && tot != 0.0) atomicAdd(a.diss, tot);
+}
+
+// the MD launch's deferred bead binning into the cell sums
+__global__ void k_bead_add_f64(MDState m, CellsF64 c, const uint32_t* bcell, const double4* bsum) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const uint32_t cid = bcell[s];
+    if (cid == 0xffffffffu) continue;
+    const double4 v = bsum[s];
+    double* sp = reinterpret_cast<double*>(c.sum + cid);
+    atomicAdd(sp + 0, v.x);
+    atomicAdd(sp + 1, v.y);
+    atomicAdd(sp + 2, v.z);
+    atomicAdd(sp + 3, v.w);
+    atomicAdd(c.cnt + cid, 1u << 16);
+  }
+}
+
+__global__ void k_bead_add_f32(MDState m, CellsF32 c, const uint32_t* bcell, const float4* bsum) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += gridDim.x * blockDim.x) {
+    if (m.moves[s] != 1) continue;
+    const uint32_t cid = bcell[s];
+    if (cid == 0xffffffffu) continue;
+    red_add_v4(c.sum + cid, bsum[s]);
+    atomicAdd(c.cnt + cid, 1u << 16);
+  }
+}
+
 // Rigid spheres after a step: the impulse and angular impulse the fluid gave
 // them this step are added to the running force and torque sums (divided by
 // h) and cleared; every sphere moves with the velocity it had during the
@@ -1106,6 +1198,29 @@ __global__ void k_collision_draws(int nc, uint64_t seed, uint64_t step, long n, 
 
 // ============================================================ launchers ===
 
+int launch_bead_maps_f64(const MDState& m, const CellsF64& c, const StepArgs& a, uint32_t* claim, uint32_t tag,
+                         cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bead_maps_f64<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, a, claim, tag);
+  return 1;
+}
+int launch_bead_maps_f32(const MDState& m, const CellsF32& c, const StepArgs& a, uint32_t* claim, uint32_t tag,
+                         cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bead_maps_f32<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, a, claim, tag);
+  return 1;
+}
+int launch_bead_add_f64(const MDState& m, const CellsF64& c, const uint32_t* bcell, const void* bsum, cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bead_add_f64<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, bcell, static_cast<const double4*>(bsum));
+  return 1;
+}
+int launch_bead_add_f32(const MDState& m, const CellsF32& c, const uint32_t* bcell, const void* bsum, cudaStream_t s) {
+  if (m.nslots == 0) return 0;
+  k_bead_add_f32<<<grid_for(m.nslots), kThreads, 0, s>>>(m, c, bcell, static_cast<const float4*>(bsum));
+  return 1;
+}
+
 int launch_spheres_update(RigidSphereDev* sph, int n, double* acc, double* fsum, double h, const Box& box,
                           cudaStream_t s) {
   if (n <= 0) return 0;
@@ -1127,10 +1242,13 @@ int launch_cell_params_f64(const CellsF64& c, const StepArgs& a, cudaStream_t s)
 int launch_fluid_step_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s, int per_sm) {
   if (f.n == 0) return 0;
   const int grid = grid_for(f.n, kThreads, per_sm);
-  if (f.n + (long)grid * kThreads < (1L << 32))
-    k_fluid_step_f64<uint32_t><<<grid, kThreads, 0, s>>>(f, c, a);
+  const bool i32 = f.n + (long)grid * kThreads < (1L << 32);
+  if (a.walls != 0 || a.sph.n > 0)
+    i32 ? k_fluid_step_f64<uint32_t, true><<<grid, kThreads, 0, s>>>(f, c, a)
+        : k_fluid_step_f64<long, true><<<grid, kThreads, 0, s>>>(f, c, a);
   else
-    k_fluid_step_f64<long><<<grid, kThreads, 0, s>>>(f, c, a);
+    i32 ? k_fluid_step_f64<uint32_t, false><<<grid, kThreads, 0, s>>>(f, c, a)
+        : k_fluid_step_f64<long, false><<<grid, kThreads, 0, s>>>(f, c, a);
   return 1;
 }
 int launch_bin_fluid_f64(const FluidF64& f, const CellsF64& c, const StepArgs& a, cudaStream_t s) {

@@ -139,6 +139,14 @@ int cilia_sim_run(cilia_sim* s) {
   });
 }
 
+int cilia_sim_writedata(cilia_sim* s, int flags) {
+  if (!s || flags < 0 || flags > 3) return MPCD_EINVAL;
+  return guarded(s->error, [&]() {
+    s->sim->write_measure((flags & 1) != 0, (flags & 2) != 0);
+    return MPCD_OK;
+  });
+}
+
 int cilia_sim_save(cilia_sim* s) {
   if (!s) return MPCD_EINVAL;
   return guarded(s->error, [&]() {

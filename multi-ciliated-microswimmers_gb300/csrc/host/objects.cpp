@@ -685,12 +685,27 @@ Simulation::Simulation(const libconfig::Setting& root, const SimOptions& o) : op
     check(mpcd_create(&p, &eng), eng, "mpcd_create");
     mpcd_set_time(eng, wc.globalt);
   }
-  // MPCD::MPCD: grid shift from mpcd.dat or three draws (src/libcilia/mpcd.cpp:86-97)
-  double a[3];
+  // MPCD::MPCD: grid shift from mpcd.dat or three draws (src/libcilia/mpcd.cpp:86-97).
+  // When the file exists the reference draws nothing and reads three values
+  // with plain stream extraction; its destructor writes the address of the
+  // shift array (mpcd.cpp:396-403, `out << a` of a double*), from which the
+  // first extraction reads 0 and the next fails, leaving 0 and then an
+  // unset value.  Here every value a failed extraction leaves is 0, so such a
+  // file gives the shift (0, 0, 0); a shift outside [0, 1) is wrapped into it
+  // (the same cell partition, renumbered).
+  double a[3] = {0.0, 0.0, 0.0};
   bool have = false;
   if (opt.read_files) {
     std::ifstream in("mpcd.dat");
-    if (in >> a[0] >> a[1] >> a[2]) have = a[0] >= 0 && a[0] < 1 && a[1] >= 0 && a[1] < 1 && a[2] >= 0 && a[2] < 1;
+    if (in.good()) {
+      have = true;
+      for (double& q : a) {
+        if (!(in >> q)) q = 0.0;
+        if (!std::isfinite(q)) q = 0.0;
+        q -= std::floor(q);
+        if (q >= 1.0) q = 0.0;
+      }
+    }
   }
   if (!have)
     for (double& q : a) q = rng->rnd();
@@ -919,6 +934,29 @@ void Simulation::debug(const char* path) {
        << o.momentum[1] << " " << o.momentum[2] << " " << o.kT << "\n";
 }
 
+// What Simulation::run writes after a measure interval (src/simulation.cpp:
+// 103-107): every object's writedata (a Clami's dissipated power from the
+// energy the thermostat removed since the last interval, which is then
+// cleared, as Clami::writedata clears MPCD::diss_energy_total); with
+// debug_row, then MPCD::debug's line in mpcd.san.
+void Simulation::write_measure(bool objects, bool debug_row) {
+  mpcd_obs o{};
+  check(mpcd_observables(eng, &o), eng, "mpcd_observables");
+  sync_from_device();
+  if (objects) {
+    for (auto& obj : md_objects) {
+      if (Clami* c = dynamic_cast<Clami*>(obj.get())) {
+        c->diss_energy_interval = o.diss_energy;
+        c->tstep = wc.tstep;
+        c->measureinterval = wc.measureinterval;
+      }
+      obj->writedata(wc.globalt);
+    }
+    check(mpcd_reset_diss(eng), eng, "mpcd_reset_diss");
+  }
+  if (debug_row) debug("mpcd.san");
+}
+
 void Simulation::write_fluid_temp(const char* path) {
   mpcd_obs o{};
   check(mpcd_observables(eng, &o), eng, "mpcd_observables");
@@ -938,18 +976,7 @@ void Simulation::run() {
   while (wc.globalt < wc.desiredt) {
     const auto t0 = clk::now();
     for (int s = 0; s < wc.measureinterval; ++s) check(next_tstep(nullptr), eng, "mpcd_step");
-    mpcd_obs o{};
-    check(mpcd_observables(eng, &o), eng, "mpcd_observables");
-    sync_from_device();
-    for (auto& obj : md_objects) {
-      if (Clami* c = dynamic_cast<Clami*>(obj.get())) {
-        c->diss_energy_interval = o.diss_energy;
-        c->tstep = wc.tstep;
-        c->measureinterval = wc.measureinterval;
-      }
-      obj->writedata(wc.globalt);
-    }
-    mpcd_reset_diss(eng);
+    write_measure(true, false);
     const double ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
     std::cout << "T =" << wc.globalt;
     if (ms > 0) std::cout << " (" << 1000.0 * wc.tstep * wc.measureinterval / ms << "fps)";

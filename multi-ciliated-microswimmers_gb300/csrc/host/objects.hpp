@@ -228,6 +228,7 @@ class Simulation {
   long nbeads = 0;
 
   MDObject* add_md_object(const libconfig::Setting& cfg);
+  void write_measure(bool objects, bool debug_row);
   void add_md_object(MDObject* obj);  // takes ownership
   void upload_md();                  // beads + springs + cilia to the engine
   void sync_from_device();           // bead state back into the objects

@@ -173,6 +173,19 @@ struct BinF64 {
     atomicAdd(sp + 3, mb * (vx * vx + vy * vy + vz * vz));
     atomicAdd(c.cnt + cid, 1u << 16);
   }
+  // the same contribution kept per slot (MDStepArgs::deferred)
+  __device__ void defer(int slot, double x, double y, double z, double vx, double vy, double vz) const {
+    const long cid = unwrapped_cell(a->box, a->a_next, x, y, z);
+    uint32_t* bc = a->bcell;
+    if (cid < 0) {
+      atomicOr(a->err, kErrCellRange);
+      bc[slot] = 0xffffffffu;
+      return;
+    }
+    const double mb = a->bead_mass;
+    bc[slot] = (uint32_t)cid;
+    static_cast<double4*>(a->bsum)[slot] = make_double4(vx * mb, vy * mb, vz * mb, mb * (vx * vx + vy * vy + vz * vz));
+  }
 };
 
 struct BinF32 {
@@ -207,6 +220,20 @@ struct BinF32 {
     atomicAdd(sp + 2, fvz * mb);
     atomicAdd(sp + 3, mb * (fvx * fvx + fvy * fvy + fvz * fvz));
     atomicAdd(c.cnt + cid, 1u << 16);
+  }
+  // the same contribution kept per slot (MDStepArgs::deferred)
+  __device__ void defer(int slot, double x, double y, double z, double vx, double vy, double vz) const {
+    const long cid = unwrapped_cell(a->box, a->a_next, x, y, z);
+    uint32_t* bc = a->bcell;
+    if (cid < 0) {
+      atomicOr(a->err, kErrCellRange);
+      bc[slot] = 0xffffffffu;
+      return;
+    }
+    const float mb = (float)a->bead_mass;
+    const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+    bc[slot] = (uint32_t)cid;
+    static_cast<float4*>(a->bsum)[slot] = make_float4(fvx * mb, fvy * mb, fvz * mb, mb * (fvx * fvx + fvy * fvy + fvz * fvz));
   }
 };
 

@@ -560,7 +560,12 @@ __device__ void md_df_body(const MDState& m, const MDStepArgs& a, Bin bin) {
     m.vx[oslot] = VX;
     m.vy[oslot] = VY;
     m.vz[oslot] = VZ;
-    if (omoves) bin(X, Y, Z, VX, VY, VZ);
+    if (omoves) {
+      if (a.deferred)
+        bin.defer(oslot, X, Y, Z, VX, VY, VZ);
+      else
+        bin(X, Y, Z, VX, VY, VZ);
+    }
   }
   // refreshed bonds back to float64
   if (refreshed) {

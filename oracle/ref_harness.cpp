@@ -21,6 +21,11 @@
 //       build, the virtual-particle momentum of wall-layer cells), and checks
 //       afterwards that the real step consumed exactly those draws.  It writes
 //       raw little-endian float64 arrays plus index.txt into <outdir>.
+//   ref_harness run ... <dump_list> <write_list>
+//       also calls every object's writedata (Clami: <name>.xyz and <name>.san,
+//       src/clami.cpp:208-284) and MPCD::debug (mpcd.san, src/libcilia/mpcd.cpp:
+//       404-467) after the steps of <write_list>, as Simulation::run does after
+//       a measure interval (src/simulation.cpp:76-107).
 #include <omp.h>
 #include <sys/stat.h>
 #include <unistd.h>
@@ -203,11 +208,16 @@ int run_mode(int argc, char** argv) {
   unsigned long seed = std::strtoul(argv[4], nullptr, 10);
   int nsteps = std::atoi(argv[5]);
   double ststep = std::atof(argv[6]);
-  std::vector<int> dumps;
+  std::vector<int> dumps, writes;
   {
     std::stringstream ss(argv[7]);
     std::string tok;
     while (std::getline(ss, tok, ',')) dumps.push_back(std::atoi(tok.c_str()));
+  }
+  if (argc > 8) {
+    std::stringstream ss(argv[8]);
+    std::string tok;
+    while (std::getline(ss, tok, ',')) writes.push_back(std::atoi(tok.c_str()));
   }
   char absbuf[4096];
   if (realpath(cfgpath.c_str(), absbuf) == nullptr) {
@@ -263,6 +273,10 @@ int run_mode(int argc, char** argv) {
     out.put("shift_" + std::to_string(s), a, {3});
     if (std::find(dumps.begin(), dumps.end(), s) != dumps.end())
       dump_state(out, *sim, "step" + std::to_string(s));
+    if (std::find(writes.begin(), writes.end(), s) != writes.end()) {
+      for (size_t k = 0; k < sim->md_objects.size(); ++k) sim->md_objects[k]->writedata();
+      sim->mpcd.debug();
+    }
   }
   double okv = ok;
   out.put("replay_ok", &okv, {1});

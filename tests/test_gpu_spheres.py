@@ -8,9 +8,10 @@ spheres (mpcd_set_rigid_spheres).  Its parity is pinned three ways:
   * planar limit: two held spheres of radius 1e7 whose surfaces pass through
     z = 0 and z = Lz - 1 stand for the no-slip walls; on the same injected
     randomness (grid shifts, Gamma variates, rotation axes and the virtual
-    particles' momenta) the fluid of the lower half matches the walls path
-    to 1e-6 (the surface's curvature over the box, 8e-7, and the float64
-    cancellation of a 1e7 radius bound the difference);
+    particles' momenta) the fluid of the lower half matches the walls path:
+    velocities to round-off, positions exactly except for the reflected
+    particles, which the surface's height over the plane (at most 1.6e-6
+    across the box) moves by up to 1e-3 for grazing incidence;
   * conservation: a free sphere exchanges momentum with the fluid only, so
     fluid + sphere momentum stays constant to round-off (float64 sums;
     float32 split: to its float rounding);
@@ -82,9 +83,16 @@ def test_planar_limit_matches_walls_path():
     ps, vs = sph.fluid()
     low = pw[:, 2] < 6.0
     assert low.sum() > 2000
-    dp = np.abs(periodic_diff(ps[low], pw[low], L)).max()
+    dp = np.abs(periodic_diff(ps[low], pw[low], L)).max(axis=1)
     dv = np.abs(vs[low] - vw[low]).max()
-    assert dp < 1e-6 and dv < 1e-6, (dp, dv)
+    # no-slip bounce-back reverses the velocity whatever the surface's tilt:
+    # velocities agree to round-off; a reflected particle's position moves by
+    # 2 |v| dz / |v_z| with dz <= (4^2 + 4^2) / (2 R) = 1.6e-6 the height of
+    # the curved surface over the plane, large only for grazing particles;
+    # every other particle is untouched by the curvature
+    assert dv < 1e-12, dv
+    assert dp.max() < 1e-3, dp.max()
+    assert np.mean(dp < 1e-12) > 0.95, np.mean(dp < 1e-12)
     # the bottom surface did reflect particles in both
     assert np.all(ps[low, 2] >= -1e-6)
 
