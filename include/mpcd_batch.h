@@ -104,6 +104,12 @@ int mpcd_batch_status(mpcd_batch* b, int r, long long* steps_done, long long* st
 int mpcd_batch_get_fluid(mpcd_batch* b, int r, long n, double* pos, double* vel);
 int mpcd_batch_get_beads(mpcd_batch* b, int r, long nb, double* pos, double* vel);
 int mpcd_batch_get_shift(mpcd_batch* b, int r, double* a3);
+/* per cilium [midpnt, tstroke] and the bond tables (any may be NULL), as mpcd_get_cilia */
+int mpcd_batch_get_cilia(mpcd_batch* b, int r, int nc, double* state2, double* newlength, double* oldlength);
+/* collisions the replica has done (the step counter that keys its random
+ * numbers), before admission: a replica rebuilt from another's state
+ * continues that one's random sequence */
+int mpcd_batch_set_step_count(mpcd_batch* b, int r, long long steps_done);
 int mpcd_batch_observables(mpcd_batch* b, int r, mpcd_obs* out);
 /* frees the replica's device ranges and its slot */
 int mpcd_batch_remove(mpcd_batch* b, int r);

@@ -252,6 +252,18 @@ int mpcd_get_rigid_spheres(mpcd_engine* h, int n, mpcd_rigid_sphere* spheres, do
 int mpcd_reset_rigid_sphere_forces(mpcd_engine* h);
 int mpcd_rigid_sphere_count(const mpcd_engine* h);
 
+/* Contact forces between cilia: GlobalForces::recalc_forces / vdw_force of
+ * the reference built with -DREPELLING=eps (src/libcilia/globalforces.cpp:
+ * 22-95; cutoff 1.5, stride N = 4): a harmonic repulsion of the section
+ * centroids of two cilia closer than the cutoff, F = -2 eps (1 - 1.5 / |d|) d,
+ * added to the three beads of each section, in every MD force evaluation,
+ * over the cilia in mpcd_set_cilia order.  (The reference's own code for it
+ * does not compile: it names a `cilias` list that its class does not
+ * declare.)  eps = 0 turns it off.  With eps != 0 the MD substeps run on the
+ * float64 grid kernel, whatever mpcd_params.md_split says; cilia of at most 64
+ * beads per filament. */
+int mpcd_set_repelling(mpcd_engine* h, double eps);
+
 /* The counter-based generator's collision draws, for checking them against
  * the reference's samplers: for cells k = 0 .. n-1 of step `step` under
  * `seed`, gamma[k] is the Gamma(3(nc-1)/2, 1) variate a free-running step

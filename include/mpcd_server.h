@@ -33,6 +33,9 @@ typedef struct {
   int keep_fluid;           /* 1: a finished request keeps its fluid state for mpcd_server_result_fluid */
   int lookahead;            /* queued requests considered per round (0: 16) */
   int prep_threads;         /* host threads building requests from their cfg (0: 2) */
+  double preempt_wait_s;    /* > 0: when the oldest waiting request has waited this long, the
+                               resident request with the most steps left (more than it needs) is
+                               pre-empted (0: never) */
 } mpcd_server_params;
 
 #define MPCD_REQ_QUEUED 0
@@ -49,6 +52,7 @@ typedef struct {
   long long footprint;     /* device bytes while resident */
   mpcd_obs obs;            /* observables at completion */
   unsigned err_bits;       /* device check bits of the replica */
+  int preemptions;         /* times it was pre-empted */
 } mpcd_request_info;
 
 typedef struct {
@@ -60,6 +64,7 @@ typedef struct {
   long long peak_resident_bytes;
   int peak_resident;
   long long gpu_launches;
+  long long preemptions;
 } mpcd_server_stats;
 
 int mpcd_server_create(const mpcd_server_params* p, mpcd_server** out);
@@ -76,6 +81,14 @@ int mpcd_server_drain(mpcd_server* s, double timeout_s);
 int mpcd_server_result_beads(mpcd_server* s, long long id, long nb, double* pos, double* vel);
 int mpcd_server_result_fluid(mpcd_server* s, long long id, long n, double* pos, double* vel);
 int mpcd_server_get_stats(mpcd_server* s, mpcd_server_stats* out);
+/* Pre-empts a resident request at the end of the current round: its state
+ * (fluid, beads, cilia beat state, grid shift, time, step counter) is read
+ * back to the host, its device ranges are freed, and it waits at the head of
+ * the queue; admitted again, it resumes from that state with the same random
+ * sequence, so its result is that of an uninterrupted run up to the order of
+ * float additions into cell sums (its dissipated energy counts from the
+ * resumption).  MPCD_ESTATE if it is not resident. */
+int mpcd_server_preempt(mpcd_server* s, long long id);
 /* why a request failed ("" otherwise); valid until the server is destroyed */
 const char* mpcd_server_request_error(mpcd_server* s, long long id);
 

@@ -76,14 +76,15 @@ class MpcdBatchTuning(ctypes.Structure):
 
 class MpcdServerParams(ctypes.Structure):
     _fields_ = [("batch", MpcdBatchParams), ("budget_bytes", ctypes.c_longlong), ("chunk_steps", ctypes.c_int),
-                ("keep_fluid", ctypes.c_int), ("lookahead", ctypes.c_int), ("prep_threads", ctypes.c_int)]
+                ("keep_fluid", ctypes.c_int), ("lookahead", ctypes.c_int), ("prep_threads", ctypes.c_int),
+                ("preempt_wait_s", _D)]
 
 
 class MpcdRequestInfo(ctypes.Structure):
     _fields_ = [("id", ctypes.c_longlong), ("state", ctypes.c_int), ("steps", ctypes.c_longlong),
                 ("t_submit", _D), ("t_admit", _D), ("t_done", _D), ("nfluid", ctypes.c_longlong),
                 ("nbeads", ctypes.c_longlong), ("footprint", ctypes.c_longlong), ("obs", MpcdObs),
-                ("err_bits", ctypes.c_uint)]
+                ("err_bits", ctypes.c_uint), ("preemptions", ctypes.c_int)]
 
 
 class MpcdServerStats(ctypes.Structure):
@@ -91,7 +92,7 @@ class MpcdServerStats(ctypes.Structure):
                 ("resident", ctypes.c_longlong), ("queued", ctypes.c_longlong), ("p50_s", _D), ("p99_s", _D),
                 ("mean_s", _D), ("max_s", _D), ("particle_steps", _D), ("busy_s", _D), ("throughput", _D),
                 ("peak_resident_bytes", ctypes.c_longlong), ("peak_resident", ctypes.c_int),
-                ("gpu_launches", ctypes.c_longlong)]
+                ("gpu_launches", ctypes.c_longlong), ("preemptions", ctypes.c_longlong)]
 
 
 REQ_QUEUED, REQ_RESIDENT, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -154,6 +155,7 @@ def lib():
             "mpcd_get_rigid_spheres": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdRigidSphere), _DP]),
             "mpcd_reset_rigid_sphere_forces": (ctypes.c_int, [P]),
             "mpcd_rigid_sphere_count": (ctypes.c_int, [P]),
+            "mpcd_set_repelling": (ctypes.c_int, [P, _D]),
             "mpcd_collision_draws": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_long,
                                                     _DP, _DP, ctypes.c_int]),
             "mpcd_batch_step_inject": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(MpcdInject)]),
@@ -207,6 +209,9 @@ def lib():
             "mpcd_server_result_fluid": (ctypes.c_int, [P, ctypes.c_longlong, ctypes.c_long, _DP, _DP]),
             "mpcd_server_get_stats": (ctypes.c_int, [P, ctypes.POINTER(MpcdServerStats)]),
             "mpcd_server_request_error": (ctypes.c_char_p, [P, ctypes.c_longlong]),
+            "mpcd_server_preempt": (ctypes.c_int, [P, ctypes.c_longlong]),
+            "mpcd_batch_get_cilia": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, _DP, _DP, _DP]),
+            "mpcd_batch_set_step_count": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_longlong]),
             "cilia_sim_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
                                                 ctypes.POINTER(P)]),
             "cilia_sim_destroy": (ctypes.c_int, [P]),
@@ -382,6 +387,10 @@ class Engine:
         n = ctypes.c_longlong()
         self._ck(lib().mpcd_kernel_time(self._h, int(kernel), ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
         return ms.value, n.value
+
+    def set_repelling(self, eps):
+        """Contact forces between cilia (the reference's -DREPELLING=eps); 0 turns them off."""
+        self._ck(lib().mpcd_set_repelling(self._h, float(eps)), "set_repelling")
 
     def snapshot(self):
         """The handle's whole state as bytes (mpcd_snapshot)."""
@@ -685,7 +694,7 @@ class Batch:
 def _info_dict(i):
     o = i.obs
     return dict(id=i.id, state=i.state, steps=i.steps, t_submit=i.t_submit, t_admit=i.t_admit, t_done=i.t_done,
-                nfluid=i.nfluid, nbeads=i.nbeads, footprint=i.footprint, err=i.err_bits,
+                nfluid=i.nfluid, nbeads=i.nbeads, footprint=i.footprint, err=i.err_bits, preemptions=i.preemptions,
                 obs=dict(momentum=np.array(o.momentum[:]), n=o.n, mass=o.mass, kT=o.kT, fluid_T=o.fluid_T,
                          diss_energy=o.diss_energy, globalt=o.globalt, energy_fluid=o.energy_fluid))
 
@@ -693,7 +702,8 @@ def _info_dict(i):
 class Server:
     """Continuous batching of swimmer runs (mpcd_server)."""
 
-    def __init__(self, *, budget_bytes=0, chunk_steps=0, keep_fluid=False, lookahead=0, prep_threads=0, **batch):
+    def __init__(self, *, budget_bytes=0, chunk_steps=0, keep_fluid=False, lookahead=0, prep_threads=0,
+                 preempt_wait_s=0.0, **batch):
         b = dict(device=0, max_replicas=16, max_particles=0, max_cells=0, max_slots=0, max_springs=0, max_halo=0,
                  max_cilia=0, max_bonds=0, md_lanes=0, md_tile=0, sort_interval=0, sorts_per_graph=0)
         b.update(batch)
@@ -702,7 +712,7 @@ class Server:
                                              b["max_bonds"], b["md_lanes"], b["md_tile"], b["sort_interval"],
                                              b["sorts_per_graph"]),
                              int(budget_bytes), int(chunk_steps), int(bool(keep_fluid)), int(lookahead),
-                             int(prep_threads))
+                             int(prep_threads), float(preempt_wait_s))
         h = ctypes.c_void_p()
         rc = lib().mpcd_server_create(ctypes.byref(p), ctypes.byref(h))
         if rc:
@@ -755,6 +765,10 @@ class Server:
         if lib().mpcd_server_result_fluid(self._h, int(rid), int(n), _dp(pos), _dp(vel)):
             raise MpcdError("no fluid result")
         return pos, vel
+
+    def preempt(self, rid):
+        """Pre-empt a resident request at the end of the round (mpcd_server_preempt); False if not resident."""
+        return lib().mpcd_server_preempt(self._h, int(rid)) == 0
 
     def error(self, rid):
         m = lib().mpcd_server_request_error(self._h, int(rid))

@@ -1236,6 +1236,30 @@ int mpcd_batch_get_beads(mpcd_batch* b, int r, long nb, double* pos, double* vel
   return MPCD_OK;
 }
 
+int mpcd_batch_get_cilia(mpcd_batch* b, int r, int nc, double* state2, double* newlength, double* oldlength) {
+  Replica* R = get_rep(b, r);
+  if (!R || nc != (int)R->cil.size()) return fail(b, MPCD_EINVAL, "get_cilia: bad replica or count");
+  if (R->admitted) {
+    int rc = pull_md_state(b, *R);
+    if (rc) return rc;
+  }
+  for (int c = 0; c < nc; ++c)
+    if (state2) {
+      state2[2 * c] = R->cil[c].midpnt;
+      state2[2 * c + 1] = R->cil[c].tstroke;
+    }
+  if (newlength) std::memcpy(newlength, R->newlen.data(), R->newlen.size() * sizeof(double));
+  if (oldlength) std::memcpy(oldlength, R->oldlen.data(), R->oldlen.size() * sizeof(double));
+  return MPCD_OK;
+}
+
+int mpcd_batch_set_step_count(mpcd_batch* b, int r, long long steps_done) {
+  Replica* R = get_rep(b, r);
+  if (!R || R->admitted || steps_done < 0) return fail(b, MPCD_EINVAL, "set_step_count: bad replica (admitted?)");
+  R->steps = steps_done;
+  return MPCD_OK;
+}
+
 int mpcd_batch_observables(mpcd_batch* b, int r, mpcd_obs* out) {
   Replica* R = get_rep(b, r);
   if (!R || !R->admitted || !out) return fail(b, MPCD_EINVAL, "observables: bad arguments");

@@ -99,6 +99,11 @@ struct mpcd_engine {
   uint32_t* d_bcell = nullptr;
   void* d_bsum = nullptr;
   int bcap = 0;  // slots d_bcell / d_bsum hold
+  // contact forces between cilia (mpcd_set_repelling): eps and the candidate pair list
+  double repel = 0.0;
+  int2* d_cpairs = nullptr;
+  int* d_ncpairs = nullptr;
+  int cpair_cap = 0;
   // rigid spheres (mpcd_set_rigid_spheres): device state, this step's
   // impulses, running force / torque sums and the steps they cover
   int nsph = 0;
@@ -315,14 +320,15 @@ int build_md(mpcd_engine* h) {
   // double-float springs for the float64 path and float springs on the same
   // double-float positions for the float32 split path (swimmer64 MD 0.204
   // against 0.215 ms, swimmer128 0.423 against 0.526)
-  const int arith = h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 3 : 2) : h->p.md_split;
+  // contact forces between cilia run on the float64 grid kernel only
+  const int arith = h->repel != 0.0 ? 0 : h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 3 : 2) : h->p.md_split;
   if (arith > 3) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1, 2 or 3");
   in.split = arith == 1;
   in.df = arith == 2 || arith == 3;
   MDPlan pl;
   // MPCD_MD_NO_CLUSTER=1 keeps split arithmetic on the cooperative grid layout
   const char* no_cl = std::getenv("MPCD_MD_NO_CLUSTER");
-  const bool allow_cluster = !(no_cl && std::atoi(no_cl) != 0);
+  const bool allow_cluster = !(no_cl && std::atoi(no_cl) != 0) && h->repel == 0.0;
   // MPCD_MD_MIN_TILE: narrowest grid-layout tile (tests of the wide layouts on small bead sets)
   const char* mt = std::getenv("MPCD_MD_MIN_TILE");
   const int min_tile = mt ? std::max(0, std::min(256, std::atoi(mt))) : 0;
@@ -452,6 +458,23 @@ int build_md(mpcd_engine* h) {
   CK(up(m.tile_cil, pl.tcil.data(), (m.ntiles + 1) * 4));
   m.bar.count = h->d_bar;
   m.bar.gen = h->d_bar + 1;
+  if (h->repel != 0.0) {
+    for (size_t c = 0; c < ncil; ++c)
+      if (pl.cd[c].len > 64) return fail(h, MPCD_EINVAL, "repelling: cilia of at most 64 beads per filament");
+    const long need = std::max<long>(1, std::min<long>((long)ncil * ((long)ncil - 1) / 2, 1L << 20));
+    if (h->cpair_cap < need) {
+      cudaFree(h->d_cpairs);
+      h->d_cpairs = nullptr;
+      h->cpair_cap = 0;
+      CK(dalloc(&h->d_cpairs, need));
+      h->cpair_cap = (int)need;
+    }
+    if (!h->d_ncpairs) CK(dalloc(&h->d_ncpairs, 1));
+    m.repel = h->repel;
+    m.cpairs = h->d_cpairs;
+    m.ncpairs = h->d_ncpairs;
+    m.cpair_cap = h->cpair_cap;
+  }
   if (h->bcap < ns) {  // the deferred bead binning of the bead-first step
     cudaFree(h->d_bcell);
     cudaFree(h->d_bsum);
@@ -719,6 +742,8 @@ int mpcd_destroy(mpcd_engine* h) {
   cudaFree(h->d_obs_part);
   cudaFree(h->d_obs_count);
   cudaFree(h->d_bar);
+  cudaFree(h->d_cpairs);
+  cudaFree(h->d_ncpairs);
   cudaFree(h->d_claim);
   cudaFree(h->d_bcell);
   cudaFree(h->d_bsum);
@@ -1062,6 +1087,7 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
       ProfScope ps(h, MPCD_K_BEAD, sm);
       h->launches += f64 ? launch_bead_collide_f64(h->md, h->c64, s, sm) : launch_bead_collide_f32(h->md, h->c32, s, sm);
     }
+    if (h->md.repel != 0.0) h->launches += launch_contact_pairs(h->md, sm);
     ProfScope ps(h, MPCD_K_MD, sm);
     if (h->md.cluster)
       h->launches += f64 ? launch_md_cluster_f64cells(h->md, h->c64, ma, sm, &coop)
@@ -1289,6 +1315,16 @@ int mpcd_get_rigid_spheres(mpcd_engine* h, int n, mpcd_rigid_sphere* spheres, do
 }
 
 int mpcd_rigid_sphere_count(const mpcd_engine* h) { return h ? h->nsph : 0; }
+
+int mpcd_set_repelling(mpcd_engine* h, double eps) {
+  if (!h || !std::isfinite(eps)) return fail(h, MPCD_EINVAL, "set_repelling: eps must be finite");
+  int rc = pull_md(h);
+  if (rc) return rc;
+  h->repel = eps;
+  h->md_dirty = true;
+  h->prepared = false;
+  return MPCD_OK;
+}
 
 int mpcd_reset_rigid_sphere_forces(mpcd_engine* h) {
   if (!h) return MPCD_EINVAL;

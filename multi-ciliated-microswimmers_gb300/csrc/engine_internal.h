@@ -171,7 +171,16 @@ struct MDState {
   double* oldlen = nullptr;
   int* tile_cil = nullptr;  // ntiles + 1 offsets into cil (cilia sorted by tile)
   GridBarrier bar{nullptr, nullptr};
+  // contact forces between cilia (the reference's -DREPELLING=eps, float64 MD
+  // kernel only): eps (0 = off), and the cilium pairs whose section bounding
+  // boxes came within reach at the start of this MPC step (k_contact_pairs)
+  double repel = 0.0;
+  int2* cpairs = nullptr;
+  int* ncpairs = nullptr;
+  int cpair_cap = 0;
 };
+// candidate cilium pairs of the contact forces for one MPC step (MD stream)
+int launch_contact_pairs(const MDState& m, cudaStream_t s);
 
 struct MDStepArgs {
   double t0, dt, tstep;

@@ -726,6 +726,11 @@ Simulation::Simulation(const libconfig::Setting& root, const SimOptions& o) : op
     if (!(opt.read_files && load_fluid("fluid_n.dat"))) create_fluid();
   }
   upload_md();
+  // contact forces between cilia: the reference's -DREPELLING=eps as a cfg key
+  //   repelling = <eps>;
+  double repel = 0.0;
+  if (!opt.host_only && root.lookupValue("repelling", repel) && repel != 0.0)
+    check(mpcd_set_repelling(eng, repel), eng, "mpcd_set_repelling");
   // rigid no-slip spheres (an addition to the reference's cfg schema):
   //   rigid_spheres = ( { position = [x, y, z]; radius = r; mass = m; velocity = [..]; omega = [..]; } );
   // mass > 0 free, absent or <= 0 held (mpcd_set_rigid_spheres)

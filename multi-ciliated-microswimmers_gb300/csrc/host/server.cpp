@@ -43,6 +43,11 @@ struct Request {
   long nbeads = 0, nfluid = 0;
   long long footprint = 0;
   int replica = -1;
+  // pre-emption: the host system keeps the springs and cilia layout while the
+  // request is resident; a pre-empted request's state is read back into it
+  long long steps_offset = 0;  // collisions done before the current admission
+  int preemptions = 0;
+  bool preempt_flag = false;
   // results
   mpcd_obs obs{};
   unsigned err = 0;
@@ -71,6 +76,7 @@ struct mpcd_server {
   // statistics (device thread writes, callers read under mu)
   long long resident_bytes = 0, peak_bytes = 0;
   int peak_resident = 0;
+  long long preemptions = 0;
   double busy_s = 0.0;
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 };
@@ -148,8 +154,10 @@ void admit_ready(mpcd_server* s) {
     bool fits = false;
     try {
       cilia::add_to_batch(s->batch, *q->sys, q->nbeads, &r);
+      if (q->steps_offset > 0 && mpcd_batch_set_step_count(s->batch, r, q->steps_offset) != MPCD_OK)
+        throw std::runtime_error(mpcd_batch_last_error(s->batch));
       if (mpcd_batch_admit(s->batch, r) == MPCD_OK) {
-        fits = mpcd_batch_set_steps(s->batch, r, q->nsteps) == MPCD_OK;
+        fits = mpcd_batch_set_steps(s->batch, r, q->nsteps - q->steps_offset) == MPCD_OK;
         if (!fits) err = mpcd_batch_last_error(s->batch);
       } else {
         err = mpcd_batch_last_error(s->batch);
@@ -162,8 +170,10 @@ void admit_ready(mpcd_server* s) {
     if (fits) {
       q->replica = r;
       q->state = MPCD_REQ_RESIDENT;
-      q->t_admit = s->now();
-      q->sys.reset();  // the host copy is not needed any more
+      if (q->t_admit < 0) q->t_admit = s->now();
+      // the fluid's host copy is not needed while resident (a pre-emption reads it back)
+      std::vector<double>().swap(q->sys->fpos);
+      std::vector<double>().swap(q->sys->fvel);
       s->resident.push_back(q);
       s->resident_bytes += q->footprint;
       s->peak_bytes = std::max(s->peak_bytes, s->resident_bytes);
@@ -179,6 +189,75 @@ void admit_ready(mpcd_server* s) {
       s->cv_done.notify_all();
     }
   }
+}
+
+// Pre-emption policy (mpcd_server_params.preempt_wait_s): when the oldest
+// ready request has waited longer than that and is still not resident, the
+// resident request with the most steps left (more than the waiting one
+// needs) is pre-empted at the end of the round, so that a short request does
+// not wait behind long ones for the whole of their runs.
+void choose_preemption(mpcd_server* s) {
+  if (s->p.preempt_wait_s <= 0) return;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->ready.empty() || s->resident.empty()) return;
+  const ReqPtr& head = s->ready.front();
+  if (s->now() - head->t_submit < s->p.preempt_wait_s) return;
+  for (const ReqPtr& q : s->resident)
+    if (q->preempt_flag) return;  // one at a time
+  ReqPtr victim;
+  long long most = head->nsteps - head->steps_offset;
+  for (const ReqPtr& q : s->resident) {
+    const long long left = q->nsteps - q->steps_done;
+    if (left > most) {
+      most = left;
+      victim = q;
+    }
+  }
+  if (victim) victim->preempt_flag = true;
+}
+
+// Reads a resident request's state back into its host system, frees its
+// replica and puts it at the head of the ready queue; it resumes from that
+// state (and its step counter, so its random sequence continues) when it is
+// admitted again.  The dissipated energy restarts from zero at resumption.
+void preempt(mpcd_server* s, const ReqPtr& q) {
+  cilia::HostSystem& h = *q->sys;
+  long long done = 0, left = 0;
+  double t = 0;
+  unsigned err = 0;
+  bool ok = mpcd_batch_status(s->batch, q->replica, &done, &left, &t, &err) == MPCD_OK && !err;
+  if (ok && q->nfluid > 0) {
+    h.fpos.resize(3 * q->nfluid);
+    h.fvel.resize(3 * q->nfluid);
+    ok = mpcd_batch_get_fluid(s->batch, q->replica, q->nfluid, h.fpos.data(), h.fvel.data()) == MPCD_OK;
+  }
+  if (ok && q->nbeads > 0) {
+    ok = mpcd_batch_get_beads(s->batch, q->replica, q->nbeads, h.bpos.data(), h.bvel.data()) == MPCD_OK;
+    std::vector<double> st(2 * h.cilia.size());
+    ok = ok && mpcd_batch_get_cilia(s->batch, q->replica, (int)h.cilia.size(), st.data(), h.newlen.data(),
+                                    h.oldlen.data()) == MPCD_OK;
+    for (size_t c = 0; ok && c < h.cilia.size(); ++c) {
+      h.cilia[c].midpnt = st[2 * c];
+      h.cilia[c].tstroke = st[2 * c + 1];
+    }
+  }
+  ok = ok && mpcd_batch_get_shift(s->batch, q->replica, h.a) == MPCD_OK;
+  if (!ok) return;  // left resident; it finishes normally
+  h.globalt = t;
+  mpcd_batch_remove(s->batch, q->replica);
+  std::lock_guard<std::mutex> lk(s->mu);
+  q->replica = -1;
+  q->steps_offset = done;
+  q->steps_done = done;
+  q->preempt_flag = false;
+  q->preemptions++;
+  s->preemptions++;
+  q->state = MPCD_REQ_QUEUED;
+  s->resident_bytes -= q->footprint;
+  s->resident.erase(std::find(s->resident.begin(), s->resident.end(), q));
+  // right behind the oldest waiting request (the one the room is made for),
+  // ahead of everything else
+  s->ready.insert(s->ready.empty() ? s->ready.begin() : s->ready.begin() + 1, q);
 }
 
 void retire(mpcd_server* s, const ReqPtr& q, long long steps, unsigned err) {
@@ -207,6 +286,7 @@ void retire(mpcd_server* s, const ReqPtr& q, long long steps, unsigned err) {
   q->state = (err || rc_obs != MPCD_OK) ? MPCD_REQ_FAILED : MPCD_REQ_DONE;
   if (q->state == MPCD_REQ_FAILED) q->error = "device check failed for this request";
   q->t_done = s->now();
+  q->sys.reset();
   s->resident_bytes -= q->footprint;
   s->resident.erase(std::find(s->resident.begin(), s->resident.end(), q));
   s->cv_done.notify_all();
@@ -244,12 +324,20 @@ void dev_loop(mpcd_server* s) {
       s->stop = true;
       return;
     }
+    choose_preemption(s);
     for (const ReqPtr& q : res) {
       long long done = 0, left = 0;
       double t = 0;
       unsigned err = 0;
       if (mpcd_batch_status(s->batch, q->replica, &done, &left, &t, &err) != MPCD_OK) err |= 0x80000000u;
-      if (left == 0 || err) retire(s, q, done, err);
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        q->steps_done = done;
+      }
+      if (left == 0 || err)
+        retire(s, q, done, err);
+      else if (q->preempt_flag)
+        preempt(s, q);
     }
     std::lock_guard<std::mutex> lk(s->mu);
     s->busy_s += s->now() - t_round;
@@ -269,6 +357,7 @@ void fill_info(const Request& q, mpcd_request_info* o) {
   o->footprint = q.footprint;
   o->obs = q.obs;
   o->err_bits = q.err;
+  o->preemptions = q.preemptions;
 }
 
 }  // namespace
@@ -439,6 +528,17 @@ int mpcd_server_get_stats(mpcd_server* s, mpcd_server_stats* out) {
   out->peak_resident_bytes = s->peak_bytes;
   out->peak_resident = s->peak_resident;
   out->gpu_launches = mpcd_batch_launch_count(s->batch);
+  out->preemptions = s->preemptions;
+  return MPCD_OK;
+}
+
+int mpcd_server_preempt(mpcd_server* s, long long id) {
+  if (!s) return MPCD_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return MPCD_EINVAL;
+  if (it->second->state != MPCD_REQ_RESIDENT) return MPCD_ESTATE;
+  it->second->preempt_flag = true;
   return MPCD_OK;
 }
 

@@ -18,6 +18,8 @@
 // Spring arithmetic: float64 (plain path) or split (kSplit): positions as
 // float hi + float lo pairs, the difference x_i - x_j formed in float from the
 // pairs, the rest of the spring in float; state and integration stay float64.
+#include <algorithm>
+
 #include "md_common.cuh"
 
 namespace mpcd {
@@ -72,6 +74,118 @@ __device__ __forceinline__ void springs_split(const MDState& m, const Stage<true
   fz = az;
 }
 
+
+// ------------------------------------------------------------ contacts ---
+// Contact forces between cilia: GlobalForces::recalc_forces / vdw_force with
+// -DREPELLING=eps (src/libcilia/globalforces.cpp:22-95, constants
+// src/libcilia/globalforces.h:22-28: cutoff 1.5, N = 4), over the cilia in
+// their input order (the reference's own code names a `cilias` list its class
+// does not declare, so its -DREPELLING build does not compile).  For a pair
+// i < j, every filament-0 bead pair (k, l) on the lattices k = 3, 7, ... and
+// l = len_j - 3, len_j - 7, ... (l >= k) closer than N * cutoff adds, for
+// sections kk = k - 2 .. k + 1 and ll = l + 2 down to max(l - 2, kk), the
+// repulsion F = -2 eps (1 - cutoff / |d|) d of the section centroids d
+// (|d| < cutoff) to the three beads of section kk and -F to those of ll.  The
+// reference gates these loops by a bounding-box overlap within the cutoff;
+// that gate never removes a pair closer than the cutoff, so only candidate
+// pairs (boxes within cutoff + 1 at the start of the MPC step: beads move far
+// less than 0.5 in one step) are looked at.  Sections past a cilium's end are
+// skipped.
+constexpr double kRepelCutoff = 1.5;
+constexpr int kRepelN = 4;
+constexpr double kRepelReach = kRepelCutoff + 1.0;
+
+__device__ __forceinline__ int cil_slot(const CiliumDev& c, int f, int j) { return c.slot0 + c.stride * (f * c.len + j); }
+
+__device__ __forceinline__ void section_sum(const double* X, const double* Y, const double* Z, const CiliumDev& c, int j,
+                                            double* s) {
+  s[0] = s[1] = s[2] = 0.0;
+  for (int f = 0; f < 3; ++f) {
+    const int sl = cil_slot(c, f, j);
+    s[0] += X[sl];
+    s[1] += Y[sl];
+    s[2] += Z[sl];
+  }
+}
+
+__global__ void k_contact_pairs(MDState m) {
+  const long n = m.ncil;
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < n * n; p += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(p / n), j = (int)(p % n);
+    if (j <= i) continue;
+    const CiliumDev ci = m.cil[i], cj = m.cil[j];
+    double lo[2][3], hi[2][3];
+    for (int w = 0; w < 2; ++w) {
+      const CiliumDev& c = w ? cj : ci;
+      for (int q = 0; q < 3; ++q) {
+        lo[w][q] = 1e300;
+        hi[w][q] = -1e300;
+      }
+      for (int s = 0; s < c.len; ++s) {
+        double x[3];
+        section_sum(m.x[0], m.y[0], m.z[0], c, s, x);
+        for (int q = 0; q < 3; ++q) {
+          lo[w][q] = fmin(lo[w][q], x[q] / 3.0);
+          hi[w][q] = fmax(hi[w][q], x[q] / 3.0);
+        }
+      }
+    }
+    bool near = true;
+    for (int q = 0; q < 3; ++q) near = near && lo[1][q] - hi[0][q] < kRepelReach && lo[0][q] - hi[1][q] < kRepelReach;
+    if (!near) continue;
+    const int k = atomicAdd(m.ncpairs, 1);
+    if (k < m.cpair_cap) m.cpairs[k] = make_int2(i, j);
+  }
+}
+
+// contact forces on this tile's beads into cf[3 * local slot] (shared, zeroed by the caller)
+__device__ void contact_forces(const MDState& m, int b, int tile, int base, double* cf) {
+  const int np = min(*m.ncpairs, m.cpair_cap);
+  const int c0 = m.tile_cil[tile], c1 = m.tile_cil[tile + 1];
+  const double* X = m.x[b];
+  const double* Y = m.y[b];
+  const double* Z = m.z[b];
+  const int N = kRepelN;
+  // work items: (pair, coarse k index, coarse l index), 16 x 16 per pair
+  for (int w = threadIdx.x; w < np * 256; w += blockDim.x) {
+    const int2 pr = m.cpairs[w >> 8];
+    const bool mi = pr.x >= c0 && pr.x < c1, mj = pr.y >= c0 && pr.y < c1;
+    if (!mi && !mj) continue;
+    const CiliumDev ci = m.cil[pr.x], cj = m.cil[pr.y];
+    const int k = 1 + N / 2 + N * ((w >> 4) & 15);
+    const int l = cj.len - 1 - N / 2 - N * (w & 15);
+    if (k >= ci.len || l < k) continue;
+    const int sk = cil_slot(ci, 0, k), sl = cil_slot(cj, 0, l);
+    const double ex = X[sk] - X[sl], ey = Y[sk] - Y[sl], ez = Z[sk] - Z[sl];
+    if (!(sqrt(ex * ex + ey * ey + ez * ez) < N * kRepelCutoff)) continue;
+    for (int kk = k - N / 2; kk < k + N / 2 && kk < ci.len; ++kk) {
+      double x0[3];
+      section_sum(X, Y, Z, ci, kk, x0);
+      for (int ll = l + N / 2; ll >= l - N / 2 && ll >= kk; --ll) {
+        double x1[3];
+        section_sum(X, Y, Z, cj, ll, x1);
+        const double dx = (x0[0] - x1[0]) / 3.0, dy = (x0[1] - x1[1]) / 3.0, dz = (x0[2] - x1[2]) / 3.0;
+        const double dis = sqrt(dx * dx + dy * dy + dz * dz);
+        if (!(dis < kRepelCutoff)) continue;
+        const double f = -2.0 * m.repel * (1.0 - kRepelCutoff / dis);
+        for (int r = 0; r < 3; ++r) {
+          if (mi) {
+            double* c = cf + 3 * (cil_slot(ci, r, kk) - base);
+            atomicAdd(c, dx * f);
+            atomicAdd(c + 1, dy * f);
+            atomicAdd(c + 2, dz * f);
+          }
+          if (mj) {
+            double* c = cf + 3 * (cil_slot(cj, r, ll) - base);
+            atomicAdd(c, -(dx * f));
+            atomicAdd(c + 1, -(dy * f));
+            atomicAdd(c + 2, -(dz * f));
+          }
+        }
+      }
+    }
+  }
+}
 
 template <bool kSplit, typename Bin>
 __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
@@ -171,6 +285,19 @@ __device__ void md_body(const MDState& m, const MDStepArgs& a, Bin bin) {
           fz += part[3 * (q + k) + 2];
         }
     }
+    if (m.repel != 0.0) {  // contact forces between cilia, summed per bead in shared memory
+      double* cf = part + 3 * T;
+      for (int i = threadIdx.x; i < 3 * T; i += blockDim.x) cf[i] = 0.0;
+      __syncthreads();
+      contact_forces(m, cur, tile, base, cf);
+      __syncthreads();
+      if (primary && lane == 0) {
+        fx += cf[3 * q];
+        fy += cf[3 * q + 1];
+        fz += cf[3 * q + 2];
+      }
+      __syncthreads();
+    }
   };
   auto publish = [&](int b) {
     if (primary && lane == 0) {
@@ -246,7 +373,8 @@ __global__ void k_md_f32cells(MDState m, CellsF32 c, MDStepArgs a) {
 
 size_t md_smem(const MDState& m) {
   const int np = m.tile + m.hmax;
-  return (m.split ? Stage<true>::bytes(np) : Stage<false>::bytes(np)) + 3 * sizeof(double) * (size_t)m.tile;
+  return (m.split ? Stage<true>::bytes(np) : Stage<false>::bytes(np)) +
+         (m.repel != 0.0 ? 6 : 3) * sizeof(double) * (size_t)m.tile;
 }
 
 template <typename K, typename C>
@@ -271,6 +399,15 @@ int launch_md_f64(const MDState& m, const CellsF64& c, const MDStepArgs& a, cuda
 
 int launch_md_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st) {
   return m.split ? launch_coop(k_md_f32cells<true>, m, c, a, s, st) : launch_coop(k_md_f32cells<false>, m, c, a, s, st);
+}
+
+int launch_contact_pairs(const MDState& m, cudaStream_t s) {
+  if (m.repel == 0.0 || m.ncil < 2) return 0;
+  cudaMemsetAsync(m.ncpairs, 0, sizeof(int), s);
+  const long n2 = (long)m.ncil * m.ncil;
+  const int g = (int)std::min<long>((n2 + 255) / 256, 4096);
+  k_contact_pairs<<<g, 256, 0, s>>>(m);
+  return 1;
 }
 
 // co-resident CTA limit for the cooperative launch of this layout

@@ -135,6 +135,9 @@ struct orc_sim {
   /* boundaries and body force (-DNOSLIP / -DSLIP, -DFLUID_FLOW_G in the reference) */
   int walls;            /* 0 periodic, 1 no-slip, 2 slip walls at z = 0 and z = Lz - 1 */
   double gravity, omega;
+  /* contact forces between cilia (-DREPELLING=eps in the reference); 0 = off */
+  double repelling;
+  long contacts; /* section pairs found within the cutoff since orc_set_repelling */
 };
 
 /* ---------------------------------------------------------------- setup -- */
@@ -860,6 +863,104 @@ static void clami_forces(orc_sim* s, obj_t* cl) {
   }
 }
 
+/* GlobalForces::recalc_forces and vdw_force with -DREPELLING=eps
+ * (src/libcilia/globalforces.cpp:22-95, constants src/libcilia/globalforces.h:22-28:
+ * cutoff 1.5, N = 4).  The reference's code indexes a `cilias` list that
+ * GlobalForces does not declare, so its -DREPELLING build does not compile;
+ * restated here over the cilia in object order.  For every pair i < j (j from
+ * the last down) whose bounding boxes of section centroids (min from 999999,
+ * max from 0, as Cilia::getBoundingBox, src/cilia.cpp:435-465) overlap within
+ * the cutoff, every filament-0 bead pair (k, l) on the stride-N lattices
+ * k = 1 + N/2, 1 + N/2 + N, ... and l = len_j - 1 - N/2, ... down to l >= k,
+ * closer than N * cutoff, adds for sections kk = k - N/2 .. k + N/2 - 1 and
+ * ll = l + N/2 down to max(l - N/2, kk) the harmonic repulsion of the section
+ * centroids, F = -2 eps (1 - cutoff / |d|) d for |d| < cutoff, to all three
+ * filaments of section kk and its negative to those of ll.  Sections past a
+ * cilium's end (k + 1 = len, which the reference reads beyond its array) are
+ * skipped. */
+static void centroid(orc_sim* s, const obj_t* o, int j, double* c) {
+  c[0] = c[1] = c[2] = 0.0;
+  for (int r = 0; r < o->rods; ++r) {
+    const double* p = BP(s, o, r, j);
+    c[0] += p[0];
+    c[1] += p[1];
+    c[2] += p[2];
+  }
+}
+
+static void cilia_bbox(orc_sim* s, const obj_t* o, double* mn, double* mx) {
+  for (int q = 0; q < 3; ++q) {
+    mn[q] = 999999.0;
+    mx[q] = 0.0;
+  }
+  for (int j = 0; j < o->len; ++j) {
+    double c[3];
+    centroid(s, o, j, c);
+    for (int q = 0; q < 3; ++q) {
+      const double a = c[q] / o->rods;
+      if (a > mx[q]) mx[q] = a;
+      if (a < mn[q]) mn[q] = a;
+    }
+  }
+}
+
+static void repel_pair(orc_sim* s, obj_t* ci, obj_t* cj, int k, int l) {
+  const int N = 4;
+  const double cutoff = 1.5, eps = s->repelling;
+  for (int kk = k - N / 2; kk < k + N / 2; ++kk) {
+    if (kk >= ci->len) break;
+    double x0[3];
+    centroid(s, ci, kk, x0);
+    for (int ll = l + N / 2; ll >= l - N / 2 && ll >= kk; --ll) {
+      double x1[3], d[3];
+      centroid(s, cj, ll, x1);
+      for (int q = 0; q < 3; ++q) d[q] = (x0[q] - x1[q]) / 3.0;
+      const double dis = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      if (!(dis < cutoff)) continue;
+      s->contacts++;
+      const double force = -2.0 * eps * (1.0 - cutoff / dis);
+      for (int r = 0; r < ci->rods; ++r) {
+        double* f = BF(s, ci, r, kk);
+        for (int q = 0; q < 3; ++q) f[q] += d[q] * force;
+      }
+      for (int r = 0; r < cj->rods; ++r) {
+        double* f = BF(s, cj, r, ll);
+        for (int q = 0; q < 3; ++q) f[q] -= d[q] * force;
+      }
+    }
+  }
+}
+
+static void repel_forces(orc_sim* s) {
+  const int N = 4;
+  const double cutoff = 1.5;
+  for (int i = 0; i < s->nobj; ++i) {
+    obj_t* ci = &s->objs[i];
+    if (ci->kind != OBJ_CILIA && ci->kind != OBJ_CBCILIA) continue;
+    double mn1[3], mx1[3];
+    cilia_bbox(s, ci, mn1, mx1);
+    for (int j = s->nobj - 1; j > i; --j) {
+      obj_t* cj = &s->objs[j];
+      if (cj->kind != OBJ_CILIA && cj->kind != OBJ_CBCILIA) continue;
+      double mn2[3], mx2[3];
+      cilia_bbox(s, cj, mn2, mx2);
+      int overlap = 1;
+      for (int q = 0; q < 3; ++q)
+        overlap &= (mn2[q] - mx1[q] < cutoff) && (mn1[q] - mx2[q] < cutoff);
+      if (!overlap) continue;
+      for (int k = 1 + N / 2; k < ci->len; k += N)
+        for (int l = cj->len - 1 - N / 2; l >= k; l -= N)
+          if (sqrt(sqdist3(BP(s, ci, 0, k), BP(s, cj, 0, l))) < N * cutoff) repel_pair(s, ci, cj, k, l);
+    }
+  }
+}
+
+void orc_set_repelling(orc_sim* s, double eps) {
+  s->repelling = eps;
+  s->contacts = 0;
+}
+long orc_contacts(const orc_sim* s) { return s->contacts; }
+
 /* Simulation::recalc_forces (src/simulation.cpp:202-215) */
 static void recalc_forces(orc_sim* s) {
   for (int k = 0; k < s->nobj; ++k) {
@@ -867,6 +968,7 @@ static void recalc_forces(orc_sim* s) {
     if (o->kind == OBJ_CILIA || o->kind == OBJ_CBCILIA) cilia_forces(s, o);
     else if (o->kind == OBJ_SPHERE) sphere_forces(s, o);
   }
+  if (s->repelling != 0.0) repel_forces(s);
   for (int k = 0; k < s->nobj; ++k)
     if (s->objs[k].kind == OBJ_CLAMI) clami_forces(s, &s->objs[k]);
 }

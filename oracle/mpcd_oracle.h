@@ -87,6 +87,9 @@ int orc_step_walls(orc_sim* s, const double* inj_shift_next, const double* inj_g
  * 346-376) and the body force g cos(omega t) along x (src/libcilia/fluid.cpp:156-158) */
 void orc_set_walls(orc_sim* s, int walls);
 void orc_set_gravity(orc_sim* s, double g, double omega);
+/* contact forces between cilia (the reference's -DREPELLING=eps); 0 = off */
+void orc_set_repelling(orc_sim* s, double eps);
+long orc_contacts(const orc_sim* s);
 double orc_diss_energy(const orc_sim* s);
 void orc_reset_diss(orc_sim* s);
 

@@ -80,6 +80,9 @@ def lib():
         L.orc_step_walls.argtypes = [_P, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP]
         L.orc_set_walls.argtypes = [_P, _I]
         L.orc_set_gravity.argtypes = [_P, _D, _D]
+        L.orc_set_repelling.argtypes = [_P, _D]
+        L.orc_contacts.restype = _L
+        L.orc_contacts.argtypes = [_P]
         L.orc_diss_energy.restype = _D
         L.orc_diss_energy.argtypes = [_P]
         L.orc_set_threads.argtypes = [_P, _I]
@@ -235,6 +238,13 @@ class OracleSim:
 
     def set_gravity(self, g, omega=0.0):
         lib().orc_set_gravity(self._h, float(g), float(omega))
+
+    def set_repelling(self, eps):
+        """Contact forces between cilia (the reference's -DREPELLING=eps)."""
+        lib().orc_set_repelling(self._h, float(eps))
+
+    def contacts(self):
+        return lib().orc_contacts(self._h)
 
     def step(self, shift_next=None, gamma=None, axis=None, record=False, virt=None):
         """One MPC step; with record=True returns (shift, gamma, axis, virt) as drawn."""

@@ -22,6 +22,8 @@ collision partners), so:
     bead deviation; kT agrees with the runs alone within 3x their spread
     (at least 2e-3).
 """
+import time
+
 import numpy as np
 import pytest
 
@@ -154,4 +156,51 @@ def test_bad_request_fails_alone():
         srv.wait(bad, 60)
     assert srv.info(bad)["state"] == cg.REQ_FAILED
     assert srv.wait(good, 300)["state"] == cg.REQ_DONE
+    srv.close()
+
+
+def test_preempted_request_resumes_like_an_uninterrupted_run():
+    """A request pre-empted mid-run (mpcd_server_preempt: its state read back
+    to the host, its device ranges freed) and admitted again continues its
+    own random sequence: after 8 steps it agrees with the same request run
+    alone without interruption within the short-run tolerances above (beads
+    1e-3, 99.9 % of fluid positions 1e-4, kT 1e-4), ran all its steps and
+    reports the pre-emption."""
+    target = request_cfg(16, 5, seed=3)
+    steps = 8
+    ia, (pa, _), fa = run_alone(target, steps, 77)
+    srv = cg.Server(chunk_steps=2, keep_fluid=True, **capacity(3))
+    rid = srv.submit(target, steps, seed=77)
+    t0 = time.time()
+    while srv.info(rid)["state"] != cg.REQ_RESIDENT and time.time() - t0 < 60:
+        time.sleep(0.002)
+    assert srv.preempt(rid)
+    info = srv.wait(rid, 300)
+    pm, _ = srv.result_beads(rid, info["nbeads"])
+    fm = srv.result_fluid(rid, info["nfluid"])
+    assert srv.stats()["preemptions"] >= 1
+    srv.close()
+    assert info["state"] == cg.REQ_DONE and info["steps"] == steps and info["preemptions"] >= 1
+    assert np.abs(pa - pm).max() < 1e-3
+    dp = np.abs(periodic_diff(fa[0], fm[0], 16)).max(axis=1)
+    assert np.mean(dp < 1e-4) > 0.999
+    assert abs(ia["obs"]["kT"] - info["obs"]["kT"]) < 1e-4
+
+
+def test_preemption_policy_lets_a_short_request_pass_a_long_one():
+    """With room for one request at a time and preempt_wait_s set, a short
+    request arriving while a long one runs pre-empts it: the short one
+    finishes first, the long one still runs all its steps."""
+    srv = cg.Server(chunk_steps=5, preempt_wait_s=0.05, **capacity(1, L=16, n_cilia=4, max_replicas=1))
+    long_id = srv.submit(request_cfg(16, 4, seed=1), 400, seed=5)
+    t0 = time.time()
+    while srv.info(long_id)["state"] != cg.REQ_RESIDENT and time.time() - t0 < 60:
+        time.sleep(0.002)
+    short_id = srv.submit(request_cfg(16, 0, seed=2), 10, seed=6)
+    s_info = srv.wait(short_id, 300)
+    l_info = srv.wait(long_id, 300)
+    assert s_info["state"] == l_info["state"] == cg.REQ_DONE
+    assert s_info["steps"] == 10 and l_info["steps"] == 400
+    assert l_info["preemptions"] >= 1 and s_info["preemptions"] == 0
+    assert s_info["t_done"] < l_info["t_done"]
     srv.close()

@@ -77,7 +77,7 @@ def test_temperature_and_vacf_match_oracle(precision, oracle_vacf):
 # Clami::writedata's observables (src/clami.cpp:208-284): the centre of mass
 # of all beads and the body axis n = x_1 - x_0 of the sphere.  A small
 # ciliated sphere (box 16, radius 4, 12 ConstantBeatCilia of 3 x 8 beads)
-# runs free on the GPU and in the oracle, six seeds each; per run:
+# runs free on the GPU and in the oracle, sixteen seeds each; per run:
 #   v2    <|v_cm|^2> (the swimmer's kinetic temperature),
 #   speed <|x_cm(t + tau) - x_cm(t)|> / tau, tau = 5 time units,
 #   rate  <angle(n(t), n(t + tau))> / tau (rotation rate),
@@ -85,11 +85,12 @@ def test_temperature_and_vacf_match_oracle(precision, oracle_vacf):
 # The run-to-run spread is large (oracle, 10 seeds: v2 6.1e-4 with sd 12 %,
 # speed 0.0126 with sd 8 %, rate 0.0041 with sd 8 %), so the test states
 # agreement of the GPU and oracle means within 3.5 standard errors of their
-# difference, the standard deviation pooled over both groups; twelve oracle
-# seeds and eight GPU seeds (with six each, one draw of six oracle seeds gave
-# v2 = 5.6e-4 and a pooled standard error a third of the one the spread
-# above implies).  v2 is also checked against equipartition, 3 kT / M with M
-# the swimmer's total mass (931 beads of mass 5: 6.4e-4), within 20 %.
+# difference, the standard deviation pooled over both groups; sixteen seeds
+# per side (with twelve oracle and eight GPU seeds one draw put the float32
+# speed 4.1 standard errors off: 0.0133 against 0.0118, while 16 GPU seeds of
+# every MD arithmetic and 24 oracle seeds gave 0.0125-0.0128 against 0.0130).
+# v2 is also checked against equipartition, 3 kT / M with M the swimmer's
+# total mass (931 beads of mass 5: 6.4e-4), within 20 %.
 SWIM_WARM, SWIM_STEPS, SWIM_EVERY, SWIM_LAG = 200, 2000, 10, 5
 
 
@@ -125,7 +126,7 @@ def oracle_swimmer():
     from oracle import build_from_cfg
 
     runs = []
-    for seed in range(11, 23):
+    for seed in range(11, 27):
         o = build_from_cfg(swimmer_cfg(), seed=seed, ststep=0.002)
         o.set_threads(8)
         runs.append(swimmer_observables(o.step, o.beads))
@@ -138,7 +139,7 @@ def test_swimmer_speed_and_rotation_match_oracle(precision, oracle_swimmer):
 
     runs = []
     nbeads = 0
-    for seed in range(21, 29):
+    for seed in range(21, 37):
         s = cg.Sim(simcfg.dumps(swimmer_cfg()), precision=precision, ststep=0.002, seed=seed)
         runs.append(swimmer_observables(s.next_tstep, s.beads))
         nbeads = s.nbeads
