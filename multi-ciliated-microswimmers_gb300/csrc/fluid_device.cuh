@@ -143,7 +143,10 @@ __device__ __forceinline__ void add_impulse(double* acc, const double* rc, const
 // velocity V + W x r_c at the contact, for the rest of the step, and the
 // sphere receives the impulse v - v' and its moment.  A particle found
 // inside at the start (after the sphere moved onto it) is put on the surface
-// along the radius and reflected there.
+// along the radius and reflected there if it approaches the centre; one that
+// is leaving (a particle a previous reflection left on the surface) streams
+// freely, as it would a hair outside: otherwise a rounding-level difference
+// in the sphere's state decides whether it is turned back.
 __device__ __forceinline__ bool sphere_bounce(const SphereSet& ss, const Box& box, double h, double* x, double* v) {
   for (int k = 0; k < ss.n; ++k) {
     const RigidSphereDev& S = ss.s[k];
@@ -159,6 +162,7 @@ __device__ __forceinline__ bool sphere_bounce(const SphereSet& ss, const Box& bo
     const double C = r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2] - R * R;
     double tc, rc[3];
     if (C < 0.0) {  // inside at the start: onto the surface along the radius
+      if (B >= 0.0) continue;  // leaving
       const double s = R / sqrt(C + R * R);
       tc = 0.0;
 #pragma unroll
