@@ -72,7 +72,10 @@ typedef struct {
                             0 float64, 1 split (float springs on hi/lo position pairs; state
                             stays float64), 2 double-float (pairs of floats, about 48
                             significand bits, for forces and substeps; float64 between steps),
-                            3 float springs (split arithmetic) on the layout of 2 */
+                            3 float springs (split arithmetic) on the layout of 2,
+                            4 float64 with each spring and its reverse evaluated once and a
+                            sphere centre's force summed from its partners' reactions
+                            (faster than 0 on GB300) */
 } mpcd_params;
 
 /* Values that replace the generator for one step (all host arrays).  Used to
@@ -195,7 +198,9 @@ int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* la
  * info[8] receives: cluster (1: one thread-block cluster, 0: cooperative
  * grid), threads per slot, slots per tile, tiles (CTAs), slots, springs,
  * largest halo of a tile, arithmetic (0 float64, 1 split, 2 double-float,
- * 3 float springs on the double-float layout). */
+ * 3 float springs on the double-float layout, 4 float64 pair kernel; for 4
+ * "threads per slot" is the CTA's threads over its slots, and springs
+ * excludes the dropped lists of sphere centres). */
 int mpcd_md_layout(mpcd_engine* h, int* info);
 
 /* Lossless snapshots of a handle's whole state, for checkpoints that keep

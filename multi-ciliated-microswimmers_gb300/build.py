@@ -21,7 +21,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", CSRC, "-I", os.path.join(REPO, "include")] + ARCH
-CU_SOURCES = ["fluid_kernels.cu", "md_kernels.cu", "md_df.cu", "md_cluster.cu", "md_plan.cu", "engine.cu", "static_step.cu",
+CU_SOURCES = ["fluid_kernels.cu", "md_kernels.cu", "md_df.cu", "md_pair.cu", "md_cluster.cu", "md_plan.cu", "engine.cu", "static_step.cu",
               "batch_kernels.cu", "batch.cu"]
 HOST_SOURCES = ["host/libconfig_lite.cpp", "host/objects.cpp", "host/cilia_capi.cpp", "host/server.cpp"]
 CXX = os.environ.get("CXX", "g++")

@@ -23,8 +23,9 @@ SPRING_CONST, SPRING_GUARDED, SPRING_BOND, SPRING_DIAG = 0, 1, 2, 3
 CILIUM_BASIC, CILIUM_CONSTANT = 0, 1
 K_CELL, K_FLUID, K_BEAD, K_MD, K_SORT = 0, 1, 2, 3, 4
 # MD arithmetic (mpcd_params.md_split): auto, float64, split floats (cluster
-# layout), double-float, float springs on the double-float grid layout
-MD_AUTO, MD_F64, MD_SPLIT, MD_DF, MD_FLOAT = -1, 0, 1, 2, 3
+# layout), double-float, float springs on the double-float grid layout,
+# float64 with each spring pair evaluated once
+MD_AUTO, MD_F64, MD_SPLIT, MD_DF, MD_FLOAT, MD_PAIR = -1, 0, 1, 2, 3, 4
 
 _D = ctypes.c_double
 _DP = ctypes.POINTER(ctypes.c_double)

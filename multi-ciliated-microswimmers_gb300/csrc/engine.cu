@@ -213,6 +213,21 @@ void free_md(MDState& m) {
   cudaFree(m.halo_run_start);
   cudaFree(m.halo_single);
   cudaFree(m.halo_single_start);
+  cudaFree(m.pr_start);
+  cudaFree(m.pr_local_end);
+  cudaFree(m.pr_code);
+  cudaFree(m.pr_rest);
+  cudaFree(m.pr_m2k);
+  cudaFree(m.pi_start);
+  cudaFree(m.pi_list);
+  cudaFree(m.pl_start);
+  cudaFree(m.pl_list);
+  cudaFree(m.hub_slot);
+  cudaFree(m.hub_pbase);
+  cudaFree(m.hubpart);
+  cudaFree(m.th_start);
+  cudaFree(m.th);
+  cudaFree(m.tr_list);
   GridBarrier bar = m.bar;
   m = MDState{};
   m.bar = bar;
@@ -322,9 +337,10 @@ int build_md(mpcd_engine* h) {
   // against 0.215 ms, swimmer128 0.423 against 0.526)
   // contact forces between cilia run on the float64 grid kernel only
   const int arith = h->repel != 0.0 ? 0 : h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 3 : 2) : h->p.md_split;
-  if (arith > 3) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1, 2 or 3");
+  if (arith > 4) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1, 2, 3 or 4");
   in.split = arith == 1;
-  in.df = arith == 2 || arith == 3;
+  in.df = arith >= 2;
+  in.pair = arith == 4;
   MDPlan pl;
   // MPCD_MD_NO_CLUSTER=1 keeps split arithmetic on the cooperative grid layout
   const char* no_cl = std::getenv("MPCD_MD_NO_CLUSTER");
@@ -335,10 +351,20 @@ int build_md(mpcd_engine* h) {
   const std::string why =
       plan_md(in, MDForce{}, allow_cluster, false, h->p.precision == MPCD_FP32 ? 1 : 0, pl, min_tile);
   if (!why.empty()) return fail(h, MPCD_EINVAL, why);
+  if (const char* ps = std::getenv("MPCD_MD_PLAN_STATS"); ps && std::atoi(ps) && pl.pair) {
+    // the pair layout's per-tile sizes: force entries (of them reaching only
+    // the tile), halo, incidences, hubs reached
+    for (int t = 0; t < pl.ntiles; ++t)
+      std::fprintf(stderr, "md tile %d entries %d local %d halo %d incidences %d hubs %d\n", t,
+                   pl.pr_start[t + 1] - pl.pr_start[t], pl.pr_local_end[t] - pl.pr_start[t],
+                   pl.hstart[t + 1] - pl.hstart[t], pl.pi_start[(t + 1) * pl.tile] - pl.pi_start[t * pl.tile],
+                   pl.th_start[t + 1] - pl.th_start[t]);
+  }
   if (pl.hstart.size() != (size_t)pl.ntiles + 1 || pl.halo.size() != (size_t)pl.hstart.back())
     return fail(h, MPCD_EINVAL, "MD plan: halo lists inconsistent with their offsets");
   m.split = pl.split;
-  m.df = pl.df ? (arith == 3 ? 2 : 1) : 0;
+  m.pair = pl.pair;
+  m.df = pl.df && !pl.pair ? (arith == 3 ? 2 : 1) : 0;
   m.cluster = pl.cluster;
   m.cl_lanes = pl.cl_lanes;
   m.cl_nsp_max = pl.cl_nsp_max;
@@ -416,9 +442,53 @@ int build_md(mpcd_engine* h) {
     CK(up(m.oldlen, pl.oldlen.data(), nbond * 8));
     CK(up(m.diag, pl.diag.data(), nbond * 8));
   }
-  if (m.df) {
+  if (m.pair) {
+    // force entries, incidences and long beads of the pair kernel
+    m.pr_nent_max = pl.pr_nent_max;
+    m.pr_ninc_max = pl.pr_ninc_max;
+    m.pr_nlong_max = pl.pr_nlong_max;
+    const size_t ne = pl.pr_code.size(), ni = pl.pi_list.size(), nlg = pl.pl_list.size();
+    CK(dalloc(&m.pr_start, m.ntiles + 1));
+    CK(dalloc(&m.pr_local_end, m.ntiles));
+    CK(dalloc(&m.pr_code, std::max<size_t>(1, ne)));
+    CK(dalloc(&m.pr_rest, std::max<size_t>(1, ne)));
+    CK(dalloc(&m.pr_m2k, std::max<size_t>(1, ne)));
+    CK(dalloc(&m.pi_start, ns + 1));
+    CK(dalloc(&m.pi_list, std::max<size_t>(1, ni)));
+    CK(dalloc(&m.pl_start, m.ntiles + 1));
+    CK(dalloc(&m.pl_list, std::max<size_t>(1, nlg)));
+    CK(up(m.pr_start, pl.pr_start.data(), (m.ntiles + 1) * sizeof(int)));
+    CK(up(m.pr_local_end, pl.pr_local_end.data(), m.ntiles * sizeof(int)));
+    if (ne) {
+      CK(up(m.pr_code, pl.pr_code.data(), ne * sizeof(uint2)));
+      CK(up(m.pr_rest, pl.pr_rest.data(), ne * sizeof(double)));
+      CK(up(m.pr_m2k, pl.pr_m2k.data(), ne * sizeof(double)));
+    }
+    CK(up(m.pi_start, pl.pi_start.data(), (ns + 1) * sizeof(int)));
+    if (ni) CK(up(m.pi_list, pl.pi_list.data(), ni * sizeof(uint32_t)));
+    CK(up(m.pl_start, pl.pl_start.data(), (m.ntiles + 1) * sizeof(int)));
+    if (nlg) CK(up(m.pl_list, pl.pl_list.data(), nlg * sizeof(int)));
+    // hubs: their slots, the partial sums' offsets and two buffers of them,
+    // the tiles' references
+    m.nhub = (int)pl.hub_slot.size();
+    m.hub_ncon = pl.hub_pbase.empty() ? 0 : pl.hub_pbase.back();
+    m.ntr = (int)pl.tr_list.size();
+    CK(dalloc(&m.hub_slot, std::max<size_t>(1, pl.hub_slot.size())));
+    CK(dalloc(&m.hub_pbase, (size_t)m.nhub + 1));
+    CK(dalloc(&m.hubpart, std::max<size_t>(1, 8 * (size_t)m.hub_ncon)));
+    CK(dalloc(&m.th_start, m.ntiles + 1));
+    CK(dalloc(&m.th, std::max<size_t>(1, pl.th.size())));
+    CK(dalloc(&m.tr_list, std::max<size_t>(1, pl.tr_list.size())));
+    if (m.nhub) CK(up(m.hub_slot, pl.hub_slot.data(), m.nhub * sizeof(int)));
+    CK(up(m.hub_pbase, pl.hub_pbase.data(), (m.nhub + 1) * sizeof(int)));
+    CK(up(m.th_start, pl.th_start.data(), (m.ntiles + 1) * sizeof(int)));
+    if (!pl.th.empty()) CK(up(m.th, pl.th.data(), pl.th.size() * sizeof(HubRef)));
+    if (m.ntr) CK(up(m.tr_list, pl.tr_list.data(), m.ntr * sizeof(int)));
+  }
+  if (m.df || m.pair) {
     // float pairs of the spring data and the packed layout; the position pair
-    // buffers are filled by the kernel
+    // buffers are filled by the kernel (the pair kernel's four float64 per
+    // slot take the same 32 bytes)
     std::vector<float2> r2(nspk), k2(nspk);
     for (long i = 0; i < nspk; ++i) {
       const dfloat a = df_from_double(pl.srest[i]), b = df_from_double(pl.sm2k[i]);
@@ -1050,7 +1120,7 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
   const bool md = h->md.nslots > 0;
   // the double-float grid kernel applies the beads' collision itself (one
   // launch less on the MD chain); the other MD kernels after the bead kernel
-  const bool folded = md && !h->md.cluster && h->md.df;
+  const bool folded = md && !h->md.cluster && (h->md.df || h->md.pair);
   // bead first (MPCD_BEAD_FIRST=1, folded MD launch only): only the maps of
   // the cells that hold beads are made before the MD launch; it is forked
   // right after them, and the maps of the other cells and the fluid pass run
@@ -1092,6 +1162,9 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj) {
     if (h->md.cluster)
       h->launches += f64 ? launch_md_cluster_f64cells(h->md, h->c64, ma, sm, &coop)
                          : launch_md_cluster_f32cells(h->md, h->c32, ma, sm, &coop);
+    else if (h->md.pair)
+      h->launches += f64 ? launch_md_pair_f64cells(h->md, h->c64, ma, sm, &coop)
+                         : launch_md_pair_f32cells(h->md, h->c32, ma, sm, &coop);
     else if (h->md.df)
       h->launches += f64 ? launch_md_df_f64cells(h->md, h->c64, ma, sm, &coop)
                          : launch_md_df_f32cells(h->md, h->c32, ma, sm, &coop);
@@ -1572,13 +1645,13 @@ int mpcd_md_layout(mpcd_engine* h, int* info) {
   }
   const MDState& m = h->md;
   info[0] = m.cluster;
-  info[1] = m.cluster ? m.cl_lanes : (m.df ? md_df_lanes(m.tile) : 4);
+  info[1] = m.cluster ? m.cl_lanes : (m.pair ? md_pair_threads(m.tile) / m.tile : (m.df ? md_df_lanes(m.tile) : 4));
   info[2] = m.tile;
   info[3] = m.ntiles;
   info[4] = m.nslots;
   info[5] = (int)h->md_nsp;
   info[6] = m.hmax;
-  info[7] = m.df ? m.df + 1 : m.split;
+  info[7] = m.pair ? 4 : (m.df ? m.df + 1 : m.split);
   return MPCD_OK;
 }
 

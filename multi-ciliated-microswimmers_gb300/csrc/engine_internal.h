@@ -98,6 +98,20 @@ __host__ __device__ inline int spring_group(int kraw) {
   const int kind = kraw & 3;
   return kind == 0 ? ((kraw & kSpringReact) ? 1 : 0) : kind + 1;
 }
+// pair kernel: a bead summing more force entries than this is summed by warps
+constexpr int kPairLong = 32;
+// pair kernel: a hub (a sphere's centre) that a tile owns or reaches.  The
+// hub has no spring list of its own; the tiles holding its partners publish
+// the negated sums of their forces, and every tile that reaches it
+// integrates a copy from those partial sums.
+struct HubRef {
+  int hub;     // index into the hub tables
+  int idx;     // its staged index in the tile (below the tile size: the tile owns it)
+  int rank;    // this tile's partial sum among the hub's contributors, or -1
+  int rs, rn;  // the tile's entries whose reaction the hub takes: tr_list[rs, rs + rn)
+  int pad;
+};
+constexpr int kTileHubs = 4;  // hubs one tile may own or reach
 int md_max_coresident_blocks(const struct MDState& m, int f32cells);
 int md_cluster_feasible(const struct MDState& m);
 
@@ -162,6 +176,35 @@ struct MDState {
   int2* halo_single = nullptr;     // per tile: halo entries outside long runs {slot, rank}
   int* halo_single_start = nullptr;
   float4* q[2] = {nullptr, nullptr};
+  // float64 pair kernel (md_pair.cu), on the layout above with one slot per
+  // bead: per tile its force entries (a spring and its exact reverse inside
+  // the tile form one entry; code {a | b << 16, kind | both << 2 | react << 3
+  // | bond << 4}, rest length, -2k), the entries reaching only the tile's
+  // beads first; per
+  // slot the entries its force sums (entry within the tile << 1 | negate);
+  // per tile the beads with more than kPairLong entries.  Positions are
+  // published as four float64 per slot in q.
+  int pair = 0;
+  int pr_nent_max = 0, pr_ninc_max = 0, pr_nlong_max = 0;
+  int* pr_start = nullptr;      // ntiles + 1
+  int* pr_local_end = nullptr;  // ntiles
+  uint2* pr_code = nullptr;
+  double* pr_rest = nullptr;
+  double* pr_m2k = nullptr;
+  int* pi_start = nullptr;      // nslots + 1
+  uint32_t* pi_list = nullptr;
+  int* pl_start = nullptr;      // ntiles + 1
+  int* pl_list = nullptr;
+  // hubs: per hub its slot and the offsets of its contributors' partial sums
+  // (nhub + 1; hub_ncon in all), two buffers of partial sums (four float64
+  // each), per tile its hub references and their entry lists
+  int nhub = 0, hub_ncon = 0, ntr = 0;
+  int* hub_slot = nullptr;
+  int* hub_pbase = nullptr;
+  double* hubpart = nullptr;
+  int* th_start = nullptr;  // ntiles + 1
+  HubRef* th = nullptr;
+  int* tr_list = nullptr;
   // cilia
   int ncil = 0;
   CiliumDev* cil = nullptr;
@@ -217,6 +260,10 @@ int launch_md_df_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs&
 int launch_md_df_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
 int md_df_max_coresident_blocks(const MDState& m, int f32cells);
 int md_df_lanes(int tile);  // threads per slot of the double-float kernel
+int launch_md_pair_f64cells(const MDState& m, const CellsF64& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+int launch_md_pair_f32cells(const MDState& m, const CellsF32& c, const MDStepArgs& a, cudaStream_t s, cudaError_t* st);
+int md_pair_max_coresident_blocks(const MDState& m, int f32cells);
+int md_pair_threads(int tile);  // threads per CTA of the pair kernel
 // reduce observables: out[0..2] sum m v, out[3] sum m v^2 (all), out[4] N, out[5] M,
 // out[6] sum v^2 over fluid, out[7] N fluid
 int launch_observables_f64(const FluidF64& f, const MDState& m, double bead_mass, double* out, cudaStream_t s);

@@ -25,11 +25,10 @@ __device__ inline double cilium_target(const CiliumDev& cl, int i, double midpnt
 }
 
 // Cilia::length(i), second part: the change from the previous rest length is
-// limited by the bending rate; tl is the bond's current length
-__device__ inline double cilium_length(const CiliumDev& cl, int i, double midpnt, double oldlen, double tl) {
-  double l = cilium_target(cl, i, midpnt);
-  if (fabs(l - tl) > cl.bending) {
-    tl = tl + cl.bending - 2.0 * cl.bending * (l < tl ? 1.0 : 0.0);
+// limited by the bending rate; l is the target, tl the bond's current length
+__device__ inline double cilium_limit(double l, double bending, double oldlen, double tl) {
+  if (fabs(l - tl) > bending) {
+    tl = tl + bending - 2.0 * bending * (l < tl ? 1.0 : 0.0);
     if ((l - oldlen) * (tl - oldlen) > 0) {
       l = tl;
     } else {
@@ -37,6 +36,9 @@ __device__ inline double cilium_length(const CiliumDev& cl, int i, double midpnt
     }
   }
   return l;
+}
+__device__ inline double cilium_length(const CiliumDev& cl, int i, double midpnt, double oldlen, double tl) {
+  return cilium_limit(cilium_target(cl, i, midpnt), cl.bending, oldlen, tl);
 }
 
 // refresh every 0.01 time units (src/cilia.cpp:206-215); the schedule of the

@@ -412,6 +412,7 @@ int launch_contact_pairs(const MDState& m, cudaStream_t s) {
 
 // co-resident CTA limit for the cooperative launch of this layout
 int md_max_coresident_blocks(const MDState& m, int f32cells) {
+  if (m.pair) return md_pair_max_coresident_blocks(m, f32cells);
   if (m.df) return md_df_max_coresident_blocks(m, f32cells);
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);

@@ -15,6 +15,142 @@
 
 namespace mpcd {
 
+namespace {
+
+// Force entries of the float64 pair kernel (md_pair.cu) from the slot-ordered
+// spring lists of a grid layout with one slot per bead.  A spring whose other
+// bead lies in the same tile, and whose exact reverse (same kind, same rest
+// length or bond, same constant) is in that bead's list, forms one entry with
+// the reverse: the two forces are fac (x_a - x_b) and its negation bit for bit
+// (the squared distance of the negated difference is the same number), so the
+// entry is evaluated once.  The reference makes every cilium and sphere
+// spring in both directions (src/cilia.cpp:127-201, src/sphere.cpp:87-119).
+// A spring whose reaction a hub takes (its other bead is the hub) is an entry
+// of its own bead; the tile's entries of each hub are listed for its partial
+// sum.  Returns "hub" when a tile would reach more than kTileHubs hubs.
+std::string plan_pair_tables(MDPlan& out, const std::vector<int>& hubs) {
+  const int T = out.tile, nt = out.ntiles, ns = out.nslots;
+  const std::vector<int>& start = out.start;
+  const int nsp = start[ns];
+  out.pair = 1;
+  out.pr_start.assign(nt + 1, 0);
+  out.pr_local_end.assign(nt, 0);
+  out.pr_code.clear();
+  out.pr_rest.clear();
+  out.pr_m2k.clear();
+  out.pi_start = start;  // one incidence per one-sided spring
+  out.pi_list.assign(nsp, 0u);
+  out.pl_start.assign(nt + 1, 0);
+  out.pl_list.clear();
+  out.pr_nent_max = out.pr_ninc_max = out.pr_nlong_max = 0;
+  const int nh = (int)hubs.size();
+  std::vector<int> hub_of(ns, -1);
+  for (int h = 0; h < nh; ++h) hub_of[hubs[h]] = h;
+  out.hub_slot = hubs;
+  std::vector<int> ncon(nh, 0);
+  out.th_start.assign(nt + 1, 0);
+  out.th.clear();
+  out.tr_list.clear();
+  std::vector<int> ent(nsp, -1);  // spring -> entry of its tile (in creation order)
+  std::vector<char> neg(nsp, 0);
+  struct Entry {
+    int a, b, kind, both, react, lref, bslot;
+    double rest, m2k;
+  };
+  std::vector<Entry> es;
+  for (int t = 0; t < nt; ++t) {
+    const int base = t * T;
+    es.clear();
+    for (int s = base; s < base + T; ++s)
+      for (int d = start[s]; d < start[s + 1]; ++d) {
+        if (ent[d] >= 0) continue;  // the reverse half of an entry made before
+        if (out.sk[d] & ~(3 | kSpringReact)) return "pair kernel: unexpected spring flags";
+        const int react = (out.sk[d] & kSpringReact) ? 1 : 0;
+        if (react && hub_of[out.so[d]] < 0) return "pair kernel: a reaction spring whose other bead is not a hub";
+        const int a = s - base, b = out.sl[d], kind = out.sk[d] & 3;
+        const int lref = kind >= MPCD_SPRING_BOND ? out.sr[d] - out.df_b0[t] : 0;
+        Entry e{a, b, kind, 0, react, lref, out.so[d], out.srest[d], out.sm2k[d]};
+        ent[d] = (int)es.size();
+        if (b < T && b != a && !react) {
+          const int so = base + b;
+          for (int r = start[so]; r < start[so + 1]; ++r) {
+            if (ent[r] >= 0 || out.so[r] != s || out.sk[r] != out.sk[d] || out.sm2k[r] != out.sm2k[d]) continue;
+            if (kind >= MPCD_SPRING_BOND ? out.sr[r] != out.sr[d] : out.srest[r] != out.srest[d]) continue;
+            ent[r] = (int)es.size();
+            neg[r] = 1;
+            e.both = 1;
+            break;
+          }
+        }
+        es.push_back(e);
+      }
+    // the entries reaching only this tile's beads first (they run while the
+    // halo loads); those reaching a hub wait for its partial sums, which
+    // arrive with the halo
+    std::vector<int> order, rank(es.size());
+    auto local = [&](const Entry& e) { return e.b < T && hub_of[e.bslot] < 0; };
+    for (size_t i = 0; i < es.size(); ++i)
+      if (local(es[i])) order.push_back((int)i);
+    const int nloc = (int)order.size();
+    for (size_t i = 0; i < es.size(); ++i)
+      if (!local(es[i])) order.push_back((int)i);
+    for (size_t i = 0; i < order.size(); ++i) rank[order[i]] = (int)i;
+    const int g0 = (int)out.pr_code.size();
+    // hubs this tile owns or reaches, with the entries whose reaction each takes
+    std::vector<HubRef> refs;
+    std::vector<std::vector<int>> rlist;
+    auto ref_of = [&](int h, int idx) {
+      for (size_t k = 0; k < refs.size(); ++k)
+        if (refs[k].hub == h) return (int)k;
+      refs.push_back(HubRef{h, idx, -1, 0, 0, 0});
+      rlist.emplace_back();
+      return (int)refs.size() - 1;
+    };
+    for (int s = base; s < base + T; ++s)
+      if (hub_of[s] >= 0) ref_of(hub_of[s], s - base);
+    for (size_t r = 0; r < order.size(); ++r) {
+      const Entry& e = es[order[r]];
+      if (e.b >= (1 << 16) || e.a >= (1 << 16) || e.lref < 0 || e.lref >= (1 << 27))
+        return "pair kernel: an MD tile is too large for packed entry codes";
+      out.pr_code.push_back(make_uint2((uint32_t)e.a | ((uint32_t)e.b << 16),
+                                       (uint32_t)e.kind | ((uint32_t)e.both << 2) | ((uint32_t)e.react << 3) |
+                                           ((uint32_t)e.lref << 4)));
+      out.pr_rest.push_back(e.rest);
+      out.pr_m2k.push_back(e.m2k);
+      if (hub_of[e.bslot] >= 0) {
+        const int k = ref_of(hub_of[e.bslot], e.b);
+        if (refs[k].idx != e.b) return "pair kernel: a hub staged twice in one tile";
+        if (e.react) rlist[k].push_back((int)r);
+      }
+    }
+    if ((int)refs.size() > kTileHubs) return "hub";
+    for (size_t k = 0; k < refs.size(); ++k) {
+      if (!rlist[k].empty()) refs[k].rank = ncon[refs[k].hub]++;
+      refs[k].rs = (int)out.tr_list.size();
+      refs[k].rn = (int)rlist[k].size();
+      out.tr_list.insert(out.tr_list.end(), rlist[k].begin(), rlist[k].end());
+      out.th.push_back(refs[k]);
+    }
+    out.th_start[t + 1] = (int)out.th.size();
+    out.pr_local_end[t] = g0 + nloc;
+    out.pr_start[t + 1] = (int)out.pr_code.size();
+    out.pr_nent_max = std::max(out.pr_nent_max, (int)es.size());
+    // per slot: the entries its force sums, in its spring order
+    for (int s = base; s < base + T; ++s) {
+      for (int d = start[s]; d < start[s + 1]; ++d) out.pi_list[d] = ((uint32_t)rank[ent[d]] << 1) | (uint32_t)neg[d];
+      if (start[s + 1] - start[s] > kPairLong) out.pl_list.push_back(s - base);
+    }
+    out.pl_start[t + 1] = (int)out.pl_list.size();
+    out.pr_nlong_max = std::max(out.pr_nlong_max, out.pl_start[t + 1] - out.pl_start[t]);
+    out.pr_ninc_max = std::max(out.pr_ninc_max, start[base + T] - start[base]);
+  }
+  out.hub_pbase.assign(nh + 1, 0);
+  for (int h = 0; h < nh; ++h) out.hub_pbase[h + 1] = out.hub_pbase[h] + ncon[h];
+  return "";
+}
+
+}  // namespace
+
 std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster, bool no_react, int grid_f32cells,
                     MDPlan& out, int min_tile) {
   // springs per helper slot: the longest serial spring chain of any thread.
@@ -23,6 +159,8 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
   // The double-float grid kernel's springs cost more per lane: shorter chunks.
   int kChunk = in.df && !in.split ? 15 : 31;
   if (const char* env = std::getenv("MPCD_MD_CHUNK")) kChunk = std::max(2, std::min(256, std::atoi(env)));
+  // the pair kernel sums long lists by warps: one slot per bead
+  if (in.pair) kChunk = INT_MAX;
   out = MDPlan{};
   const bool forced = force.lanes > 0;
   out.split = in.split;
@@ -135,13 +273,77 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
         fill[t] += width[cl.bead0 + k];
       }
     }
-    size_t tcur = 0;
+    // the pair kernel keeps the other beads (a sphere) in tiles of their own:
+    // fewer springs between tiles, and a hub's partial sums come from those
+    // tiles only
+    size_t tcur = in.pair ? fill.size() : 0;
     for (long b = 0; b < nb; ++b) {
       if (owner[b] >= 0) continue;
       while (tcur < fill.size() && fill[tcur] + width[b] > tile) ++tcur;
       if (tcur == fill.size()) fill.push_back(0);
       slot_of[b] = (int)tcur * tile + fill[tcur];
       fill[tcur] += width[b];
+    }
+    return (int)fill.size();
+  };
+  // Pair-kernel packing: cilia as above; every run of consecutive other beads
+  // (a sphere, whose bead order does not follow its mesh) is cut by recursive
+  // coordinate bisection into compact patches, each in a tile of its own, so
+  // that many of a patch's springs join two of its own beads (one entry for
+  // both) and its work stays near a cilium tile's.  In bead order the
+  // swimmer64 sphere put 500-680 entries into a tile against 207 in a cilium
+  // tile.
+  auto pack_pair = [&](int tile) {
+    pack(tile);  // the cilia's tiles
+    const int ncil_tiles = ncil > 0 ? cil_tile[ncil - 1] + 1 : 0;
+    fill.resize(ncil_tiles);
+    for (long b = 0; b < nb; ++b)
+      if (owner[b] < 0) slot_of[b] = -1;
+    // beads per patch: a third of a tile (swimmer64 float64 MD per launch:
+    // 0.374 ms against 0.382 at half a tile and 0.399 at a quarter;
+    // MPCD_MD_PATCH=n overrides)
+    const char* pe = std::getenv("MPCD_MD_PATCH");
+    const int cap = std::max(1, std::min(tile, pe ? std::atoi(pe) : tile / 3));
+    std::vector<long> idx;
+    std::vector<std::pair<size_t, size_t>> todo;
+    for (long b = 0; b < nb;) {
+      if (owner[b] >= 0) {
+        ++b;
+        continue;
+      }
+      long e = b;
+      while (e < nb && owner[e] < 0) ++e;
+      idx.clear();
+      for (long k = b; k < e; ++k) idx.push_back(k);
+      todo.assign(1, {0, idx.size()});
+      while (!todo.empty()) {  // depth first, left part first: patches in a fixed order
+        const auto [lo, hi] = todo.back();
+        todo.pop_back();
+        const size_t n = hi - lo;
+        if ((int)n <= cap) {
+          fill.push_back(0);
+          const int t = (int)fill.size() - 1;
+          for (size_t k = lo; k < hi; ++k) slot_of[idx[k]] = t * tile + fill[t]++;
+          continue;
+        }
+        double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+        for (size_t k = lo; k < hi; ++k)
+          for (int d = 0; d < 3; ++d) {
+            mn[d] = std::min(mn[d], in.bpos[3 * idx[k] + d]);
+            mx[d] = std::max(mx[d], in.bpos[3 * idx[k] + d]);
+          }
+        int ax = 0;
+        for (int d = 1; d < 3; ++d)
+          if (mx[d] - mn[d] > mx[ax] - mn[ax]) ax = d;
+        const size_t parts = (n + cap - 1) / cap, left = n * (parts / 2) / parts;
+        std::nth_element(idx.begin() + lo, idx.begin() + lo + left, idx.begin() + hi, [&](long p, long q) {
+          const double a = in.bpos[3 * p + ax], c = in.bpos[3 * q + ax];
+          return a < c || (a == c && p < q);
+        });
+        todo.push_back({lo + left, hi});
+        todo.push_back({lo, lo + left});
+      }
+      b = e;
     }
     return (int)fill.size();
   };
@@ -268,7 +470,10 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     // per slot), unless a wider one is asked for: the grid must be co-resident
     tile = std::max(std::max(32, min_tile), ((maxw + 15) / 16) * 16);
     if (tile > 256) return "an MD group needs more than 256 slots";  // four threads per slot
-    pack(tile);
+    if (in.pair)
+      pack_pair(tile);
+    else
+      pack(tile);
   }
   // a hub and all its partners must share one tile, one hub per tile
   {
@@ -284,6 +489,43 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     for (long i = 0; i < nsp && !bad; ++i)
       if (react[i] && slot_of[in.sp_t[i]] / tile != slot_of[in.sp_o[i]] / tile) bad = true;
     if (bad) return plan_md(in, force, allow_cluster, true, grid_f32cells, out, min_tile);
+  }
+  // Hubs of the pair kernel: a bead outside the cilia with more than
+  // kPairLong springs, each with an exact reverse partner (a sphere's centre,
+  // src/sphere.cpp:87-96), whose neighbours are not such beads themselves.
+  // Its own list is dropped; its force is the negated sum of its partners'
+  // forces, which the tiles holding the partners add up and publish, and
+  // every tile that reaches the hub integrates a copy of it.
+  std::vector<char> phub(nb, 0);
+  if (in.pair && !no_react) {
+    auto candidate = [&](long b) { return owner[b] < 0 && nspr[b] > kPairLong; };
+    for (long b = 0; b < nb; ++b) {
+      if (!candidate(b)) continue;
+      std::vector<int> partners;
+      bool ok = true;
+      for (int q = bstart[b]; q < bstart[b + 1] && ok; ++q) {
+        const int i = blist[q];
+        const int o = in.sp_o[i];
+        if (o == b || candidate(o)) {
+          ok = false;
+          break;
+        }
+        int found = -1;
+        for (int r = bstart[o]; r < bstart[o + 1]; ++r) {
+          const int j = blist[r];
+          if (in.sp_o[j] != b || in.sp_k[j] != in.sp_k[i] || in.sp_kk[j] != in.sp_kk[i] || react[j]) continue;
+          if (in.sp_k[i] >= MPCD_SPRING_BOND ? in.sp_r[j] != in.sp_r[i] : in.sp_rest[j] != in.sp_rest[i]) continue;
+          found = j;
+          break;
+        }
+        if (found < 0) ok = false;
+        else partners.push_back(found);
+      }
+      if (!ok) continue;
+      phub[b] = 1;
+      for (int j : partners) react[j] = 1;
+      for (int q = bstart[b]; q < bstart[b + 1]; ++q) dropped[blist[q]] = 1;
+    }
   }
   out.tile = tile;
   out.ntiles = (int)fill.size();
@@ -384,6 +626,13 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
   }
   // halos: per tile the distinct slots of other tiles its springs reach, and
   // every spring's other bead as an index into the tile's staged positions
+  std::vector<char> hub_at(ns, 0);  // slots of the pair kernel's hubs
+  std::vector<int> hub_slots;
+  for (long b = 0; b < nb; ++b)
+    if (phub[b]) {
+      hub_at[slot_of[b]] = 1;
+      hub_slots.push_back(slot_of[b]);
+    }
   out.sl.assign(nspk, 0);
   out.hstart.assign(out.ntiles + 1, 0);
   out.df_runs.clear();
@@ -412,9 +661,15 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     // runs by bulk copy measured slower.  MPCD_MD_LONG_RUN=n overrides.
     const char* lr_env = std::getenv("MPCD_MD_LONG_RUN");
     const size_t kLongRun = lr_env ? (size_t)std::max(1, std::atoi(lr_env)) : (size_t)32;
+    // (a pair-kernel hub keeps its staged place but is never copied: every
+    // tile that reaches it integrates its own copy)
     for (size_t i = 0; i < ext.size();) {
+      if (hub_at[ext[i]]) {
+        ++i;
+        continue;
+      }
       size_t e = i + 1;
-      while (e < ext.size() && ext[e] == ext[e - 1] + 1) ++e;
+      while (e < ext.size() && ext[e] == ext[e - 1] + 1 && !hub_at[ext[e]]) ++e;
       if (e - i >= kLongRun)
         out.df_runs.push_back({ext[i], (int)i, (int)(e - i), 0});
       else
@@ -488,7 +743,17 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
       }
     }
   }
+  if (in.pair) {
+    if (!out.df) return "the pair kernel needs the double-float grid layout";
+    const std::string e = plan_pair_tables(out, hub_slots);
+    if (e == "hub") return plan_md(in, force, allow_cluster, true, grid_f32cells, out, min_tile);  // no hubs then
+    if (!e.empty()) return e;
+  }
   MDState probe;  // the fields the feasibility checks read
+  probe.pair = out.pair;
+  probe.pr_nent_max = out.pr_nent_max;
+  probe.pr_ninc_max = out.pr_ninc_max;
+  probe.pr_nlong_max = out.pr_nlong_max;
   probe.tile = tile;
   probe.ntiles = out.ntiles;
   probe.nslots = ns;

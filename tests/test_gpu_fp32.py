@@ -35,11 +35,12 @@ def test_fp32_fluid_tracks_reference_golden():
     assert np.mean(dv < 2e-4) > 0.995
 
 
-@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_DF, cg.MD_SPLIT, cg.MD_FLOAT])
+@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_DF, cg.MD_SPLIT, cg.MD_FLOAT, cg.MD_PAIR])
 def test_fp32_swimmer_tracks_reference_golden(arith):
     """MD in split arithmetic on the double-float kernel's grid layout (the
-    default of the float32 path), in double-float, and in split arithmetic on
-    one thread-block cluster (the replica batch's MD)."""
+    default of the float32 path), in double-float, in split arithmetic on
+    one thread-block cluster (the replica batch's MD), and in float64 on the
+    pair kernel, beside the float32 fluid."""
     g = golden("clami10")
     text = open(f"{GOLDEN}/cases/clami10.cfg").read()
     s = cg.Sim(text, precision=cg.MPCD_FP32, ststep=0.002, create_fluid=False, md_arith=arith)

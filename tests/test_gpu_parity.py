@@ -58,7 +58,7 @@ def test_fluid_matches_reference_golden(case):
     assert abs(obs["diss_energy"] - g[f"step{int(steps)}_meta"][1]) < 1e-8 * max(1, abs(g[f"step{int(steps)}_meta"][1]))
 
 
-@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64])
+@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64, cg.MD_PAIR])
 @pytest.mark.parametrize("case", ["clami10", "objects8"])
 def test_swimmer_matches_reference_golden(case, arith):
     """MD substeps in double-float (the float64 path's default) and in float64."""
@@ -89,7 +89,9 @@ def test_swimmer_matches_reference_golden(case, arith):
 
 
 @pytest.mark.parametrize("arith,bulk,min_tile", [(cg.MD_DF, False, 0), (cg.MD_DF, True, 0), (cg.MD_F64, False, 0),
-                                                  (cg.MD_DF, False, 128), (cg.MD_DF, False, 256)])
+                                                  (cg.MD_DF, False, 128), (cg.MD_DF, False, 256),
+                                                  (cg.MD_PAIR, False, 0), (cg.MD_PAIR, True, 0),
+                                                  (cg.MD_PAIR, False, 128), (cg.MD_PAIR, False, 256)])
 def test_multi_tile_swimmer_matches_oracle(arith, bulk, min_tile, monkeypatch):
     """A Clami whose cilia fill many MD tiles (halos between tiles, a sphere
     centre with helper slots) against the C oracle, injected randomness, 6 MPC
@@ -97,7 +99,8 @@ def test_multi_tile_swimmer_matches_oracle(arith, bulk, min_tile, monkeypatch):
     two or more slots by bulk asynchronous copies (TMA) instead of per-entry
     cp.async.  min_tile: the wide tiles that large swimmers get when the
     narrow grid would not be co-resident (128 slots at four lanes per slot,
-    256 at two)."""
+    256 at two).  MD_PAIR: float64 with each spring pair inside a tile
+    evaluated once and the sphere centre's long list summed by warps."""
     if bulk:
         monkeypatch.setenv("MPCD_MD_LONG_RUN", "2")
     if min_tile:
@@ -109,7 +112,7 @@ def test_multi_tile_swimmer_matches_oracle(arith, bulk, min_tile, monkeypatch):
     lay = e.md_layout()
     assert lay["arith"] == arith and lay["cluster"] == 0 and lay["hmax"] > 0
     assert lay["ntiles"] > (4 if not min_tile else 2) and lay["tile"] >= min_tile
-    if min_tile:
+    if min_tile and arith == cg.MD_DF:
         assert lay["lanes"] == (4 if min_tile == 128 else 2)
     p0, v0 = o.fluid()
     e.set_fluid(p0, v0)
