@@ -154,6 +154,7 @@ MD_ARITH_NAMES = {
     2: "double-float (pairs of floats, 48-bit significand; integer cell + offset coordinates)",
     3: "float springs on double-float positions (split arithmetic; integer cell + offset coordinates)",
     4: "float64, each spring pair evaluated once (pair kernel)",
+    5: "double-float, each spring pair evaluated once (pair kernel; integer cell + offset coordinates)",
 }
 
 

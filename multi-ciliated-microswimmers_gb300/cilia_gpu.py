@@ -24,8 +24,8 @@ CILIUM_BASIC, CILIUM_CONSTANT = 0, 1
 K_CELL, K_FLUID, K_BEAD, K_MD, K_SORT = 0, 1, 2, 3, 4
 # MD arithmetic (mpcd_params.md_split): auto, float64, split floats (cluster
 # layout), double-float, float springs on the double-float grid layout,
-# float64 with each spring pair evaluated once
-MD_AUTO, MD_F64, MD_SPLIT, MD_DF, MD_FLOAT, MD_PAIR = -1, 0, 1, 2, 3, 4
+# float64 and double-float with each spring pair evaluated once (pair kernel)
+MD_AUTO, MD_F64, MD_SPLIT, MD_DF, MD_FLOAT, MD_PAIR, MD_PAIR_DF = -1, 0, 1, 2, 3, 4, 5
 
 _D = ctypes.c_double
 _DP = ctypes.POINTER(ctypes.c_double)

@@ -215,13 +215,16 @@ void free_md(MDState& m) {
   cudaFree(m.halo_single_start);
   cudaFree(m.pr_start);
   cudaFree(m.pr_local_end);
+  cudaFree(m.pr_hub_begin);
   cudaFree(m.pr_code);
   cudaFree(m.pr_rest);
   cudaFree(m.pr_m2k);
   cudaFree(m.pi_start);
-  cudaFree(m.pi_list);
+  cudaFree(m.pr_pos);
   cudaFree(m.pl_start);
   cudaFree(m.pl_list);
+  cudaFree(m.pl_base);
+  cudaFree(m.pr_nslot);
   cudaFree(m.hub_slot);
   cudaFree(m.hub_pbase);
   cudaFree(m.hubpart);
@@ -337,10 +340,10 @@ int build_md(mpcd_engine* h) {
   // against 0.215 ms, swimmer128 0.423 against 0.526)
   // contact forces between cilia run on the float64 grid kernel only
   const int arith = h->repel != 0.0 ? 0 : h->p.md_split < 0 ? (h->p.precision == MPCD_FP32 ? 3 : 2) : h->p.md_split;
-  if (arith > 4) return fail(h, MPCD_EINVAL, "md_split must be -1, 0, 1, 2, 3 or 4");
+  if (arith > 5) return fail(h, MPCD_EINVAL, "md_split must be -1 or 0 to 5");
   in.split = arith == 1;
   in.df = arith >= 2;
-  in.pair = arith == 4;
+  in.pair = arith == 4 ? 1 : (arith == 5 ? 2 : 0);
   MDPlan pl;
   // MPCD_MD_NO_CLUSTER=1 keeps split arithmetic on the cooperative grid layout
   const char* no_cl = std::getenv("MPCD_MD_NO_CLUSTER");
@@ -447,27 +450,33 @@ int build_md(mpcd_engine* h) {
     m.pr_nent_max = pl.pr_nent_max;
     m.pr_ninc_max = pl.pr_ninc_max;
     m.pr_nlong_max = pl.pr_nlong_max;
-    const size_t ne = pl.pr_code.size(), ni = pl.pi_list.size(), nlg = pl.pl_list.size();
+    const size_t ne = pl.pr_code.size(), nlg = pl.pl_list.size();
     CK(dalloc(&m.pr_start, m.ntiles + 1));
     CK(dalloc(&m.pr_local_end, m.ntiles));
+    CK(dalloc(&m.pr_hub_begin, m.ntiles));
     CK(dalloc(&m.pr_code, std::max<size_t>(1, ne)));
     CK(dalloc(&m.pr_rest, std::max<size_t>(1, ne)));
     CK(dalloc(&m.pr_m2k, std::max<size_t>(1, ne)));
     CK(dalloc(&m.pi_start, ns + 1));
-    CK(dalloc(&m.pi_list, std::max<size_t>(1, ni)));
+    CK(dalloc(&m.pr_pos, std::max<size_t>(1, ne)));
     CK(dalloc(&m.pl_start, m.ntiles + 1));
     CK(dalloc(&m.pl_list, std::max<size_t>(1, nlg)));
+    CK(dalloc(&m.pl_base, std::max<size_t>(1, nlg)));
+    CK(dalloc(&m.pr_nslot, m.ntiles));
     CK(up(m.pr_start, pl.pr_start.data(), (m.ntiles + 1) * sizeof(int)));
     CK(up(m.pr_local_end, pl.pr_local_end.data(), m.ntiles * sizeof(int)));
+    CK(up(m.pr_hub_begin, pl.pr_hub_begin.data(), m.ntiles * sizeof(int)));
     if (ne) {
       CK(up(m.pr_code, pl.pr_code.data(), ne * sizeof(uint2)));
       CK(up(m.pr_rest, pl.pr_rest.data(), ne * sizeof(double)));
       CK(up(m.pr_m2k, pl.pr_m2k.data(), ne * sizeof(double)));
     }
     CK(up(m.pi_start, pl.pi_start.data(), (ns + 1) * sizeof(int)));
-    if (ni) CK(up(m.pi_list, pl.pi_list.data(), ni * sizeof(uint32_t)));
+    if (ne) CK(up(m.pr_pos, pl.pr_pos.data(), ne * sizeof(uint32_t)));
     CK(up(m.pl_start, pl.pl_start.data(), (m.ntiles + 1) * sizeof(int)));
     if (nlg) CK(up(m.pl_list, pl.pl_list.data(), nlg * sizeof(int)));
+    if (nlg) CK(up(m.pl_base, pl.pl_base.data(), nlg * sizeof(int)));
+    CK(up(m.pr_nslot, pl.pr_nslot.data(), m.ntiles * sizeof(int)));
     // hubs: their slots, the partial sums' offsets and two buffers of them,
     // the tiles' references
     m.nhub = (int)pl.hub_slot.size();
@@ -1651,7 +1660,7 @@ int mpcd_md_layout(mpcd_engine* h, int* info) {
   info[4] = m.nslots;
   info[5] = (int)h->md_nsp;
   info[6] = m.hmax;
-  info[7] = m.pair ? 4 : (m.df ? m.df + 1 : m.split);
+  info[7] = m.pair ? 3 + m.pair : (m.df ? m.df + 1 : m.split);
   return MPCD_OK;
 }
 

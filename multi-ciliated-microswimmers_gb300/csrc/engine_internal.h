@@ -108,7 +108,7 @@ struct HubRef {
   int hub;     // index into the hub tables
   int idx;     // its staged index in the tile (below the tile size: the tile owns it)
   int rank;    // this tile's partial sum among the hub's contributors, or -1
-  int rs, rn;  // the tile's entries whose reaction the hub takes: tr_list[rs, rs + rn)
+  int rs, rn;  // incidence slots holding the forces whose reaction the hub takes: tr_list[rs, rs + rn)
   int pad;
 };
 constexpr int kTileHubs = 4;  // hubs one tile may own or reach
@@ -176,25 +176,28 @@ struct MDState {
   int2* halo_single = nullptr;     // per tile: halo entries outside long runs {slot, rank}
   int* halo_single_start = nullptr;
   float4* q[2] = {nullptr, nullptr};
-  // float64 pair kernel (md_pair.cu), on the layout above with one slot per
-  // bead: per tile its force entries (a spring and its exact reverse inside
-  // the tile form one entry; code {a | b << 16, kind | both << 2 | react << 3
-  // | bond << 4}, rest length, -2k), the entries reaching only the tile's
-  // beads first; per
-  // slot the entries its force sums (entry within the tile << 1 | negate);
-  // per tile the beads with more than kPairLong entries.  Positions are
-  // published as four float64 per slot in q.
-  int pair = 0;
+  // pair kernel (md_pair.cu), on the layout above with one slot per bead:
+  // per tile its force entries (a spring and its exact reverse inside the
+  // tile form one entry; code {a | b << 16, kind | both << 2 | react << 3 |
+  // bond << 4}, rest length, -2k, and the incidence slots its force goes to),
+  // the entries reaching only the tile's beads first, those reaching a hub
+  // last; per slot its range of incidence slots (one per spring of its list,
+  // in its spring order); per tile the beads with more than kPairLong
+  // incidences.  Positions are published as 32 bytes per slot in q.
+  int pair = 0;  // 1 float64, 2 double-float arithmetic
   int pr_nent_max = 0, pr_ninc_max = 0, pr_nlong_max = 0;
   int* pr_start = nullptr;      // ntiles + 1
   int* pr_local_end = nullptr;  // ntiles
+  int* pr_hub_begin = nullptr;  // ntiles: entries reaching a hub come last
   uint2* pr_code = nullptr;
   double* pr_rest = nullptr;
   double* pr_m2k = nullptr;
   int* pi_start = nullptr;      // nslots + 1
-  uint32_t* pi_list = nullptr;
+  uint32_t* pr_pos = nullptr;   // per entry: incidence of its first bead | of its second << 16 (0xffff none)
   int* pl_start = nullptr;      // ntiles + 1
   int* pl_list = nullptr;
+  int* pl_base = nullptr;       // each long bead's first incidence slot
+  int* pr_nslot = nullptr;      // ntiles: incidence slot words (pr_ninc_max: the most of any tile)
   // hubs: per hub its slot and the offsets of its contributors' partial sums
   // (nhub + 1; hub_ncon in all), two buffers of partial sums (four float64
   // each), per tile its hub references and their entry lists

@@ -35,13 +35,16 @@ std::string plan_pair_tables(MDPlan& out, const std::vector<int>& hubs) {
   out.pair = 1;
   out.pr_start.assign(nt + 1, 0);
   out.pr_local_end.assign(nt, 0);
+  out.pr_hub_begin.assign(nt, 0);
   out.pr_code.clear();
   out.pr_rest.clear();
   out.pr_m2k.clear();
   out.pi_start = start;  // one incidence per one-sided spring
-  out.pi_list.assign(nsp, 0u);
+  out.pr_pos.clear();
   out.pl_start.assign(nt + 1, 0);
   out.pl_list.clear();
+  out.pl_base.clear();
+  out.pr_nslot.clear();
   out.pr_nent_max = out.pr_ninc_max = out.pr_nlong_max = 0;
   const int nh = (int)hubs.size();
   std::vector<int> hub_of(ns, -1);
@@ -52,15 +55,35 @@ std::string plan_pair_tables(MDPlan& out, const std::vector<int>& hubs) {
   out.th.clear();
   out.tr_list.clear();
   std::vector<int> ent(nsp, -1);  // spring -> entry of its tile (in creation order)
-  std::vector<char> neg(nsp, 0);
   struct Entry {
     int a, b, kind, both, react, lref, bslot;
     double rest, m2k;
+    int da, db;  // its spring (first bead) and the reverse (second bead), or -1
   };
   std::vector<Entry> es;
+  std::vector<int> lbase(T);
   for (int t = 0; t < nt; ++t) {
     const int base = t * T;
     es.clear();
+    // incidence slots: the j-th spring of a bead a with at most kPairLong
+    // springs at j * T + a (the threads summing consecutive beads read
+    // consecutive words), longer lists one after another beyond T * kmax
+    int kmax = 0, lsum = 0;
+    for (int s = base; s < base + T; ++s)
+      if (start[s + 1] - start[s] <= kPairLong) kmax = std::max(kmax, start[s + 1] - start[s]);
+    for (int s = base; s < base + T; ++s) {
+      lbase[s - base] = -1;
+      if (start[s + 1] - start[s] > kPairLong) {
+        lbase[s - base] = T * kmax + lsum;
+        lsum += start[s + 1] - start[s];
+        out.pl_list.push_back(s - base);
+        out.pl_base.push_back(lbase[s - base]);
+      }
+    }
+    auto slot_pos = [&](int d, int a) {  // spring d of local bead a
+      const int j = d - start[base + a];
+      return lbase[a] >= 0 ? lbase[a] + j : j * T + a;
+    };
     for (int s = base; s < base + T; ++s)
       for (int d = start[s]; d < start[s + 1]; ++d) {
         if (ent[d] >= 0) continue;  // the reverse half of an entry made before
@@ -69,7 +92,7 @@ std::string plan_pair_tables(MDPlan& out, const std::vector<int>& hubs) {
         if (react && hub_of[out.so[d]] < 0) return "pair kernel: a reaction spring whose other bead is not a hub";
         const int a = s - base, b = out.sl[d], kind = out.sk[d] & 3;
         const int lref = kind >= MPCD_SPRING_BOND ? out.sr[d] - out.df_b0[t] : 0;
-        Entry e{a, b, kind, 0, react, lref, out.so[d], out.srest[d], out.sm2k[d]};
+        Entry e{a, b, kind, 0, react, lref, out.so[d], out.srest[d], out.sm2k[d], d, -1};
         ent[d] = (int)es.size();
         if (b < T && b != a && !react) {
           const int so = base + b;
@@ -77,24 +100,26 @@ std::string plan_pair_tables(MDPlan& out, const std::vector<int>& hubs) {
             if (ent[r] >= 0 || out.so[r] != s || out.sk[r] != out.sk[d] || out.sm2k[r] != out.sm2k[d]) continue;
             if (kind >= MPCD_SPRING_BOND ? out.sr[r] != out.sr[d] : out.srest[r] != out.srest[d]) continue;
             ent[r] = (int)es.size();
-            neg[r] = 1;
             e.both = 1;
+            e.db = r;
             break;
           }
         }
         es.push_back(e);
       }
     // the entries reaching only this tile's beads first (they run while the
-    // halo loads); those reaching a hub wait for its partial sums, which
-    // arrive with the halo
-    std::vector<int> order, rank(es.size());
-    auto local = [&](const Entry& e) { return e.b < T && hub_of[e.bslot] < 0; };
+    // halo loads), then those reaching the halo, then those reaching a hub
+    // (after its copy has been advanced)
+    std::vector<int> order;
+    auto to_hub = [&](const Entry& e) { return hub_of[e.bslot] >= 0; };
     for (size_t i = 0; i < es.size(); ++i)
-      if (local(es[i])) order.push_back((int)i);
+      if (es[i].b < T && !to_hub(es[i])) order.push_back((int)i);
     const int nloc = (int)order.size();
     for (size_t i = 0; i < es.size(); ++i)
-      if (!local(es[i])) order.push_back((int)i);
-    for (size_t i = 0; i < order.size(); ++i) rank[order[i]] = (int)i;
+      if (es[i].b >= T && !to_hub(es[i])) order.push_back((int)i);
+    const int nhub0 = (int)order.size();
+    for (size_t i = 0; i < es.size(); ++i)
+      if (to_hub(es[i])) order.push_back((int)i);
     const int g0 = (int)out.pr_code.size();
     // hubs this tile owns or reaches, with the entries whose reaction each takes
     std::vector<HubRef> refs;
@@ -117,10 +142,14 @@ std::string plan_pair_tables(MDPlan& out, const std::vector<int>& hubs) {
                                            ((uint32_t)e.lref << 4)));
       out.pr_rest.push_back(e.rest);
       out.pr_m2k.push_back(e.m2k);
+      // the incidence slots its force (first bead) and negated force (second) go to
+      const int ka = slot_pos(e.da, e.a), kb = e.db >= 0 ? slot_pos(e.db, e.b) : 0xffff;
+      if (ka < 0 || ka >= 0xffff || kb < 0 || kb > 0xffff) return "pair kernel: an MD tile has too many springs";
+      out.pr_pos.push_back((uint32_t)ka | ((uint32_t)kb << 16));
       if (hub_of[e.bslot] >= 0) {
         const int k = ref_of(hub_of[e.bslot], e.b);
         if (refs[k].idx != e.b) return "pair kernel: a hub staged twice in one tile";
-        if (e.react) rlist[k].push_back((int)r);
+        if (e.react) rlist[k].push_back(ka);  // the reaction is read from the first bead's slot
       }
     }
     if ((int)refs.size() > kTileHubs) return "hub";
@@ -133,16 +162,13 @@ std::string plan_pair_tables(MDPlan& out, const std::vector<int>& hubs) {
     }
     out.th_start[t + 1] = (int)out.th.size();
     out.pr_local_end[t] = g0 + nloc;
+    out.pr_hub_begin[t] = g0 + nhub0;
     out.pr_start[t + 1] = (int)out.pr_code.size();
     out.pr_nent_max = std::max(out.pr_nent_max, (int)es.size());
-    // per slot: the entries its force sums, in its spring order
-    for (int s = base; s < base + T; ++s) {
-      for (int d = start[s]; d < start[s + 1]; ++d) out.pi_list[d] = ((uint32_t)rank[ent[d]] << 1) | (uint32_t)neg[d];
-      if (start[s + 1] - start[s] > kPairLong) out.pl_list.push_back(s - base);
-    }
     out.pl_start[t + 1] = (int)out.pl_list.size();
+    out.pr_nslot.push_back(T * kmax + lsum);
     out.pr_nlong_max = std::max(out.pr_nlong_max, out.pl_start[t + 1] - out.pl_start[t]);
-    out.pr_ninc_max = std::max(out.pr_ninc_max, start[base + T] - start[base]);
+    out.pr_ninc_max = std::max(out.pr_ninc_max, T * kmax + lsum);
   }
   out.hub_pbase.assign(nh + 1, 0);
   for (int h = 0; h < nh; ++h) out.hub_pbase[h + 1] = out.hub_pbase[h] + ncon[h];
@@ -497,7 +523,8 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
   // forces, which the tiles holding the partners add up and publish, and
   // every tile that reaches the hub integrates a copy of it.
   std::vector<char> phub(nb, 0);
-  if (in.pair && !no_react) {
+  const char* nh_env = std::getenv("MPCD_MD_NO_HUBS");  // 1: hubs keep their own lists (diagnostics)
+  if (in.pair && !no_react && !(nh_env && std::atoi(nh_env))) {
     auto candidate = [&](long b) { return owner[b] < 0 && nspr[b] > kPairLong; };
     for (long b = 0; b < nb; ++b) {
       if (!candidate(b)) continue;
@@ -748,6 +775,7 @@ std::string plan_md(const MDInput& in, const MDForce& force, bool allow_cluster,
     const std::string e = plan_pair_tables(out, hub_slots);
     if (e == "hub") return plan_md(in, force, allow_cluster, true, grid_f32cells, out, min_tile);  // no hubs then
     if (!e.empty()) return e;
+    out.pair = in.pair;
   }
   MDState probe;  // the fields the feasibility checks read
   probe.pair = out.pair;

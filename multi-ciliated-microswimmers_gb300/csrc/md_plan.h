@@ -26,7 +26,7 @@ struct MDInput {
   const double *newlen = nullptr, *oldlen = nullptr;
   int split = 0;  // 1: float spring arithmetic on hi/lo position pairs
   int df = 0;     // 1: double-float arithmetic (md_df.cu; grid layout, split 0)
-  int pair = 0;   // 1 (with df 1): the float64 pair kernel (md_pair.cu) on the grid layout
+  int pair = 0;   // with df 1: the pair kernel (md_pair.cu) on the grid layout, 1 float64, 2 double-float
 };
 
 // A fixed cluster layout (lanes per slot, slots per tile), or {0, 0} to let
@@ -57,19 +57,24 @@ struct MDPlan {
   std::vector<int2> df_single;     // other halo entries {slot, staged rank}
   std::vector<int> df_single_start;
   int df_nsp_max = 0, df_nb_max = 0, df_nrun_max = 0, df_nsingle_max = 0;
-  // float64 pair kernel (md_pair.cu): per tile its force entries (a spring
-  // and its exact reverse inside the tile form one entry), the entries
-  // reaching only the tile's own beads first; per slot the entries its force
-  // sums, in its spring order (entry << 1 | 1 when the entry's force is
-  // negated for it); per tile the beads with long lists (summed by warps)
+  // pair kernel (md_pair.cu): per tile its force entries (a spring and its
+  // exact reverse inside the tile form one entry), the entries reaching only
+  // the tile's own beads first, those reaching a hub last; per entry the
+  // incidence slots its force (and, for its second bead, the negated force)
+  // is written to: a bead's incidences are its springs in its spring order,
+  // so that its force is the sum of a contiguous range; per tile the beads
+  // with long lists (summed by warps)
   int pair = 0;
   std::vector<int> pr_start, pr_local_end;  // ntiles + 1, ntiles (global entry offsets)
+  std::vector<int> pr_hub_begin;            // ntiles: the first entry reaching a hub
   std::vector<uint2> pr_code;  // {a | b << 16, kind | both << 2 | react << 3 | bond << 4}
   std::vector<double> pr_rest, pr_m2k;
   std::vector<int> pi_start;                // nslots + 1
-  std::vector<uint32_t> pi_list;            // entry index within the tile << 1 | negate
+  std::vector<uint32_t> pr_pos;  // per entry: its first bead's incidence | its second's << 16 (0xffff: none)
   std::vector<int> pl_start, pl_list;       // ntiles + 1; local slot of each long bead
-  int pr_nent_max = 0, pr_ninc_max = 0, pr_nlong_max = 0;
+  std::vector<int> pl_base;                 // each long bead's first incidence slot
+  std::vector<int> pr_nslot;                // ntiles: incidence slot words of the tile
+  int pr_nent_max = 0, pr_ninc_max = 0, pr_nlong_max = 0;  // pr_ninc_max: most slot words of a tile
   // hubs of the pair kernel (engine_internal.h, HubRef)
   std::vector<int> hub_slot, hub_pbase;  // nhub, nhub + 1
   std::vector<int> th_start;             // ntiles + 1

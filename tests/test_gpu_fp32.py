@@ -35,7 +35,7 @@ def test_fp32_fluid_tracks_reference_golden():
     assert np.mean(dv < 2e-4) > 0.995
 
 
-@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_DF, cg.MD_SPLIT, cg.MD_FLOAT, cg.MD_PAIR])
+@pytest.mark.parametrize("arith", [cg.MD_AUTO, cg.MD_DF, cg.MD_SPLIT, cg.MD_FLOAT, cg.MD_PAIR, cg.MD_PAIR_DF])
 def test_fp32_swimmer_tracks_reference_golden(arith):
     """MD in split arithmetic on the double-float kernel's grid layout (the
     default of the float32 path), in double-float, in split arithmetic on

@@ -58,7 +58,7 @@ def test_fluid_matches_reference_golden(case):
     assert abs(obs["diss_energy"] - g[f"step{int(steps)}_meta"][1]) < 1e-8 * max(1, abs(g[f"step{int(steps)}_meta"][1]))
 
 
-@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64, cg.MD_PAIR])
+@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64, cg.MD_PAIR, cg.MD_PAIR_DF])
 @pytest.mark.parametrize("case", ["clami10", "objects8"])
 def test_swimmer_matches_reference_golden(case, arith):
     """MD substeps in double-float (the float64 path's default) and in float64."""
@@ -91,7 +91,9 @@ def test_swimmer_matches_reference_golden(case, arith):
 @pytest.mark.parametrize("arith,bulk,min_tile", [(cg.MD_DF, False, 0), (cg.MD_DF, True, 0), (cg.MD_F64, False, 0),
                                                   (cg.MD_DF, False, 128), (cg.MD_DF, False, 256),
                                                   (cg.MD_PAIR, False, 0), (cg.MD_PAIR, True, 0),
-                                                  (cg.MD_PAIR, False, 128), (cg.MD_PAIR, False, 256)])
+                                                  (cg.MD_PAIR, False, 128), (cg.MD_PAIR, False, 256),
+                                                  (cg.MD_PAIR_DF, False, 0), (cg.MD_PAIR_DF, True, 0),
+                                                  (cg.MD_PAIR_DF, False, 128), (cg.MD_PAIR_DF, False, 256)])
 def test_multi_tile_swimmer_matches_oracle(arith, bulk, min_tile, monkeypatch):
     """A Clami whose cilia fill many MD tiles (halos between tiles, a sphere
     centre with helper slots) against the C oracle, injected randomness, 6 MPC
@@ -99,8 +101,9 @@ def test_multi_tile_swimmer_matches_oracle(arith, bulk, min_tile, monkeypatch):
     two or more slots by bulk asynchronous copies (TMA) instead of per-entry
     cp.async.  min_tile: the wide tiles that large swimmers get when the
     narrow grid would not be co-resident (128 slots at four lanes per slot,
-    256 at two).  MD_PAIR: float64 with each spring pair inside a tile
-    evaluated once and the sphere centre's long list summed by warps."""
+    256 at two).  MD_PAIR / MD_PAIR_DF: float64 / double-float with each
+    spring pair inside a tile evaluated once and the sphere centre integrated
+    from its partners' reactions."""
     if bulk:
         monkeypatch.setenv("MPCD_MD_LONG_RUN", "2")
     if min_tile:

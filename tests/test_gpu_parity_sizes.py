@@ -70,7 +70,7 @@ def test_plain32_matches_oracle(precision):
         assert np.mean(dp < 2e-4) > 0.999 and np.mean(dv < 2e-4) > 0.999, (np.sort(dp)[-3:], np.sort(dv)[-3:])
 
 
-@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64, cg.MD_PAIR])
+@pytest.mark.parametrize("arith", [cg.MD_DF, cg.MD_F64, cg.MD_PAIR, cg.MD_PAIR_DF])
 def test_swimmer64_matches_oracle(arith):
     cfg = simcfg.baseline_config("swimmer64", seed=3)
     o = build_from_cfg(cfg, seed=5, ststep=0.002)
@@ -79,7 +79,7 @@ def test_swimmer64_matches_oracle(arith):
     lay = e.md_layout()
     assert lay["arith"] == arith
     assert s.nbeads == o.bead_count() == 643 + 100 * 45
-    if arith == cg.MD_PAIR:
+    if arith in (cg.MD_PAIR, cg.MD_PAIR_DF):
         # the sphere centre's 642 radial springs are dropped: its force is the
         # negated sum of the surface beads' reactions
         d = cg.Sim(simcfg.dumps(cfg), precision=cg.MPCD_FP64, ststep=0.002, create_fluid=False, md_arith=cg.MD_DF)

@@ -125,34 +125,40 @@ def test_free_sphere_conserves_momentum(precision):
 
 
 def test_held_sphere_stokes_drag():
+    """Stokes drag of a held sphere in a periodic box, three runs (the ratio
+    below varies by about 7 % from run to run: the mean fluid velocity U over
+    100 samples is noisy), their mean within 15 % of Hasimoto's factor."""
     L = (16, 16, 16)
     R = 3.0
     g = 0.001
-    sp = dict(center=(8.0, 8.0, 8.0), radius=R)
-    pos, vel = fluid_outside(L, [sp], seed=3)
-    nf = len(pos)
-    e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=cg.MPCD_FP32, seed=11, gravity=g)
-    e.set_fluid(pos, vel)
-    e.set_rigid_spheres([sp])
-    e.run(4000)
-    e.reset_sphere_forces()
-    us = []
-    for _ in range(100):
-        e.run(40)
-        us.append(e.observables()["momentum"][0])
-    (s1,), ft = e.rigid_spheres()
-    F = ft[0, 0]
-    U = float(np.mean(us))
-    # momentum balance of the steady state: the sphere holds the fluid against the body force
-    assert abs(F - nf * g) < 0.05 * nf * g, (F, nf * g)
     c = 4.0 / 3.0 * np.pi * R ** 3 / np.prod(L)
     K = 1.0 / (1.0 - 1.7601 * c ** (1.0 / 3.0) + c - 1.5593 * c * c)
     eta = 8.70
-    ratio = F / (6 * np.pi * eta * R * U) / K
-    print("stokes", dict(F=F, U=U, K=K, ratio=ratio))
-    assert abs(ratio - 1.0) < 0.15, ratio
-    # the held sphere did not move
-    assert np.array_equal(s1["center"], np.array(sp["center"])) and not s1["velocity"].any()
+    ratios = []
+    for run in range(3):
+        sp = dict(center=(8.0, 8.0, 8.0), radius=R)
+        pos, vel = fluid_outside(L, [sp], seed=3 + run)
+        nf = len(pos)
+        e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=cg.MPCD_FP32, seed=11 + run, gravity=g)
+        e.set_fluid(pos, vel)
+        e.set_rigid_spheres([sp])
+        e.run(4000)
+        e.reset_sphere_forces()
+        us = []
+        for _ in range(100):
+            e.run(40)
+            us.append(e.observables()["momentum"][0])
+        (s1,), ft = e.rigid_spheres()
+        F = ft[0, 0]
+        U = float(np.mean(us))
+        # momentum balance of the steady state: the sphere holds the fluid against the body force
+        assert abs(F - nf * g) < 0.05 * nf * g, (F, nf * g)
+        ratios.append(F / (6 * np.pi * eta * R * U) / K)
+        # the held sphere did not move
+        assert np.array_equal(s1["center"], np.array(sp["center"])) and not s1["velocity"].any()
+        e.close()
+    print("stokes", dict(K=K, ratios=ratios))
+    assert abs(np.mean(ratios) - 1.0) < 0.15, ratios
 
 
 def test_rigid_sphere_arguments_rejected():
