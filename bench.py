@@ -186,8 +186,9 @@ def run_gpu(args, rank=0, md_arith=None, steps=None, workload=None, precision=No
     prec = cg.MPCD_FP64 if precision == "fp64" else cg.MPCD_FP32
     cfg = workload_cfg(workload, seed=1000 + rank)
     text = simcfg.dumps(cfg)
-    sim = cg.Sim(text, precision=prec, seed=1000 + rank, device=args.device,
-                 md_arith=cg.MD_AUTO if md_arith is None else md_arith)
+    if md_arith is None:  # --md-arith for the main line (profiling runs of one MD kernel)
+        md_arith = {"auto": cg.MD_AUTO, "pair": cg.MD_PAIR, "pair-df": cg.MD_PAIR_DF}[getattr(args, "md_arith", "auto")]
+    sim = cg.Sim(text, precision=prec, seed=1000 + rank, device=args.device, md_arith=md_arith)
     steps = args.steps if steps is None else steps
     eng = sim.engine
     nf = len(eng.fluid()[1]) if args.verify_counts else int(cfg["sizex"]) ** 3 * 10
@@ -598,6 +599,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="swimmer64", choices=["swimmer64", "swimmer128", "plain32"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--md-arith", default="auto", choices=["auto", "pair", "pair-df"],
+                    help="MD arithmetic of the main line (auto: the default; pair: float64 pair kernel)")
     ap.add_argument("--device", type=int, default=None)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
