@@ -211,7 +211,11 @@ __device__ __forceinline__ void collision_map(double4 s, uint32_t w, long cid, c
     } else {
       g = (double)gamma_mt(num, a.seed, a.step, (uint32_t)cid, &gfail);
     }
-    sc = sqrt(g / (erel * 0.5));
+    // sqrt(g / (erel / 2)) = 2g / sqrt(2g erel): one reciprocal square root in
+    // place of a float64 division and square root (the cell pass is bound
+    // by the float64 pipe); outside the float range the direct form
+    const double q = 2.0 * g, x = q * erel;
+    sc = (x > 1e-30 && x < 1e30) ? q * rsqrt_f64(x) : sqrt(g / (erel * 0.5));
   }
   double rx, ry, rz;
   if (a.inj_axis) {

@@ -63,17 +63,6 @@ __device__ __forceinline__ double flip_sign(double v, uint32_t w) {
   return __hiloint2double(__double2hiint(v) ^ (int)((w & 1u) << 31), __double2loint(v));
 }
 
-// 1 / sqrt(d2) for a positive normal d2: the float reciprocal square root
-// (relative error about 2^-23) refined by one cubic step of the Householder
-// iteration for f(y) = y^-2 - d2: with r = 1 - d2 y^2, y' = y + y r (1/2 + 3/8 r),
-// whose error is of order r^3 (about 2^-69), below float64 rounding; five
-// float64 operations
-__device__ __forceinline__ double rsqrt_f64(double d2) {
-  const double y = (double)rsqrtf((float)d2);
-  const double r = fma(-d2 * y, y, 1.0);
-  return fma(y * r, fma(0.375, r, 0.5), y);
-}
-
 struct StagePair {
   const Pos4* p;
   __device__ double dist(int i, int j) const {

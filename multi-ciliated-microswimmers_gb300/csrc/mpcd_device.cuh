@@ -195,4 +195,17 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned target,
   return ok != 0;
 }
 
+// 1 / sqrt(x) for x in the float range (about 1e-30 to 1e30): the float
+// reciprocal square root (relative error about 2^-23) refined by one cubic
+// step of the Householder iteration for f(y) = y^-2 - x: with r = 1 - x y^2,
+// y' = y + y r (1/2 + 3/8 r), whose error is of order r^3 (about 2^-69), below
+// float64 rounding (within about one ulp, like the library's rsqrt); five
+// float64 operations, where GB300's float64 division and square root cost
+// several times more
+__device__ __forceinline__ double rsqrt_f64(double x) {
+  const double y = (double)rsqrtf((float)x);
+  const double r = fma(-x * y, y, 1.0);
+  return fma(y * r, fma(0.375, r, 0.5), y);
+}
+
 }  // namespace mpcd
