@@ -41,7 +41,8 @@ typedef struct {
   int md_arith;            /* MD arithmetic: 0 auto (double-float for float64, float springs on
                               double-float positions for float32), else mpcd_params.md_split + 1
                               (1 float64, 2 split, 3 double-float, 4 float springs on the
-                              double-float layout, 5 float64 pair kernel) */
+                              double-float layout, 5 float64 pair kernel, 6 double-float pair
+                              kernel) */
 } cilia_options;
 
 /* cfg is a file path, or libconfig text when is_text != 0 */

@@ -75,7 +75,7 @@ typedef struct {
                             3 float springs (split arithmetic) on the layout of 2,
                             4 float64 with each spring and its reverse evaluated once and a
                             sphere centre's force summed from its partners' reactions
-                            (faster than 0 on GB300) */
+                            (faster than 0 on GB300), 5 the same in double-float */
 } mpcd_params;
 
 /* Values that replace the generator for one step (all host arrays).  Used to
@@ -198,9 +198,10 @@ int mpcd_kernel_time(mpcd_engine* h, int kernel, double* total_ms, long long* la
  * info[8] receives: cluster (1: one thread-block cluster, 0: cooperative
  * grid), threads per slot, slots per tile, tiles (CTAs), slots, springs,
  * largest halo of a tile, arithmetic (0 float64, 1 split, 2 double-float,
- * 3 float springs on the double-float layout, 4 float64 pair kernel; for 4
- * "threads per slot" is the CTA's threads over its slots, and springs
- * excludes the dropped lists of sphere centres). */
+ * 3 float springs on the double-float layout, 4 float64 pair kernel, 5
+ * double-float pair kernel; for 4 and 5 "threads per slot" is the CTA's
+ * threads over its slots, and springs excludes the dropped lists of sphere
+ * centres). */
 int mpcd_md_layout(mpcd_engine* h, int* info);
 
 /* Lossless snapshots of a handle's whole state, for checkpoints that keep
