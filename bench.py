@@ -238,10 +238,12 @@ def roofline(nf, kernels, precision):
 def run_e2e(args):
     """Through the C ABI with host buffers, over a fixed window of E2E_STEPS
     steps: upload of the fluid (the swimmer is built on the host and uploaded
-    with the Sim), every step followed by an observables read-back, final
-    download of fluid and beads; wall clock."""
+    with the Sim), every step followed by an observables read-back (enqueued
+    with mpcd_observables_async, collected inside the window), final download
+    of fluid and beads; wall clock."""
     import cilia_gpu as cg
 
+    assert E2E_STEPS <= cg.OBS_RING
     prec = cg.MPCD_FP64 if args.precision == "fp64" else cg.MPCD_FP32
     cfg = workload_cfg(args.workload, seed=77)
     L = int(cfg["sizex"])
@@ -259,15 +261,22 @@ def run_e2e(args):
     eng.set_fluid(pos, vel)
     for _ in range(3):
         eng.step()
-        eng.observables()
+        eng.observables_result(eng.observables_async())
     eng.fluid()
     t0 = time.perf_counter()
     eng.set_fluid(pos, vel)
     t1 = time.perf_counter()
+    # each step's observables are enqueued behind it and all are collected
+    # inside the window: the read-backs are all done, the host just does not
+    # stall the next step on them
+    tickets = []
     for _ in range(E2E_STEPS):
         eng.step()
-        eng.observables()
+        tickets.append(eng.observables_async())
+    obs = [eng.observables_result(t) for t in tickets]
     t2 = time.perf_counter()
+    if not all(np.isfinite(o["kT"]) for o in obs):
+        raise RuntimeError("non-finite observables in the end-to-end window")
     p, v = eng.fluid()
     bp, bv = sim.beads()
     t3 = time.perf_counter()

@@ -170,6 +170,16 @@ int mpcd_step(mpcd_engine* h, const mpcd_inject* inj);
 /* nsteps free-running MPC steps; observables read back only at the end */
 int mpcd_run(mpcd_engine* h, int nsteps);
 int mpcd_observables(mpcd_engine* h, mpcd_obs* out);
+/* The same observables without stalling the host: mpcd_observables_async
+ * enqueues the sums of the current state on the handle's stream and returns a
+ * ticket at once; mpcd_observables_result waits for that ticket's read-back
+ * only (not for steps issued after it) and fills out as mpcd_observables does,
+ * globalt included.  The newest MPCD_OBS_RING tickets can be collected, in any
+ * order and more than once; an older or never-issued ticket is MPCD_EINVAL.
+ * No counterpart in the reference (MPCD::debug prints at once). */
+#define MPCD_OBS_RING 256
+int mpcd_observables_async(mpcd_engine* h, long long* ticket);
+int mpcd_observables_result(mpcd_engine* h, long long ticket, mpcd_obs* out);
 int mpcd_reset_diss(mpcd_engine* h);
 /* waits for the handle's stream; reports device-side errors */
 int mpcd_sync(mpcd_engine* h);

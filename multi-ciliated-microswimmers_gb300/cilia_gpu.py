@@ -26,6 +26,7 @@ K_CELL, K_FLUID, K_BEAD, K_MD, K_SORT = 0, 1, 2, 3, 4
 # layout), double-float, float springs on the double-float grid layout,
 # float64 and double-float with each spring pair evaluated once (pair kernel)
 MD_AUTO, MD_F64, MD_SPLIT, MD_DF, MD_FLOAT, MD_PAIR, MD_PAIR_DF = -1, 0, 1, 2, 3, 4, 5
+OBS_RING = 256  # observables tickets a handle keeps collectable (MPCD_OBS_RING)
 
 _D = ctypes.c_double
 _DP = ctypes.POINTER(ctypes.c_double)
@@ -140,6 +141,8 @@ def lib():
             "mpcd_step": (ctypes.c_int, [P, ctypes.POINTER(MpcdInject)]),
             "mpcd_run": (ctypes.c_int, [P, ctypes.c_int]),
             "mpcd_observables": (ctypes.c_int, [P, ctypes.POINTER(MpcdObs)]),
+            "mpcd_observables_async": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
+            "mpcd_observables_result": (ctypes.c_int, [P, ctypes.c_longlong, ctypes.POINTER(MpcdObs)]),
             "mpcd_reset_diss": (ctypes.c_int, [P]),
             "mpcd_sync": (ctypes.c_int, [P]),
             "mpcd_launch_count": (ctypes.c_longlong, [P]),
@@ -364,6 +367,19 @@ class Engine:
     def observables(self):
         o = MpcdObs()
         self._ck(lib().mpcd_observables(self._h, ctypes.byref(o)), "observables")
+        return dict(momentum=np.array(o.momentum[:]), n=o.n, mass=o.mass, kT=o.kT, fluid_T=o.fluid_T,
+                    diss_energy=o.diss_energy, globalt=o.globalt, energy_fluid=o.energy_fluid)
+
+    def observables_async(self):
+        """Enqueues the observables of the current state; returns a ticket for
+        observables_result (the newest OBS_RING tickets stay collectable)."""
+        t = ctypes.c_longlong(0)
+        self._ck(lib().mpcd_observables_async(self._h, ctypes.byref(t)), "observables_async")
+        return t.value
+
+    def observables_result(self, ticket):
+        o = MpcdObs()
+        self._ck(lib().mpcd_observables_result(self._h, ticket, ctypes.byref(o)), "observables_result")
         return dict(momentum=np.array(o.momentum[:]), n=o.n, mass=o.mass, kT=o.kT, fluid_T=o.fluid_T,
                     diss_energy=o.diss_energy, globalt=o.globalt, energy_fluid=o.energy_fluid)
 

@@ -27,6 +27,10 @@
 
 using namespace mpcd;
 
+namespace {
+constexpr int kObsSlot = 16;  // doubles per observables ring slot (10 used; 128-byte slots)
+}
+
 struct mpcd_engine {
   mpcd_params p{};
   Box box{};
@@ -49,7 +53,14 @@ struct mpcd_engine {
   unsigned* d_err = nullptr;
   double* d_diss = nullptr;
   double* d_obs = nullptr;
-  double* h_obs = nullptr;  // pinned: observables, dissipated energy and error bits of one read-back
+  // observables read-backs in flight: ticket t lands in slot t % MPCD_OBS_RING
+  // of a pinned ring (kObsSlot doubles: the sums, the dissipated energy, the
+  // error word), its copy marked by that slot's event
+  double* h_ring = nullptr;
+  cudaEvent_t ring_ev[MPCD_OBS_RING] = {};
+  double ring_t[MPCD_OBS_RING] = {};       // globalt when the ticket was taken
+  unsigned char ring_raw[MPCD_OBS_RING] = {};  // 1: error word copied as raw bits, 0: as a double
+  long long obs_next = 0;                  // the next ticket
   double* d_obs_part = nullptr;     // per-block partials of the cell-sum observables
   unsigned* d_obs_count = nullptr;  // blocks finished (reset by the last one)
   unsigned* d_bar = nullptr;
@@ -604,11 +615,7 @@ int pull_md(mpcd_engine* h) {
   return MPCD_OK;
 }
 
-int device_error(mpcd_engine* h) {
-  unsigned e = 0;
-  CK(cudaStreamSynchronize(h->stream));
-  CK(cudaMemcpy(&e, h->d_err, sizeof e, cudaMemcpyDeviceToHost));
-  if (e == 0) return MPCD_OK;
+static std::string error_text(unsigned e) {
   std::string msg = "device check failed:";
   if (e & kErrGammaMissing) msg += " injected gamma missing for a thermostatted cell;";
   if (e & kErrGammaLoop) msg += " Gamma sampler exceeded its iteration cap;";
@@ -616,8 +623,16 @@ int device_error(mpcd_engine* h) {
   if (e & kErrCellRange) msg += " non-finite or out-of-range coordinate (unstable MD step?);";
   if (e & kErrCellOverflow) msg += " cell occupancy overflow;";
   if (e & kErrLayout) msg += " MD shared-memory layout mismatch;";
+  return msg;
+}
+
+int device_error(mpcd_engine* h) {
+  unsigned e = 0;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(&e, h->d_err, sizeof e, cudaMemcpyDeviceToHost));
+  if (e == 0) return MPCD_OK;
   cudaMemset(h->d_err, 0, sizeof(unsigned));
-  return fail(h, MPCD_EDEVICE, msg);
+  return fail(h, MPCD_EDEVICE, error_text(e));
 }
 
 // brackets one launch with events when profiling is on
@@ -755,7 +770,8 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
   if ((e = dalloc(&h->d_err, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_diss, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs, 16)) != cudaSuccess) return bail(e, "alloc");
-  if ((e = cudaMallocHost((void**)&h->h_obs, 16 * sizeof(double))) != cudaSuccess) return bail(e, "alloc");
+  if ((e = cudaMallocHost((void**)&h->h_ring, kObsSlot * sizeof(double) * MPCD_OBS_RING)) != cudaSuccess)
+    return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs_part, 7 * (size_t)kObsBlocks)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs_count, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = cudaMemset(h->d_obs_count, 0, sizeof(unsigned))) != cudaSuccess) return bail(e, "alloc");
@@ -817,7 +833,9 @@ int mpcd_destroy(mpcd_engine* h) {
   cudaFree(h->d_err);
   cudaFree(h->d_diss);
   cudaFree(h->d_obs);
-  cudaFreeHost(h->h_obs);
+  cudaFreeHost(h->h_ring);
+  for (cudaEvent_t ev : h->ring_ev)
+    if (ev) cudaEventDestroy(ev);
   cudaFree(h->d_obs_part);
   cudaFree(h->d_obs_count);
   cudaFree(h->d_bar);
@@ -1243,22 +1261,29 @@ int mpcd_reset_diss(mpcd_engine* h) {
   return MPCD_OK;
 }
 
-int mpcd_observables(mpcd_engine* h, mpcd_obs* out) {
-  if (!h || !out) return MPCD_EINVAL;
+// Enqueues the observables of the current state behind the work issued so far
+// and returns at once; no counterpart in the reference (MPCD::debug,
+// src/libcilia/mpcd.cpp:404-467, sums and prints in one go).  The sums land in
+// ring slot ticket % MPCD_OBS_RING; every later call on the handle is ordered
+// after their copy on the stream, so the next step runs while the host has not
+// yet read them.
+int mpcd_observables_async(mpcd_engine* h, long long* ticket) {
+  if (!h || !ticket) return MPCD_EINVAL;
   if (h->md_dirty && h->nb) {
     int rc = build_md(h);
     if (rc) return rc;
   }
-  double* o = h->h_obs;  // pinned: the sums, the dissipated energy, the error bits
-  unsigned err_bits = 0;
+  const long long t = h->obs_next;
+  const int slot = (int)(t % MPCD_OBS_RING);
+  double* o = h->h_ring + (size_t)slot * kObsSlot;
+  if (!h->ring_ev[slot]) CK(cudaEventCreateWithFlags(&h->ring_ev[slot], cudaEventDisableTiming));
   if (h->p.precision == MPCD_FP64 && h->prepared) {
     // the cell sums of the last binning (the state has not changed since: every
     // setter clears `prepared`) hold the totals; one kernel, one read-back
     h->launches += launch_observables_cells_f64(h->c64, h->md, h->p.bead_mass, h->d_diss, h->d_err, h->d_obs_part,
                                                 h->d_obs_count, h->d_obs, h->stream);
     CK(cudaMemcpyAsync(o, h->d_obs, 10 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    err_bits = (unsigned)o[9];
+    h->ring_raw[slot] = 0;
   } else {
     CK(cudaMemsetAsync(h->d_obs, 0, 8 * sizeof(double), h->stream));
     if (h->p.precision == MPCD_FP64)
@@ -1268,9 +1293,32 @@ int mpcd_observables(mpcd_engine* h, mpcd_obs* out) {
     CK(cudaMemcpyAsync(o, h->d_obs, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(o + 8, h->d_diss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(o + 9, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    std::memcpy(&err_bits, o + 9, sizeof err_bits);
+    h->ring_raw[slot] = 1;
   }
+  CK(cudaEventRecord(h->ring_ev[slot], h->stream));
+  h->ring_t[slot] = h->globalt;
+  h->obs_next = t + 1;
+  *ticket = t;
+  return MPCD_OK;
+}
+
+// Waits for the read-back of one ticket (not for later work on the stream) and
+// converts it as mpcd_observables does.
+int mpcd_observables_result(mpcd_engine* h, long long ticket, mpcd_obs* out) {
+  if (!h || !out) return MPCD_EINVAL;
+  if (ticket < 0 || ticket >= h->obs_next)
+    return fail(h, MPCD_EINVAL, "observables ticket " + std::to_string(ticket) + " was not issued");
+  if (ticket < h->obs_next - MPCD_OBS_RING)
+    return fail(h, MPCD_EINVAL, "observables ticket " + std::to_string(ticket) + " was overwritten (more than " +
+                                    std::to_string(MPCD_OBS_RING) + " newer tickets)");
+  const int slot = (int)(ticket % MPCD_OBS_RING);
+  CK(cudaEventSynchronize(h->ring_ev[slot]));
+  const double* o = h->h_ring + (size_t)slot * kObsSlot;
+  unsigned err_bits = 0;
+  if (h->ring_raw[slot])
+    std::memcpy(&err_bits, o + 9, sizeof err_bits);
+  else
+    err_bits = (unsigned)o[9];
   const double diss = o[8];
   const double M = o[5] > 0 ? o[5] : 1.0, N = o[4] > 0 ? o[4] : 1.0;
   out->momentum[0] = o[0] / M;
@@ -1281,9 +1329,19 @@ int mpcd_observables(mpcd_engine* h, mpcd_obs* out) {
   out->kT = o[3] / 3.0 / N;
   out->fluid_T = o[7] > 0 ? o[6] / o[7] / 3.0 : 0.0;
   out->diss_energy = diss;
-  out->globalt = h->globalt;
+  out->globalt = h->ring_t[slot];
   out->energy_fluid = 0.5 * o[6];
-  return err_bits ? device_error(h) : MPCD_OK;
+  if (!err_bits) return MPCD_OK;
+  // the error word as it was at the ticket (a later call may have cleared it)
+  const int rc = device_error(h);
+  return rc ? rc : fail(h, MPCD_EDEVICE, error_text(err_bits));
+}
+
+int mpcd_observables(mpcd_engine* h, mpcd_obs* out) {
+  if (!h || !out) return MPCD_EINVAL;
+  long long t = 0;
+  const int rc = mpcd_observables_async(h, &t);
+  return rc ? rc : mpcd_observables_result(h, t, out);
 }
 
 int mpcd_timed_run(mpcd_engine* h, int nsteps, int flush_l2, double* step_ms) {

@@ -282,6 +282,44 @@ def test_observables_from_cell_sums_match_particle_sums():
     s.close()
 
 
+@pytest.mark.parametrize("precision", [cg.MPCD_FP64, cg.MPCD_FP32])
+def test_async_observables_match_sync_and_reject_stale_tickets(precision):
+    """mpcd_observables_async / mpcd_observables_result: a ticket taken after a
+    step and collected several steps later (out of order) holds what
+    mpcd_observables returned right after that step, globalt included; tickets
+    never issued or older than the ring are rejected, the newest stay valid."""
+    import simcfg
+
+    cfg = simcfg.swimmer_config(16, radius=4.0, n_cilia=12, rodlength=8, seed=3, ststep=0.002)
+    s = cg.Sim(simcfg.dumps(cfg), precision=precision, ststep=0.002, seed=4)
+    e = s.engine
+    tickets, sync = [], []
+    for _ in range(5):
+        e.step()
+        tickets.append(e.observables_async())
+        sync.append(e.observables())
+    for t, want in reversed(list(zip(tickets, sync))):
+        got = e.observables_result(t)
+        for k in ("kT", "fluid_T", "n", "mass", "diss_energy", "energy_fluid", "globalt"):
+            assert got[k] == pytest.approx(want[k], rel=1e-12, abs=1e-14), k
+        assert np.abs(got["momentum"] - want["momentum"]).max() < 1e-14
+    assert len({o["globalt"] for o in sync}) == len(sync)
+    first = tickets[0]
+    latest = [e.observables_async() for _ in range(cg.OBS_RING)]
+    with pytest.raises(cg.MpcdError, match="overwritten"):
+        e.observables_result(first)
+    with pytest.raises(cg.MpcdError, match="not issued"):
+        e.observables_result(latest[-1] + 1)
+    with pytest.raises(cg.MpcdError, match="not issued"):
+        e.observables_result(-1)
+    a, b = e.observables_result(latest[0]), e.observables_result(latest[-1])
+    # the same state each time; the float32 path's sums are atomic additions,
+    # so they agree to the order of those additions
+    c = e.observables()
+    assert a["kT"] == pytest.approx(c["kT"], rel=1e-12) and b["kT"] == pytest.approx(c["kT"], rel=1e-12)
+    s.close()
+
+
 def test_unstable_md_step_reports_error_without_fault():
     """A too-large MD step lets the beads diverge; the kernels report it."""
     import simcfg
