@@ -34,6 +34,8 @@
 #ifndef MPCD_GPU_H
 #define MPCD_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -113,6 +115,11 @@ int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel)
 /* positions come back wrapped into [0, L) */
 int mpcd_get_fluid(mpcd_engine* h, long n, double* pos, double* vel);
 long mpcd_fluid_count(const mpcd_engine* h);
+/* Page-lock (and release) a caller's host buffer, e.g. the arrays given to
+ * mpcd_set_fluid / mpcd_get_fluid, so that their copies run as direct DMA
+ * rather than through staging of pageable memory; unpin before freeing it. */
+int mpcd_pin_host(mpcd_engine* h, void* p, size_t bytes);
+int mpcd_unpin_host(mpcd_engine* h, void* p);
 
 /* grid shift and simulation time */
 int mpcd_set_shift(mpcd_engine* h, const double* a3);

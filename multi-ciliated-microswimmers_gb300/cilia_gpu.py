@@ -141,6 +141,8 @@ def lib():
             "mpcd_step": (ctypes.c_int, [P, ctypes.POINTER(MpcdInject)]),
             "mpcd_run": (ctypes.c_int, [P, ctypes.c_int]),
             "mpcd_observables": (ctypes.c_int, [P, ctypes.POINTER(MpcdObs)]),
+            "mpcd_pin_host": (ctypes.c_int, [P, P, ctypes.c_size_t]),
+            "mpcd_unpin_host": (ctypes.c_int, [P, P]),
             "mpcd_observables_async": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_longlong)]),
             "mpcd_observables_result": (ctypes.c_int, [P, ctypes.c_longlong, ctypes.POINTER(MpcdObs)]),
             "mpcd_reset_diss": (ctypes.c_int, [P]),
@@ -307,12 +309,31 @@ class Engine:
         pos, vel = _f64(pos), _f64(vel)
         self._ck(lib().mpcd_set_fluid(self._h, pos.shape[0], _dp(pos), _dp(vel)), "set_fluid")
 
-    def fluid(self):
+    def fluid(self, out=None):
+        """(pos, vel) as n x 3 float64 arrays; out=(pos, vel) fills given
+        C-contiguous float64 arrays of that shape (e.g. pinned ones)."""
         n = lib().mpcd_fluid_count(self._h)
-        pos = np.zeros((n, 3))
-        vel = np.zeros((n, 3))
+        if out is None:
+            pos = np.zeros((n, 3))
+            vel = np.zeros((n, 3))
+        else:
+            pos, vel = out
+            for a in (pos, vel):
+                if a.shape != (n, 3) or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"fluid: out arrays must be C-contiguous float64 of shape ({n}, 3)")
         self._ck(lib().mpcd_get_fluid(self._h, n, _dp(pos), _dp(vel)), "get_fluid")
         return pos, vel
+
+    def pin(self, a):
+        """Page-locks a C-contiguous numpy array for direct DMA copies; unpin
+        it before it is freed."""
+        if not a.flags["C_CONTIGUOUS"] or a.nbytes == 0:
+            raise ValueError("pin: needs a non-empty C-contiguous array")
+        self._ck(lib().mpcd_pin_host(self._h, a.ctypes.data, a.nbytes), "pin_host")
+        return a
+
+    def unpin(self, a):
+        self._ck(lib().mpcd_unpin_host(self._h, a.ctypes.data), "unpin_host")
 
     @property
     def shift(self):

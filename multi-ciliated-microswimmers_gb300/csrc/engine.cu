@@ -57,6 +57,11 @@ struct mpcd_engine {
   // of a pinned ring (kObsSlot doubles: the sums, the dissipated energy, the
   // error word), its copy marked by that slot's event
   double* h_ring = nullptr;
+  double* d_ring = nullptr;  // the same ring mapped into the device (the cell-sum kernel writes it)
+  // staging of the fluid copies (6 doubles per particle), kept between calls
+  double* d_stage = nullptr;
+  size_t stage_cap = 0;  // doubles
+  unsigned* d_stage_flag = nullptr;
   cudaEvent_t ring_ev[MPCD_OBS_RING] = {};
   double ring_t[MPCD_OBS_RING] = {};       // globalt when the ticket was taken
   unsigned char ring_raw[MPCD_OBS_RING] = {};  // 1: error word copied as raw bits, 0: as a double
@@ -248,7 +253,12 @@ void free_md(MDState& m) {
 }
 
 int alloc_fluid(mpcd_engine* h, long n) {
-  if (h->p.precision == MPCD_FP64) {
+  // the same particle count: the arrays are kept (the load rewrites every one)
+  const bool f64 = h->p.precision == MPCD_FP64;
+  if (h->d_rank && (f64 ? (h->f64.id && h->f64tmp.id && h->f64.n == n && h->f64tmp.n == n)
+                        : (h->f32.id && h->f32tmp.id && h->f32.n == n && h->f32tmp.n == n)))
+    return MPCD_OK;
+  if (f64) {
     free_fluid(h->f64);
     free_fluid(h->f64tmp);
     for (FluidF64* f : {&h->f64, &h->f64tmp}) {
@@ -770,8 +780,10 @@ int mpcd_create(const mpcd_params* params, mpcd_engine** out) {
   if ((e = dalloc(&h->d_err, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_diss, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs, 16)) != cudaSuccess) return bail(e, "alloc");
-  if ((e = cudaMallocHost((void**)&h->h_ring, kObsSlot * sizeof(double) * MPCD_OBS_RING)) != cudaSuccess)
+  if ((e = cudaHostAlloc((void**)&h->h_ring, kObsSlot * sizeof(double) * MPCD_OBS_RING,
+                         cudaHostAllocMapped | cudaHostAllocPortable)) != cudaSuccess)
     return bail(e, "alloc");
+  if ((e = cudaHostGetDevicePointer((void**)&h->d_ring, h->h_ring, 0)) != cudaSuccess) return bail(e, "map");
   if ((e = dalloc(&h->d_obs_part, 7 * (size_t)kObsBlocks)) != cudaSuccess) return bail(e, "alloc");
   if ((e = dalloc(&h->d_obs_count, 1)) != cudaSuccess) return bail(e, "alloc");
   if ((e = cudaMemset(h->d_obs_count, 0, sizeof(unsigned))) != cudaSuccess) return bail(e, "alloc");
@@ -834,6 +846,8 @@ int mpcd_destroy(mpcd_engine* h) {
   cudaFree(h->d_diss);
   cudaFree(h->d_obs);
   cudaFreeHost(h->h_ring);
+  cudaFree(h->d_stage);
+  cudaFree(h->d_stage_flag);
   for (cudaEvent_t ev : h->ring_ev)
     if (ev) cudaEventDestroy(ev);
   cudaFree(h->d_obs_part);
@@ -869,27 +883,33 @@ long mpcd_fluid_count(const mpcd_engine* h) {
 }
 
 // Device staging of the caller's N x 3 float64 arrays (pos, vel): 48 bytes per
-// particle, released when the transfer is done.
+// particle and a flag word (cleared), kept by the handle and grown to the
+// largest fluid copied, so that repeated uploads and downloads allocate nothing.
 struct Staging {
   double* d = nullptr;
   unsigned* flag = nullptr;
-  ~Staging() {
-    cudaFree(d);
-    cudaFree(flag);
-  }
-  cudaError_t alloc(long n) {
-    cudaError_t e = dalloc(&d, 6 * (size_t)(n > 0 ? n : 1));
-    if (e == cudaSuccess) e = dalloc(&flag, 1);
-    if (e == cudaSuccess) e = cudaMemset(flag, 0, sizeof(unsigned));
-    return e;
-  }
 };
+int staging(mpcd_engine* h, long n, Staging& st) {
+  const size_t need = 6 * (size_t)(n > 0 ? n : 1);
+  if (need > h->stage_cap) {
+    cudaFree(h->d_stage);
+    h->d_stage = nullptr;
+    h->stage_cap = 0;
+    CK(dalloc(&h->d_stage, need));
+    h->stage_cap = need;
+  }
+  if (!h->d_stage_flag) CK(dalloc(&h->d_stage_flag, 1));
+  CK(cudaMemsetAsync(h->d_stage_flag, 0, sizeof(unsigned), h->stream));
+  st.d = h->d_stage;
+  st.flag = h->d_stage_flag;
+  return MPCD_OK;
+}
 
 int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel) {
   if (!h || n < 0 || (n > 0 && (!pos || !vel))) return fail(h, MPCD_EINVAL, "set_fluid: bad arguments");
   if (n > 0x7fffffffL) return fail(h, MPCD_EINVAL, "set_fluid: more than 2^31 - 1 particles");
   Staging st;
-  CK(st.alloc(n));
+  if (int rc_st = staging(h, n, st)) return rc_st;
   double* dpos = st.d;
   double* dvel = st.d + 3 * (size_t)n;
   if (n > 0) {
@@ -909,7 +929,7 @@ int mpcd_set_fluid(mpcd_engine* h, long n, const double* pos, const double* vel)
     h->launches += launch_load_fluid_f64(n, dpos, dvel, h->box, h->f64, h->stream);
   else
     h->launches += launch_load_fluid_f32(n, dpos, dvel, h->box, h->f32, h->stream);
-  CK(cudaStreamSynchronize(h->stream));  // the staging buffer is released on return
+  CK(cudaStreamSynchronize(h->stream));  // the staging buffer is free again on return
   h->prepared = false;
   return MPCD_OK;
 }
@@ -920,7 +940,7 @@ int mpcd_get_fluid(mpcd_engine* h, long n, double* pos, double* vel) {
   if (n != have) return fail(h, MPCD_EINVAL, "get_fluid: n does not match the fluid size");
   if (n == 0) return device_error(h);
   Staging st;
-  CK(st.alloc(n));
+  if (int rc_st = staging(h, n, st)) return rc_st;
   double* dpos = st.d;
   double* dvel = st.d + 3 * (size_t)n;
   // back into the caller's order (by particle id) and layout on the device
@@ -935,6 +955,20 @@ int mpcd_get_fluid(mpcd_engine* h, long n, double* pos, double* vel) {
   CK(cudaStreamSynchronize(h->stream));
   if (bad) return fail(h, MPCD_EDEVICE, "particle id out of range");
   return device_error(h);
+}
+
+// Page-locks a caller's buffer so that the fluid and bead copies of this
+// library run as direct DMA instead of through the driver's staging of
+// pageable memory (no counterpart in the reference, which has no device).
+int mpcd_pin_host(mpcd_engine* h, void* p, size_t bytes) {
+  if (!h || !p || bytes == 0) return MPCD_EINVAL;
+  CK(cudaHostRegister(p, bytes, cudaHostRegisterPortable));
+  return MPCD_OK;
+}
+int mpcd_unpin_host(mpcd_engine* h, void* p) {
+  if (!h || !p) return MPCD_EINVAL;
+  CK(cudaHostUnregister(p));
+  return MPCD_OK;
 }
 
 int mpcd_set_shift(mpcd_engine* h, const double* a3) {
@@ -1279,10 +1313,10 @@ int mpcd_observables_async(mpcd_engine* h, long long* ticket) {
   if (!h->ring_ev[slot]) CK(cudaEventCreateWithFlags(&h->ring_ev[slot], cudaEventDisableTiming));
   if (h->p.precision == MPCD_FP64 && h->prepared) {
     // the cell sums of the last binning (the state has not changed since: every
-    // setter clears `prepared`) hold the totals; one kernel, one read-back
+    // setter clears `prepared`) hold the totals; one kernel, which writes the
+    // ten results straight into the mapped ring slot
     h->launches += launch_observables_cells_f64(h->c64, h->md, h->p.bead_mass, h->d_diss, h->d_err, h->d_obs_part,
-                                                h->d_obs_count, h->d_obs, h->stream);
-    CK(cudaMemcpyAsync(o, h->d_obs, 10 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+                                                h->d_obs_count, h->d_ring + (size_t)slot * kObsSlot, h->stream);
     h->ring_raw[slot] = 0;
   } else {
     CK(cudaMemsetAsync(h->d_obs, 0, 8 * sizeof(double), h->stream));

@@ -498,7 +498,8 @@ __global__ void k_observables_f64(FluidF64 f, MDState m, double bead_mass, doubl
 // thousand) is summed beside it to split off the fluid's.  Per-block
 // partials, added in block order by the last block to finish (no memset, no
 // float atomics into the result); out = {P x, y, z, sum m v^2, n, mass,
-// fluid sum v^2, fluid n, dissipated energy, error bits}.
+// fluid sum v^2, fluid n, dissipated energy, error bits}, device memory or a
+// mapped page-locked host slot (then no copy follows the kernel).
 __global__ void k_observables_cells_f64(CellsF64 c, MDState m, double bead_mass, const double* diss,
                                         const unsigned* err, double* part, unsigned* counter, double* out) {
   double px = 0, py = 0, pz = 0, e = 0, nf = 0, nb = 0, eb = 0;
@@ -518,26 +519,26 @@ __global__ void k_observables_cells_f64(CellsF64 c, MDState m, double bead_mass,
     const double vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
     eb += bead_mass * (vx * vx + vy * vy + vz * vz);
   }
-  const double vals[7] = {px, py, pz, e, nf, nb, eb};
+  double vals[7] = {px, py, pz, e, nf, nb, eb};
   __shared__ bool last;
-#pragma unroll
-  for (int k = 0; k < 7; ++k) {
-    const double t = block_sum_f64(vals[k]);
-    if (threadIdx.x == 0) part[7 * blockIdx.x + k] = t;
-  }
-  if (threadIdx.x == 0) {
+  __shared__ double tot[7];
+  block_sum7_f64(vals, tot);  // tot[k] for every thread after it
+  if (threadIdx.x < 7) {
+    part[7 * blockIdx.x + threadIdx.x] = tot[threadIdx.x];
     __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
   if (!last) return;
-  double tot[7];
+  __threadfence();
 #pragma unroll
   for (int k = 0; k < 7; ++k) {
     double v = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(part + 7 * b + k);
-    tot[k] = block_sum_f64(v);
+    vals[k] = v;
   }
+  block_sum7_f64(vals, tot);
   if (threadIdx.x == 0) {
     out[0] = tot[0];
     out[1] = tot[1];

@@ -259,6 +259,18 @@ def test_fluid_upload_download_round_trip(precision):
         e.set_fluid(bad, vel)
     p2, v2 = e.fluid()
     assert np.array_equal(p2, p) and np.array_equal(v2, v)
+    # the same copies from and into page-locked caller buffers
+    pin_pos, pin_vel = pos.copy(), vel.copy()
+    outp, outv = np.empty_like(pos), np.empty_like(vel)
+    for a in (pin_pos, pin_vel, outp, outv):
+        e.pin(a)
+    e.set_fluid(pin_pos, pin_vel)
+    e.fluid(out=(outp, outv))
+    assert np.array_equal(outp, p) and np.array_equal(outv, v)
+    for a in (pin_pos, pin_vel, outp, outv):
+        e.unpin(a)
+    with pytest.raises(ValueError):
+        e.fluid(out=(np.empty((n, 3), dtype=np.float32), outv))
 
 
 def test_observables_from_cell_sums_match_particle_sums():
