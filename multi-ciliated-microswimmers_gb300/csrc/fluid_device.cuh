@@ -37,15 +37,16 @@ __device__ __forceinline__ double block_sum_f64(double v) {
   return r;  // valid in thread 0
 }
 
-// Seven sums over the block at once (blockDim.x a multiple of 32): shuffles
-// within each warp, then one shared-memory round adds the warps in warp order;
-// out (shared) holds the totals for every thread on return.
-__device__ __forceinline__ void block_sum7_f64(const double (&v)[7], double* out) {
-  __shared__ double red[7][32];
+// N sums over the block at once (blockDim.x a multiple of 32, N <= 32):
+// shuffles within each warp, then one shared-memory round adds the warps in
+// warp order; out (shared) holds the totals for every thread on return.
+template <int N>
+__device__ __forceinline__ void block_sums_f64(const double (&v)[N], double* out) {
+  __shared__ double red[N][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double w[7];
+  double w[N];
 #pragma unroll
-  for (int k = 0; k < 7; ++k) {
+  for (int k = 0; k < N; ++k) {
     double x = v[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -54,10 +55,10 @@ __device__ __forceinline__ void block_sum7_f64(const double (&v)[7], double* out
   __syncthreads();  // earlier readers of red and out are done
   if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < 7; ++k) red[k][wid] = w[k];
+    for (int k = 0; k < N; ++k) red[k][wid] = w[k];
   }
   __syncthreads();
-  if (threadIdx.x < 7) {
+  if (threadIdx.x < N) {
     double s = 0.0;
     for (int i = 0; i < nw; ++i) s += red[threadIdx.x][i];
     out[threadIdx.x] = s;

@@ -500,10 +500,35 @@ __global__ void k_observables_f64(FluidF64 f, MDState m, double bead_mass, doubl
 // float atomics into the result); out = {P x, y, z, sum m v^2, n, mass,
 // fluid sum v^2, fluid n, dissipated energy, error bits}, device memory or a
 // mapped page-locked host slot (then no copy follows the kernel).
-__global__ void k_observables_cells_f64(CellsF64 c, MDState m, double bead_mass, const double* diss,
-                                        const unsigned* err, double* part, unsigned* counter, double* out) {
-  double px = 0, py = 0, pz = 0, e = 0, nf = 0, nb = 0, eb = 0;
-  for (long cid = (long)blockIdx.x * blockDim.x + threadIdx.x; cid < c.ncell; cid += (long)gridDim.x * blockDim.x) {
+// GB300 runs float64 adds at a small fraction of its float32 rate, so the
+// counts are summed as integers and the grid is one block per SM (fewer
+// block reductions); four cells' loads are in flight per thread.
+__global__ void __launch_bounds__(kThreads) k_observables_cells_f64(CellsF64 c, MDState m, double bead_mass,
+                                                                    const double* diss, const unsigned* err,
+                                                                    double* part, unsigned* counter, double* out) {
+  double px = 0, py = 0, pz = 0, e = 0, eb = 0;
+  uint32_t nf = 0, nb = 0;
+  const long stride = (long)gridDim.x * blockDim.x;
+  long cid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; cid + 3 * stride < c.ncell; cid += 4 * stride) {
+    uint32_t w[4];
+    double4 s[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) w[u] = c.cnt[cid + u * stride];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s[u] = c.sum[cid + u * stride];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (w[u] != 0) {
+        px += s[u].x;
+        py += s[u].y;
+        pz += s[u].z;
+        e += s[u].w;
+        nf += (uint32_t)cnt_fluid(w[u]);
+        nb += (uint32_t)cnt_beads(w[u]);
+      }
+  }
+  for (; cid < c.ncell; cid += stride) {
     const uint32_t w = c.cnt[cid];
     if (w == 0) continue;
     const double4 s = c.sum[cid];
@@ -511,20 +536,42 @@ __global__ void k_observables_cells_f64(CellsF64 c, MDState m, double bead_mass,
     py += s.y;
     pz += s.z;
     e += s.w;
-    nf += (double)cnt_fluid(w);
-    nb += (double)cnt_beads(w);
+    nf += (uint32_t)cnt_fluid(w);
+    nb += (uint32_t)cnt_beads(w);
   }
-  for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += (long)gridDim.x * blockDim.x) {
+  for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < m.nslots; s += stride) {
     if (m.moves[s] != 1) continue;
     const double vx = m.vx[s], vy = m.vy[s], vz = m.vz[s];
     eb += bead_mass * (vx * vx + vy * vy + vz * vz);
   }
-  double vals[7] = {px, py, pz, e, nf, nb, eb};
+  // the counts as integers up to the block total, then exact in float64
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nf += __shfl_xor_sync(0xffffffffu, nf, o);
+    nb += __shfl_xor_sync(0xffffffffu, nb, o);
+  }
+  __shared__ uint32_t s_cnt[2][32];
+  if ((threadIdx.x & 31) == 0) {
+    s_cnt[0][threadIdx.x >> 5] = nf;
+    s_cnt[1][threadIdx.x >> 5] = nb;
+  }
+  const double v5[5] = {px, py, pz, e, eb};
   __shared__ bool last;
+  __shared__ double t5[5];
   __shared__ double tot[7];
-  block_sum7_f64(vals, tot);  // tot[k] for every thread after it
-  if (threadIdx.x < 7) {
-    part[7 * blockIdx.x + threadIdx.x] = tot[threadIdx.x];
+  block_sums_f64<5>(v5, t5);  // t5 for every thread after it (its barriers order s_cnt too)
+  if (threadIdx.x < 7) {  // partial k: P x, y, z, sum m v^2, fluid n, bead n, bead sum m v^2
+    double r;
+    if (threadIdx.x < 4) {
+      r = t5[threadIdx.x];
+    } else if (threadIdx.x == 6) {
+      r = t5[4];
+    } else {
+      uint32_t t = 0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += s_cnt[threadIdx.x - 4][i];
+      r = (double)t;
+    }
+    part[7 * blockIdx.x + threadIdx.x] = r;
     __threadfence();
   }
   __syncthreads();
@@ -532,13 +579,14 @@ __global__ void k_observables_cells_f64(CellsF64 c, MDState m, double bead_mass,
   __syncthreads();
   if (!last) return;
   __threadfence();
+  double vals[7];
 #pragma unroll
   for (int k = 0; k < 7; ++k) {
     double v = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(part + 7 * b + k);
     vals[k] = v;
   }
-  block_sum7_f64(vals, tot);
+  block_sums_f64<7>(vals, tot);
   if (threadIdx.x == 0) {
     out[0] = tot[0];
     out[1] = tot[1];
@@ -1274,7 +1322,8 @@ int launch_bin_beads_f64(const MDState& m, const CellsF64& c, const StepArgs& a,
 int launch_observables_cells_f64(const CellsF64& c, const MDState& m, double bead_mass, const double* diss,
                                  const unsigned* err, double* part, unsigned* counter, double* out, cudaStream_t s) {
   const long n = c.ncell > m.nslots ? c.ncell : m.nslots;
-  const int g = grid_for(n) < kObsBlocks ? grid_for(n) : kObsBlocks;
+  const int g1 = grid_for(n, kThreads, 1);  // at most one block per SM
+  const int g = g1 < kObsBlocks ? g1 : kObsBlocks;
   k_observables_cells_f64<<<g, kThreads, 0, s>>>(c, m, bead_mass, diss, err, part, counter, out);
   return 1;
 }
