@@ -105,42 +105,58 @@ def poiseuille_viscosity(profile, g, rho=10.0, zmin=1.5, zmax=None):
 
 
 def test_poiseuille_viscosity_matches_oracle():
+    """One run's viscosity scatters by about 2 % (sd over seeds, this box and
+    length: 0.19 of 8.8), so the GPU figure is the mean of four seeds and the
+    oracle's of two runs; they agree within 8 % (about 4 sd of the
+    difference)."""
     L = (8, 8, 14)
     grav, warm, samples, every = 0.01, 600, 1000, 5
     nbin = L[2] - 1
-    # GPU (float32 split: the production path for long runs)
     o = OracleSim(L, tstep=0.1, ststep=0.002, seed=21)
     o.init_shift()
     o.fluid_create()
     p0, v0 = o.fluid()
-    e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=cg.MPCD_FP32, walls=cg.WALLS_NOSLIP, gravity=grav, seed=9)
-    e.set_fluid(p0, v0)
-    e.run(warm)
-    prof = np.zeros(nbin)
-    cnt = np.zeros(nbin)
-    for _ in range(samples):
-        e.run(every)
-        p, v = e.fluid()
-        b = np.clip(p[:, 2].astype(int), 0, nbin - 1)
-        prof += np.bincount(b, weights=v[:, 0], minlength=nbin)
-        cnt += np.bincount(b, minlength=nbin)
-    eta_gpu = poiseuille_viscosity(prof / cnt, grav)
-    # oracle, same set-up and length
-    o.set_walls(1)
-    o.set_gravity(grav, 0.0)
-    o.set_threads(8)
-    o.init_bins()
-    for _ in range(warm):
-        o.step()
-    prof[:] = 0
-    cnt[:] = 0
-    for _ in range(samples):
-        for _ in range(every):
+    # GPU (float32 split: the production path for long runs)
+    etas_gpu = []
+    for seed in (9, 10, 11, 12):
+        e = cg.Engine(L, tstep=0.1, ststep=0.002, precision=cg.MPCD_FP32, walls=cg.WALLS_NOSLIP, gravity=grav,
+                      seed=seed)
+        e.set_fluid(p0, v0)
+        e.run(warm)
+        prof = np.zeros(nbin)
+        cnt = np.zeros(nbin)
+        for _ in range(samples):
+            e.run(every)
+            p, v = e.fluid()
+            b = np.clip(p[:, 2].astype(int), 0, nbin - 1)
+            prof += np.bincount(b, weights=v[:, 0], minlength=nbin)
+            cnt += np.bincount(b, minlength=nbin)
+        etas_gpu.append(poiseuille_viscosity(prof / cnt, grav))
+        e.close()
+    eta_gpu = float(np.mean(etas_gpu))
+    # oracle, same set-up and length, two runs
+    etas_orc = []
+    for run in range(2):
+        if run:
+            o = OracleSim(L, tstep=0.1, ststep=0.002, seed=22)
+            o.init_shift()
+            o.fluid_create()
+        o.set_walls(1)
+        o.set_gravity(grav, 0.0)
+        o.set_threads(8)
+        o.init_bins()
+        for _ in range(warm):
             o.step()
-        p, v = o.fluid()
-        b = np.clip(p[:, 2].astype(int), 0, nbin - 1)
-        prof += np.bincount(b, weights=v[:, 0], minlength=nbin)
-        cnt += np.bincount(b, minlength=nbin)
-    eta_orc = poiseuille_viscosity(prof / cnt, grav)
+        prof = np.zeros(nbin)
+        cnt = np.zeros(nbin)
+        for _ in range(samples):
+            for _ in range(every):
+                o.step()
+            p, v = o.fluid()
+            b = np.clip(p[:, 2].astype(int), 0, nbin - 1)
+            prof += np.bincount(b, weights=v[:, 0], minlength=nbin)
+            cnt += np.bincount(b, minlength=nbin)
+        etas_orc.append(poiseuille_viscosity(prof / cnt, grav))
+    eta_orc = float(np.mean(etas_orc))
     assert 2.0 < eta_orc < 20.0
-    assert abs(eta_gpu - eta_orc) < 0.08 * eta_orc, (eta_gpu, eta_orc)
+    assert abs(eta_gpu - eta_orc) < 0.08 * eta_orc, (etas_gpu, etas_orc)
