@@ -45,6 +45,7 @@ Multi-GPU: replicas only - every rank advances its own independent box.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -268,23 +269,30 @@ def run_e2e(args):
         eng.step()
         eng.observables_result(eng.observables_async())
     eng.fluid(out=(pout, vout))
-    t0 = time.perf_counter()
-    eng.set_fluid(pos, vel)
-    t1 = time.perf_counter()
-    # each step's observables are enqueued behind it and all are collected
-    # inside the window: the read-backs are all done, the host just does not
-    # stall the next step on them
-    tickets = []
-    for _ in range(E2E_STEPS):
-        eng.step()
-        tickets.append(eng.observables_async())
-    obs = [eng.observables_result(t) for t in tickets]
-    t2 = time.perf_counter()
+    # no garbage-collector pass inside the window (after the other bench legs
+    # one took milliseconds of host time)
+    gc.collect()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
+        eng.set_fluid(pos, vel)
+        t1 = time.perf_counter()
+        # each step's observables are enqueued behind it and all are collected
+        # inside the window: the read-backs are all done, the host just does
+        # not stall the next step on them
+        tickets = []
+        for _ in range(E2E_STEPS):
+            eng.step()
+            tickets.append(eng.observables_async())
+        obs = [eng.observables_result(t) for t in tickets]
+        t2 = time.perf_counter()
+        p, v = eng.fluid(out=(pout, vout))
+        bp, bv = sim.beads()
+        t3 = time.perf_counter()
+    finally:
+        gc.enable()
     if not all(np.isfinite(o["kT"]) for o in obs):
         raise RuntimeError("non-finite observables in the end-to-end window")
-    p, v = eng.fluid(out=(pout, vout))
-    bp, bv = sim.beads()
-    t3 = time.perf_counter()
     for a in pinned:
         eng.unpin(a)
     sim.close()
