@@ -717,6 +717,11 @@ def main():
     }
     if g["md_arith"] is not None:
         line["md_arith"] = MD_ARITH_NAMES[g["md_arith"]]
+    # the end-to-end window before the other legs: after the batch, serving
+    # and 128^3 legs in the same process its 126 MB download took 6-12 ms
+    # instead of 1.3 ms; and before the CPU baseline, whose OpenMP threads keep
+    # spinning for a while after it and slow the host side of the copies
+    e = run_e2e(args) if not args.no_extra else None
     # the long nested records first, the short headline figures last (the end
     # of the line is what a truncated log keeps)
     if not args.no_ensemble and args.gpus == 1:
@@ -737,10 +742,7 @@ def main():
                              "md_ms_per_step": f["kernels"]["md"][0] / max(f["prof_steps"], 1), "steps": k,
                              "md_arith": MD_ARITH_NAMES[4]}
     line["roofline"] = roofline(g["nf"], g["kernels"], args.precision)
-    if not args.no_extra:
-        # before the CPU baseline: its OpenMP threads keep spinning for a while
-        # after it and slow the host side of the copies
-        e = run_e2e(args)
+    if e is not None:
         line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                        "d2h_bytes_per_step": e["d2h"], "steps": E2E_STEPS,
                        "steady_value": e["steady"], "steady_ms_per_step": e["step_ms"],
