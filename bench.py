@@ -263,7 +263,7 @@ def run_e2e(args):
     pout, vout = np.empty_like(pos), np.empty_like(vel)
     pinned = [eng.pin(a) for a in (pos, vel, pout, vout)]
     # one untimed pass of the same calls (first-use costs of the host pages
-    # and the driver's copy path stay out of the window)
+    # and the CUDA driver's copy path stay out of the window)
     eng.set_fluid(pos, vel)
     for _ in range(3):
         eng.step()

@@ -958,7 +958,7 @@ int mpcd_get_fluid(mpcd_engine* h, long n, double* pos, double* vel) {
 }
 
 // Page-locks a caller's buffer so that the fluid and bead copies of this
-// library run as direct DMA instead of through the driver's staging of
+// library run as direct DMA instead of through the CUDA driver's staging of
 // pageable memory (no counterpart in the reference, which has no device).
 int mpcd_pin_host(mpcd_engine* h, void* p, size_t bytes) {
   if (!h || !p || bytes == 0) return MPCD_EINVAL;
