@@ -165,7 +165,7 @@ def describe(name, nf, nb, precision):
     elif name == "swimmer128":
         geo = "128^3 cells x 10 fluid, Clami R=16 with 400 cilia (3x20 beads), 50 MD substeps"
     else:
-        geo = f"{name}: periodic fluid, no swimmer"
+        geo = "32^3 cells x 10 fluid, periodic, no swimmer"
     return f"{name}: {geo}; {nf} fluid + {nb} beads; {precision}"
 
 
