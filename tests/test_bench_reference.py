@@ -30,3 +30,23 @@ def test_reference_arm_other_ranks_print_nothing():
                         "--steps", "2", "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=REPO,
                        env=env)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_roofline_uses_the_algorithmic_bytes_and_the_measured_peak():
+    """frac = particles x 112 B (float64: read + write of the reference's
+    56 B state) / the fluid kernel's average launch time / MEASURED_PEAKS
+    hbm_gbs; the build's own 96 B layout is reported beside it."""
+    sys.path.insert(0, REPO)
+    import bench
+
+    nf = 2621440
+    kernels = {"fluid": (1.34, 10), "cell": (0.5, 10), "md": (2.2, 10), "bead": (0.0, 0), "sort": (0.0, 0)}
+    r = bench.roofline(nf, kernels, "fp64")
+    hbm, kind = bench.peaks()
+    achieved = nf * 112 / 0.134e-3 / 1e9
+    assert abs(r["achieved"] - achieved) < 1e-6 * achieved and abs(r["frac"] - achieved / hbm) < 1e-9
+    assert r["peak"] == hbm and r["peak_kind"] == kind and r["bound"] == "hbm" and r["unit"] == "GB/s"
+    assert abs(r["frac_state_bytes"] - nf * 96 / 0.134e-3 / 1e9 / hbm) < 1e-9
+    assert r["traffic"] == bench.TRAFFIC_B_PER_PARTICLE["fp64"] * nf
+    r32 = bench.roofline(nf, kernels, "fp32")
+    assert abs(r32["achieved"] - nf * 64 / 0.134e-3 / 1e9) < 1e-6 * r32["achieved"]
