@@ -1299,8 +1299,8 @@ int mpcd_reset_diss(mpcd_engine* h) {
 // and returns at once; no counterpart in the reference (MPCD::debug,
 // src/libcilia/mpcd.cpp:404-467, sums and prints in one go).  The sums land in
 // ring slot ticket % MPCD_OBS_RING; every later call on the handle is ordered
-// after their copy on the stream, so the next step runs while the host has not
-// yet read them.
+// after the kernel (and copies) that write them on the stream, so the next step
+// runs while the host has not yet read them.
 int mpcd_observables_async(mpcd_engine* h, long long* ticket) {
   if (!h || !ticket) return MPCD_EINVAL;
   if (h->md_dirty && h->nb) {
@@ -1329,6 +1329,7 @@ int mpcd_observables_async(mpcd_engine* h, long long* ticket) {
     CK(cudaMemcpyAsync(o + 9, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
     h->ring_raw[slot] = 1;
   }
+  if (int rc = check_launch(h, "observables")) return rc;  // no ticket for a launch that failed
   CK(cudaEventRecord(h->ring_ev[slot], h->stream));
   h->ring_t[slot] = h->globalt;
   h->obs_next = t + 1;
