@@ -76,6 +76,16 @@ int cilia_sim_writedata(cilia_sim* s, int flags);
 int cilia_batch_add_cfg(mpcd_batch* b, const char* cfg, int is_text, const cilia_options* opt, int* replica);
 /* writes the cfg back with the current globalt (src/main.cpp:95-96) */
 int cilia_sim_write_cfg(cilia_sim* s, const char* path);
+/* The initial state the Simulation's constructor (src/simulation.cpp:19-35)
+ * builds from a sim.cfg, on the host only and without a GPU: the grid shift
+ * (MPCD::MPCD), the md_objects' beads (Sphere::create, Cilia::create,
+ * Clami::attach) and, with opt->create_fluid, the fluid of Fluid::create
+ * (src/libcilia/fluid.cpp:55-98) or fluid_n.dat.  sizes = {fluid particles,
+ * beads, one-sided springs}: call with every array NULL to get them, then
+ * with arrays of those sizes (n x 3 each; any may stay NULL).  Errors come
+ * back through cilia_sim_last_error(NULL). */
+int cilia_cfg_host_state(const char* cfg, int is_text, const cilia_options* opt, long sizes[3], double* shift3,
+                         double* fluid_pos, double* fluid_vel, double* bead_pos, double* bead_vel);
 
 #ifdef __cplusplus
 }

@@ -231,6 +231,8 @@ def lib():
             "cilia_sim_save": (ctypes.c_int, [P]),
             "cilia_sim_writedata": (ctypes.c_int, [P, ctypes.c_int]),
             "cilia_sim_write_cfg": (ctypes.c_int, [P, ctypes.c_char_p]),
+            "cilia_cfg_host_state": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(CiliaOptions),
+                                                    ctypes.POINTER(ctypes.c_long), _DP, _DP, _DP, _DP, _DP]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -474,6 +476,27 @@ class Engine:
         self._ck(lib().mpcd_md_layout(self._h, a), "md_layout")
         keys = ("cluster", "lanes", "tile", "ntiles", "nslots", "nsprings", "hmax", "arith")
         return dict(zip(keys, list(a)))
+
+
+def cfg_host_state(cfg, *, is_text=True, seed=1, create_fluid=True, read_files=False):
+    """The initial state a sim.cfg describes, built on the host only (no GPU):
+    dict(shift, fluid_pos, fluid_vel, bead_pos, bead_vel, nsprings)."""
+    o = CiliaOptions(MPCD_FP64, 0, seed, 0.0, int(create_fluid), int(read_files), WALLS_NONE, 0.0, 5.0, 0, 0)
+    text = cfg.encode() if isinstance(cfg, str) else cfg
+    sizes = (ctypes.c_long * 3)()
+
+    def call(*arrays):
+        rc = lib().cilia_cfg_host_state(text, int(is_text), ctypes.byref(o), sizes, *arrays)
+        if rc:
+            msg = lib().cilia_sim_last_error(None)
+            raise MpcdError(f"cilia_cfg_host_state failed ({rc}): {msg.decode() if msg else ''}")
+
+    call(None, None, None, None, None)
+    nf, nb = sizes[0], sizes[1]
+    shift = np.zeros(3)
+    fp, fv, bp, bv = np.zeros((nf, 3)), np.zeros((nf, 3)), np.zeros((nb, 3)), np.zeros((nb, 3))
+    call(_dp(shift), _dp(fp), _dp(fv), _dp(bp), _dp(bv))
+    return dict(shift=shift, fluid_pos=fp, fluid_vel=fv, bead_pos=bp, bead_vel=bv, nsprings=sizes[2])
 
 
 class Sim:

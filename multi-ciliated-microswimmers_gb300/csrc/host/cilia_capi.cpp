@@ -75,6 +75,35 @@ int cilia_batch_add_cfg(mpcd_batch* b, const char* cfg, int is_text, const cilia
   });
 }
 
+int cilia_cfg_host_state(const char* cfg, int is_text, const cilia_options* opt, long sizes[3], double* shift3,
+                         double* fluid_pos, double* fluid_vel, double* bead_pos, double* bead_vel) {
+  if (!cfg || !sizes) return MPCD_EINVAL;
+  return guarded(g_create_error, [&]() {
+    libconfig::Config c;
+    if (is_text)
+      c.readString(cfg);
+    else
+      c.readFile(cfg);
+    cilia::SimOptions so = to_options(opt);
+    so.host_only = 1;
+    cilia::Simulation sim(c.getRoot(), so);
+    const cilia::HostSystem& h = sim.host;
+    const long nf = (long)(h.fpos.size() / 3), nb = (long)(h.bpos.size() / 3);
+    // with arrays: they must be the sizes the caller was told
+    if ((fluid_pos || fluid_vel || bead_pos || bead_vel) && (sizes[0] != nf || sizes[1] != nb))
+      throw std::runtime_error("cilia_cfg_host_state: sizes do not match the system (ask with NULL arrays first)");
+    sizes[0] = nf;
+    sizes[1] = nb;
+    sizes[2] = (long)h.springs.size();
+    if (shift3) std::memcpy(shift3, h.a, sizeof h.a);
+    if (fluid_pos) std::memcpy(fluid_pos, h.fpos.data(), h.fpos.size() * sizeof(double));
+    if (fluid_vel) std::memcpy(fluid_vel, h.fvel.data(), h.fvel.size() * sizeof(double));
+    if (bead_pos) std::memcpy(bead_pos, h.bpos.data(), h.bpos.size() * sizeof(double));
+    if (bead_vel) std::memcpy(bead_vel, h.bvel.data(), h.bvel.size() * sizeof(double));
+    return MPCD_OK;
+  });
+}
+
 int cilia_sim_create(const char* cfg, int is_text, const cilia_options* opt, cilia_sim** out) {
   if (!cfg || !out) return MPCD_EINVAL;
   *out = nullptr;
