@@ -55,3 +55,19 @@ def test_cfg_errors_come_back_as_messages():
         cg.cfg_host_state("sizex = 8; sizey = 8; sizez = 8;", create_fluid=False)
     with pytest.raises(cg.MpcdError, match="Parse error"):
         cg.cfg_host_state("sizex = ;", create_fluid=False)
+
+
+def test_libconfig_syntax_variants_build_the_same_system():
+    """The cfg reader takes libconfig's syntax variants as the reference's
+    libconfig++ does: ':' for '=', '//' and '/* */' comments, exponents, a
+    trailing comma-free list, whitespace anywhere; the system is the same."""
+    text = open(f"{GOLDEN}/cases/objects8.cfg").read()
+    v = text.replace("springconstant = 2000.0;", "springconstant : 2.0e3; // the sphere's springs")
+    v = v.replace("rodlength = 5;", "/* five\n   sections */ rodlength=5 ;")
+    v = v.replace("position = [ 5.0, 5.0, 3.0 ];", "position:[5.0,5.0,\n 3.0];")
+    assert v != text
+    a = cg.cfg_host_state(text, seed=3, create_fluid=True)
+    b = cg.cfg_host_state(v, seed=3, create_fluid=True)
+    for k in ("shift", "fluid_pos", "fluid_vel", "bead_pos", "bead_vel"):
+        assert np.array_equal(a[k], b[k]), k
+    assert a["nsprings"] == b["nsprings"]
